@@ -1,0 +1,129 @@
+/*
+ * jacobi2000 GB300 engine: C ABI.
+ *
+ * A drop-in for the reference engine crate's model API. Each entry point
+ * names the reference interface it replaces. Conventions:
+ *   - plain pointers and sizes, caller-owned buffers; no C++ or framework types;
+ *   - every function returns a jc_status; nothing panics or aborts across the
+ *     boundary; jc_last_error() gives a thread-local message for the last
+ *     failure on the calling thread;
+ *   - states are normalized f32 [channels, ny, nx] (channel 0 = h, 1 = u,
+ *     2 = v), the layout of crates/engine/src/norm.rs:1-3;
+ *   - a model handle owns one CUDA stream; calls on one handle must not run
+ *     concurrently from several threads (use one handle per thread).
+ */
+#ifndef JACOBI2000_H
+#define JACOBI2000_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. 1-4 mirror lean_runtime::Error::{NoAdapter/NoDevice, Limit,
+ * Map, Poll} (crates/lean-runtime/src/error.rs:6-13); the rest replace the
+ * reference's panics on bad checkpoints (weights.rs:39,52-54, config.rs:71). */
+typedef enum {
+    JC_OK = 0,
+    JC_NO_DEVICE = 1,       /* no CUDA device, or not an sm_103 device */
+    JC_LIMIT = 2,           /* a size exceeds a kernel limit */
+    JC_MAP = 3,             /* a host<->device copy failed */
+    JC_POLL = 4,            /* waiting for the device failed */
+    JC_BAD_CHECKPOINT = 5,  /* safetensors / config.json malformed or missing a tensor */
+    JC_BAD_SHAPE = 6,       /* grid not divisible by the patch, shapes inconsistent */
+    JC_OVER_BUDGET = 7,     /* admission refused: device memory budget */
+    JC_DEVICE_TIMEOUT = 8,  /* a device-side wait hit its iteration limit */
+    JC_BAD_ARGUMENT = 9,    /* null pointer, negative count, unknown flag */
+    JC_CUDA_ERROR = 10,     /* any other CUDA runtime error */
+    JC_NOT_FOUND = 11       /* unknown request id */
+} jc_status;
+
+/* Arithmetic of a model's kernels. FP32: f32 weights and activations on CUDA
+ * cores (the reference's arithmetic). BF16: bf16 weights and activations on
+ * the tcgen05 tensor cores with f32 accumulation; LayerNorm statistics,
+ * softmax, residual stream and the projection scalars stay f32/f64. */
+typedef enum { JC_FP32 = 0, JC_BF16 = 1 } jc_precision;
+
+/* Tick-loop flags (crates/engine-cli/src/eval.rs:144-157 order: step, mass
+ * projection, energy projection). */
+#define JC_PROJECT_MASS   1u
+#define JC_PROJECT_ENERGY 2u
+
+typedef struct jc_model jc_model;
+
+/* config.json as read by crates/engine/src/config.rs:43-67. mask_kind 0 =
+ * Full, 1 = Stencil{mask_radius, mask_dilation}. */
+typedef struct {
+    int32_t nx, ny, patch, channels, dim, layers, heads;
+    int32_t head_dim, ff_inner, meta_dim;
+    int32_t mask_kind, mask_radius, mask_dilation;
+    float norm_mean[3], norm_std[3], norm_depth;
+    float dx, dt, g, depth, nu, energy_r_max;
+} jc_config;
+
+/* Replaces engine::Model::from_bytes + Model::to_gpu (crates/engine/src/lib.rs:45-50,
+ * 64-67; gpu.rs:212-218): parse a model.safetensors image and config.json text,
+ * upload the weights in the requested precision. */
+jc_status jc_model_create(const uint8_t* safetensors, size_t safetensors_len,
+                          const char* config_json, int32_t precision,
+                          jc_model** out);
+
+/* Replaces dropping a GpuModel (gpu.rs:199-209). Null is accepted. */
+void jc_model_destroy(jc_model* m);
+
+/* Replaces engine::Model::cfg / GpuModel::cfg (lib.rs:30-33, gpu.rs:426-428). */
+jc_status jc_model_config(const jc_model* m, jc_config* out);
+
+/* Replaces engine::meta_of(&cfg.params()) (solver_meta.rs:9-11): the
+ * [ln dx, ln dt, ln g, ln depth, ln(nu + 1e-6)] conditioning vector. */
+jc_status jc_meta_of(const jc_model* m, float* meta_out);
+
+/* Replaces Model::forward / GpuModel::forward (lib.rs:53-55, gpu.rs:374-424):
+ * host state [channels, ny, nx] and meta [meta_dim] in, the predicted
+ * increment out (same shape as the state). Blocks until done. */
+jc_status jc_forward(jc_model* m, const float* state, const float* meta, float* increment);
+
+/* Replaces Model::step / GpuModel::step (lib.rs:58-60, gpu.rs:431-437):
+ * next = state + forward(state, meta). */
+jc_status jc_step(jc_model* m, const float* state, const float* meta, float* next_state);
+
+/* Replaces the tick loops of crates/engine-cli/src/main.rs:117-121 and
+ * eval.rs:144-157 (and, on a reverse checkpoint, the web demo's rewind,
+ * crates/web/src/lib.rs:383-409): `ticks` steps from x0, each followed by the
+ * projections `flags` selects, done on the device with f64 compensated sums
+ * (mass target = box mean of x0's channel 0; energy bound = previous tick's
+ * energy times energy_r_max). Writes the final state to `final_state`; when
+ * `trajectory` is non-null it receives ticks+1 states (x0 first); when
+ * `energies` is non-null it receives ticks+1 energies (f64). */
+jc_status jc_rollout(jc_model* m, const float* x0, const float* meta, int32_t ticks,
+                     uint32_t flags, float* final_state, float* trajectory,
+                     double* energies);
+
+/* Device-resident forms of jc_forward / jc_rollout for callers that keep
+ * state in device memory: all pointers are device pointers, `stream` is a
+ * cudaStream_t (null = the model's own stream). They enqueue and return. */
+jc_status jc_forward_device(jc_model* m, const float* d_state, const float* d_meta,
+                            float* d_increment, void* stream);
+jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta,
+                            int32_t ticks, uint32_t flags, float* d_final,
+                            double* d_energies, void* stream);
+
+/* Host-side projections, engine::project (crates/engine/src/project.rs:22-54),
+ * with f64 compensated sums. n = cells per channel; x is [3, n]. */
+double jc_mass(const float* x, int64_t n);
+double jc_energy(const float* x, const jc_config* cfg, int64_t n);
+void   jc_project_mass(float* x, double target, int64_t n);
+void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int64_t n);
+
+/* Thread-local description of the last failure on this thread ("" if none). */
+const char* jc_last_error(void);
+
+/* Library version string. */
+const char* jc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

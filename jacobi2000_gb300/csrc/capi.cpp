@@ -1,0 +1,166 @@
+// The extern "C" surface (include/jacobi2000.h). Every entry point catches
+// all exceptions and returns a status; the message is kept per thread.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "../../include/jacobi2000.h"
+#include "runtime.hpp"
+
+struct jc_model {
+    jc::Model* m;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+jc_status fail(jc_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+template <class F>
+jc_status guard(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return JC_OK;
+    } catch (const jc::Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(JC_OVER_BUDGET, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(JC_CUDA_ERROR, e.what());
+    } catch (...) {
+        return fail(JC_CUDA_ERROR, "unknown error");
+    }
+}
+
+struct Neu {
+    double s = 0.0, c = 0.0;
+    void add(double v) {
+        double t = s + v;
+        if (std::fabs(s) >= std::fabs(v)) c += (s - t) + v; else c += (v - t) + s;
+        s = t;
+    }
+    double val() const { return s + c; }
+};
+
+void pk(const float* x, const jc_config* c, int64_t n, double* P, double* K) {
+    Neu p, k;
+    const double hoff = (double)c->norm_mean[0] + (double)c->norm_depth;
+    for (int64_t i = 0; i < n; i++) {
+        double h = (double)x[i] * c->norm_std[0] + hoff;
+        double u = (double)x[n + i] * c->norm_std[1] + c->norm_mean[1];
+        double v = (double)x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
+        p.add(0.5 * (double)c->g * h * h);
+        k.add(0.5 * h * (u * u + v * v));
+    }
+    *P = p.val();
+    *K = k.val();
+}
+}  // namespace
+
+extern "C" {
+
+jc_status jc_model_create(const uint8_t* st, size_t st_len, const char* config_json, int32_t precision,
+                          jc_model** out) {
+    if (!out) return fail(JC_BAD_ARGUMENT, "out is null");
+    *out = nullptr;
+    return guard([&] {
+        jc::Model* m = new jc::Model(st, st_len, config_json, precision);
+        *out = new jc_model{m};
+    });
+}
+
+void jc_model_destroy(jc_model* m) {
+    if (!m) return;
+    try {
+        delete m->m;
+    } catch (...) {
+    }
+    delete m;
+}
+
+jc_status jc_model_config(const jc_model* m, jc_config* out) {
+    if (!m || !out) return fail(JC_BAD_ARGUMENT, "null argument");
+    *out = m->m->cfg;
+    return JC_OK;
+}
+
+jc_status jc_meta_of(const jc_model* m, float* meta_out) {
+    if (!m || !meta_out) return fail(JC_BAD_ARGUMENT, "null argument");
+    m->m->meta_of(meta_out);
+    return JC_OK;
+}
+
+jc_status jc_forward(jc_model* m, const float* state, const float* meta, float* increment) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    return guard([&] { m->m->forward_host(state, meta, increment); });
+}
+
+jc_status jc_step(jc_model* m, const float* state, const float* meta, float* next_state) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    return guard([&] { m->m->step_host(state, meta, next_state); });
+}
+
+jc_status jc_rollout(jc_model* m, const float* x0, const float* meta, int32_t ticks, uint32_t flags,
+                     float* final_state, float* trajectory, double* energies) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    return guard([&] { m->m->rollout_host(x0, meta, ticks, flags, final_state, trajectory, energies); });
+}
+
+jc_status jc_forward_device(jc_model* m, const float* d_state, const float* d_meta, float* d_increment,
+                            void* stream) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    return guard([&] { m->m->forward_device(d_state, d_meta, d_increment, (cudaStream_t)stream); });
+}
+
+jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta, int32_t ticks, uint32_t flags,
+                            float* d_final, double* d_energies, void* stream) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    if (!d_x0 || !d_meta) return fail(JC_BAD_ARGUMENT, "null buffer");
+    return guard([&] { m->m->rollout_device(d_x0, d_meta, ticks, flags, d_final, d_energies, (cudaStream_t)stream); });
+}
+
+double jc_mass(const float* x, int64_t n) {
+    if (!x || n <= 0) return 0.0;
+    Neu s;
+    for (int64_t i = 0; i < n; i++) s.add((double)x[i]);
+    return s.val() / (double)n;
+}
+
+double jc_energy(const float* x, const jc_config* cfg, int64_t n) {
+    if (!x || !cfg || n <= 0) return 0.0;
+    double P, K;
+    pk(x, cfg, n, &P, &K);
+    return P + K;
+}
+
+void jc_project_mass(float* x, double target, int64_t n) {
+    if (!x || n <= 0) return;
+    float delta = (float)(target - jc_mass(x, n));
+    for (int64_t i = 0; i < n; i++) x[i] += delta;
+}
+
+void jc_project_energy(float* x, double prev_energy, const jc_config* c, int64_t n) {
+    if (!x || !c || n <= 0) return;
+    double P, K;
+    pk(x, c, n, &P, &K);
+    double budget = prev_energy * (double)c->energy_r_max - P;
+    if (!(budget > 0.0)) budget = 0.0;
+    double s = std::sqrt(budget / (K > 1e-12 ? K : 1e-12));
+    float s32 = (float)(s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s));
+    for (int64_t i = 0; i < n; i++) {
+        float u = x[n + i] * c->norm_std[1] + c->norm_mean[1];
+        float v = x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
+        x[n + i] = (u * s32 - c->norm_mean[1]) / c->norm_std[1];
+        x[2 * n + i] = (v * s32 - c->norm_mean[2]) / c->norm_std[2];
+    }
+}
+
+const char* jc_last_error(void) { return g_last_error.c_str(); }
+
+const char* jc_version(void) { return "jacobi2000-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// Shared device-side definitions for the jacobi2000 GB300 engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace jc {
+
+// One grid instance inside a packed launch. Token-level buffers of all
+// instances are concatenated row-wise (instance i owns rows
+// [row0, row0 + tx*ty)); cell-level channel-last buffers likewise own cells
+// [cell0, cell0 + nx*ny). `state` is the instance's normalized
+// [channels, ny, nx] f32 state.
+struct InstDev {
+    int row0;         // first token row
+    int tx, ty;       // token grid
+    int nx, ny;       // cell grid
+    long long cell0;  // first cell in cell-level packed buffers
+    float* state;     // [3][ny][nx], read by the forward, updated by the tick
+    float* out;       // where the tick writes (next state or increment)
+    const float* pos; // [tx*ty, dim]
+    const float* meta;// [meta_dim]
+    int proj;         // projection slot index (per-instance scalars)
+    int pad_;
+};
+
+// Per-instance projection scalars, f64 (one slot per instance).
+struct ProjSlot {
+    double mass0;       // target box mean of channel 0
+    double energy;      // energy of the current (projected) state
+    double max_viol;    // max relative energy violation so far
+    double last_scale;  // last energy-projection scale
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Exact-erf GELU, 0.5 x (1 + erf(x / sqrt 2)) (crates/engine/src/cpu.rs:67-74),
+// with CUDA's erff.
+__device__ __forceinline__ float gelu_erf(float x) {
+    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752440f));
+}
+
+// Neumaier compensated accumulator in f64.
+struct Neu {
+    double s, c;
+    __device__ __forceinline__ void init() { s = 0.0; c = 0.0; }
+    __device__ __forceinline__ void add(double v) {
+        double t = s + v;
+        if (fabs(s) >= fabs(v)) c += (s - t) + v; else c += (v - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ double val() const { return s + c; }
+};
+
+#endif  // __CUDACC__
+
+}  // namespace jc

@@ -1,0 +1,196 @@
+"""Python binding of the C ABI (include/jacobi2000.h) through ctypes.
+
+Mirrors the reference engine crate's model API (crates/engine/src/lib.rs:30-68,
+gpu.rs:211-438): ``Model.load`` / ``Model.from_bytes``, ``forward``, ``step``,
+plus the tick loop of crates/engine-cli/src/eval.rs:144-157 as ``rollout``
+and the projections of crates/engine/src/project.rs as module functions.
+Every call goes to the CUDA library; there is no CPU fallback. If the library
+cannot be loaded, importing this module raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+PROJECT_MASS = 1
+PROJECT_ENERGY = 2
+FP32 = 0
+BF16 = 1
+
+STATUS = {0: "OK", 1: "NO_DEVICE", 2: "LIMIT", 3: "MAP", 4: "POLL", 5: "BAD_CHECKPOINT", 6: "BAD_SHAPE",
+          7: "OVER_BUDGET", 8: "DEVICE_TIMEOUT", 9: "BAD_ARGUMENT", 10: "CUDA_ERROR", 11: "NOT_FOUND"}
+
+
+class JcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+
+
+class JcConfig(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("nx", "ny", "patch", "channels", "dim", "layers", "heads", "head_dim",
+                                         "ff_inner", "meta_dim", "mask_kind", "mask_radius", "mask_dilation")] + [
+        ("norm_mean", C.c_float * 3), ("norm_std", C.c_float * 3), ("norm_depth", C.c_float),
+        ("dx", C.c_float), ("dt", C.c_float), ("g", C.c_float), ("depth", C.c_float), ("nu", C.c_float),
+        ("energy_r_max", C.c_float)]
+
+
+# Every symbol include/jacobi2000.h declares.
+EXPORTED = ["jc_model_create", "jc_model_destroy", "jc_model_config", "jc_meta_of", "jc_forward", "jc_step",
+            "jc_rollout", "jc_forward_device", "jc_rollout_device", "jc_mass", "jc_energy", "jc_project_mass",
+            "jc_project_energy", "jc_last_error", "jc_version"]
+
+_lib = None
+
+
+def load_library(path: str | Path | None = None):
+    """Loads (building first if needed) libjacobi2000.so and declares its
+    signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else _build.build()
+    L = C.CDLL(str(p))
+    F = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    D = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    vp = C.c_void_p
+    L.jc_model_create.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_int32, C.POINTER(vp)]
+    L.jc_model_destroy.argtypes = [vp]
+    L.jc_model_destroy.restype = None
+    L.jc_model_config.argtypes = [vp, C.POINTER(JcConfig)]
+    L.jc_meta_of.argtypes = [vp, F]
+    L.jc_forward.argtypes = [vp, F, F, F]
+    L.jc_step.argtypes = [vp, F, F, F]
+    L.jc_rollout.argtypes = [vp, F, F, C.c_int32, C.c_uint32, F, vp, vp]
+    L.jc_forward_device.argtypes = [vp, vp, vp, vp, vp]
+    L.jc_rollout_device.argtypes = [vp, vp, vp, C.c_int32, C.c_uint32, vp, vp, vp]
+    L.jc_mass.argtypes = [F, C.c_int64]
+    L.jc_mass.restype = C.c_double
+    L.jc_energy.argtypes = [F, C.POINTER(JcConfig), C.c_int64]
+    L.jc_energy.restype = C.c_double
+    L.jc_project_mass.argtypes = [F, C.c_double, C.c_int64]
+    L.jc_project_mass.restype = None
+    L.jc_project_energy.argtypes = [F, C.c_double, C.POINTER(JcConfig), C.c_int64]
+    L.jc_project_energy.restype = None
+    L.jc_last_error.restype = C.c_char_p
+    L.jc_version.restype = C.c_char_p
+    for name in EXPORTED:
+        if name.startswith("jc_") and not name.endswith("_destroy") and name not in (
+                "jc_mass", "jc_energy", "jc_project_mass", "jc_project_energy", "jc_last_error", "jc_version"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise JcError(status, load_library().jc_last_error().decode())
+
+
+class Model:
+    """A checkpoint on the GPU (engine::Model + GpuModel in one)."""
+
+    def __init__(self, safetensors: bytes, config_json: str, precision: int = FP32):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.jc_model_create(safetensors, len(safetensors), config_json.encode(), int(precision), C.byref(h)))
+        self._h = h
+        self._L = L
+        c = JcConfig()
+        _check(L.jc_model_config(h, C.byref(c)))
+        self.config = c
+        self.precision = precision
+        self.shape = (c.channels, c.ny, c.nx)
+        self.cells = c.nx * c.ny
+
+    @classmethod
+    def load(cls, directory: str | Path, precision: int = FP32) -> "Model":
+        """engine::Model::load (lib.rs:36-40): model.safetensors + config.json."""
+        d = Path(directory)
+        return cls((d / "model.safetensors").read_bytes(), (d / "config.json").read_text(), precision)
+
+    @classmethod
+    def from_bytes(cls, safetensors: bytes, config_json: str, precision: int = FP32) -> "Model":
+        return cls(safetensors, config_json, precision)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.jc_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _state(self, x) -> np.ndarray:
+        a = np.ascontiguousarray(x, dtype=np.float32)
+        if a.size != int(np.prod(self.shape)):
+            raise JcError(6, f"state has {a.size} elements, expected {int(np.prod(self.shape))}")
+        return a.reshape(self.shape)
+
+    def _meta(self, m) -> np.ndarray:
+        a = np.ascontiguousarray(m, dtype=np.float32).ravel()
+        if a.size != self.config.meta_dim:
+            raise JcError(6, f"meta has {a.size} elements, expected {self.config.meta_dim}")
+        return a
+
+    def meta_of(self) -> np.ndarray:
+        out = np.zeros(self.config.meta_dim, dtype=np.float32)
+        _check(self._L.jc_meta_of(self._h, out))
+        return out
+
+    def forward(self, state, meta) -> np.ndarray:
+        """The predicted increment (cpu.rs:249-352)."""
+        out = np.empty(self.shape, dtype=np.float32)
+        _check(self._L.jc_forward(self._h, self._state(state), self._meta(meta), out))
+        return out
+
+    def step(self, state, meta) -> np.ndarray:
+        """state + forward(state, meta) (cpu.rs:84-88)."""
+        out = np.empty(self.shape, dtype=np.float32)
+        _check(self._L.jc_step(self._h, self._state(state), self._meta(meta), out))
+        return out
+
+    def rollout(self, x0, meta, ticks: int, flags: int = PROJECT_MASS | PROJECT_ENERGY, trajectory: bool = False):
+        """``ticks`` ticks of step + projections. Returns (final, energies[,
+        trajectory])."""
+        final = np.empty(self.shape, dtype=np.float32)
+        energies = np.empty(ticks + 1, dtype=np.float64)
+        traj = np.empty((ticks + 1,) + self.shape, dtype=np.float32) if trajectory else None
+        _check(self._L.jc_rollout(self._h, self._state(x0), self._meta(meta), int(ticks), int(flags), final,
+                                  traj.ctypes.data if traj is not None else None, energies.ctypes.data))
+        return (final, energies, traj) if trajectory else (final, energies)
+
+
+def mass(x, cells: int) -> float:
+    return load_library().jc_mass(np.ascontiguousarray(x, dtype=np.float32).ravel(), int(cells))
+
+
+def energy(x, config: JcConfig, cells: int) -> float:
+    return load_library().jc_energy(np.ascontiguousarray(x, dtype=np.float32).ravel(), C.byref(config), int(cells))
+
+
+def project_mass(x, target: float, cells: int) -> np.ndarray:
+    y = np.array(x, dtype=np.float32, copy=True)
+    load_library().jc_project_mass(y.reshape(-1), float(target), int(cells))
+    return y
+
+
+def project_energy(x, prev_energy: float, config: JcConfig, cells: int) -> np.ndarray:
+    y = np.array(x, dtype=np.float32, copy=True)
+    load_library().jc_project_energy(y.reshape(-1), float(prev_energy), C.byref(config), int(cells))
+    return y

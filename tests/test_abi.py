@@ -1,0 +1,110 @@
+"""The C ABI without a GPU: the library loads and exports every symbol
+include/jacobi2000.h declares; checkpoint errors map to status codes before
+any device work; the host projections agree with the oracle."""
+
+import ctypes as C
+import json
+import re
+
+import numpy as np
+import pytest
+
+from jacobi2000_gb300 import engine
+from jacobi2000_gb300.checkpoint import read_safetensors, write_safetensors_bytes
+from conftest import ROOT
+from oracle.oracle import identity_config, projection_only
+
+
+def test_header_symbols_are_exported():
+    header = (ROOT / "include" / "jacobi2000.h").read_text()
+    declared = set(re.findall(r"\b(jc_[a-z_0-9]+)\s*\(", header))
+    L = engine.load_library()
+    missing = [s for s in sorted(declared) if not hasattr(L, s)]
+    assert not missing, missing
+    assert declared >= set(engine.EXPORTED)
+
+
+def _create(st: bytes, cj: str):
+    L = engine.load_library()
+    h = C.c_void_p()
+    status = L.jc_model_create(st, len(st), cj.encode(), 0, C.byref(h))
+    return status, L.jc_last_error().decode()
+
+
+def test_truncated_safetensors_is_a_bad_checkpoint(pt_tiny):
+    status, msg = _create(pt_tiny["st_bytes"][:100], pt_tiny["config"])
+    assert engine.STATUS[status] == "BAD_CHECKPOINT", msg
+    status, msg = _create(b"\x01\x02", pt_tiny["config"])
+    assert engine.STATUS[status] == "BAD_CHECKPOINT"
+
+
+def test_non_f32_tensor_is_rejected(pt_tiny):
+    st = pt_tiny["st_bytes"]
+    (hlen,) = np.frombuffer(st[:8], dtype="<u8")
+    header = json.loads(st[8:8 + int(hlen)])
+    header["pos"]["dtype"] = "F16"
+    hb = json.dumps(header).encode()
+    bad = np.uint64(len(hb)).tobytes() + hb + st[8 + int(hlen):]
+    status, msg = _create(bad, pt_tiny["config"])
+    assert engine.STATUS[status] == "BAD_CHECKPOINT" and "F32" in msg
+
+
+def test_missing_tensor_is_named(pt_tiny):
+    t = dict(pt_tiny["tensors"])
+    del t["blocks.1.ff2.bias"]
+    status, msg = _create(write_safetensors_bytes(t), pt_tiny["config"])
+    assert engine.STATUS[status] == "BAD_CHECKPOINT" and "blocks.1.ff2.bias" in msg
+
+
+def test_grid_not_divisible_by_patch_is_a_bad_shape(pt_tiny):
+    c = json.loads(pt_tiny["config"])
+    c["nx"] = 18
+    status, msg = _create(pt_tiny["st_bytes"], json.dumps(c))
+    assert engine.STATUS[status] == "BAD_SHAPE", msg
+
+
+def test_missing_config_field_and_bad_json(pt_tiny):
+    c = json.loads(pt_tiny["config"])
+    del c["dt"]
+    status, msg = _create(pt_tiny["st_bytes"], json.dumps(c))
+    assert engine.STATUS[status] == "BAD_CHECKPOINT" and "dt" in msg
+    status, _ = _create(pt_tiny["st_bytes"], "{not json")
+    assert engine.STATUS[status] == "BAD_CHECKPOINT"
+
+
+def test_pos_shape_must_match_the_grid(pt_tiny):
+    c = json.loads(pt_tiny["config"])
+    c["nx"] = c["ny"] = 32
+    status, msg = _create(pt_tiny["st_bytes"], json.dumps(c))
+    assert engine.STATUS[status] == "BAD_SHAPE" and "pos" in msg
+
+
+def test_null_out_pointer_is_a_bad_argument(pt_tiny):
+    L = engine.load_library()
+    st = pt_tiny["st_bytes"]
+    assert engine.STATUS[L.jc_model_create(st, len(st), pt_tiny["config"].encode(), 0, None)] == "BAD_ARGUMENT"
+    h = C.c_void_p()
+    assert engine.STATUS[L.jc_model_create(st, len(st), pt_tiny["config"].encode(), 7, C.byref(h))] == "BAD_ARGUMENT"
+
+
+def test_host_projections_match_the_oracle():
+    rng = np.random.default_rng(3)
+    n = 300
+    cfg = identity_config(n, r_max=1.0)
+    cfg.norm_mean = (0.1, -0.05, 0.02)
+    cfg.norm_std = (0.3, 0.2, 0.2)
+    cfg.norm_depth = 1.0
+    orc = projection_only(cfg)
+    x = (0.5 * rng.standard_normal(3 * n)).astype(np.float32)
+    jcfg = engine.JcConfig()
+    jcfg.norm_mean[:] = cfg.norm_mean
+    jcfg.norm_std[:] = cfg.norm_std
+    jcfg.norm_depth, jcfg.g, jcfg.energy_r_max = 1.0, 9.81, 1.0
+    assert engine.mass(x, n) == pytest.approx(orc.mass_sum64(x), rel=0, abs=1e-15)
+    assert engine.energy(x, jcfg, n) == pytest.approx(orc.energy_sum64(x), rel=1e-15)
+    y = engine.project_mass(x, 0.25, n)
+    assert np.array_equal(y, orc.project_mass(x, 0.25, sum64=True))
+    e0 = orc.energy_sum64(x)
+    y = engine.project_energy(x, 0.999 * e0, jcfg, n)
+    assert np.array_equal(y, orc.project_energy(x, 0.999 * e0, sum64=True))
+    assert engine.energy(y, jcfg, n) <= 0.999 * e0 * (1 + 1e-6)
