@@ -1,0 +1,353 @@
+"""Throughput of the shallow-water transformer rollout on GB300.
+
+Workload (default): B instances of a 128x128 grid, model20-shaped checkpoint
+(dim 128, 4 layers, 4 heads, stencil r1 d1, random init seed 0), 8 seeded
+Gaussian drops per instance (amplitude U[0.02, 0.15], sigma U[2, 6] cells,
+periodic images), a 50-tick rollout with mass and energy projection per
+instance. One step = one batched rollout of all B instances. Metric:
+cell-ticks/s = sum over instances of nx * ny * ticks / seconds.
+
+* ``value``: device-resident inputs (x0/meta already in HBM), timed with CUDA
+  events on the launching stream.
+* ``e2e``: the same rollouts through the C ABI with host buffers; host->device
+  copies of x0/meta and device->host copies of the final states and energies
+  are inside the timed region.
+* ``fp32_plain``: the FP32 single-request path, one rollout at a time.
+* ``--impl reference``: the reference's CPU forward pass and projections
+  (the C restatement of crates/engine/src/cpu.rs and project.rs, with the
+  reference's own O(T^2) masked attention scan) on the host cores.
+
+Under torchrun each rank runs its own B instances (no exchange step):
+weak scaling, barrier + max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-ticks/s BF16 served vs FP32 plain on 1 GB300 at stated error; p50/p99 lat"
+UNIT = "cell-ticks/s"
+FLOP_PER_CELL_TICK = {(128, 4): 141_056, (256, 6): 691_456}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--side", type=int, default=128)
+    ap.add_argument("--ticks", type=int, default=50)
+    ap.add_argument("--dim", type=int, default=128)
+    ap.add_argument("--layers", type=int, default=4)
+    ap.add_argument("--cpu-sample-ticks", type=int, default=1)
+    return ap.parse_args()
+
+
+def workload(args):
+    from jacobi2000_gb300.checkpoint import parse_config, synthetic_checkpoint, meta_of
+    from jacobi2000_gb300.ic import random_drops
+
+    t, cj = synthetic_checkpoint(args.side, args.dim, args.layers, 0)
+    cfg = parse_config(cj, t)
+    rank = int(os.environ.get("RANK", "0"))
+    x0s = [random_drops(cfg, seed=rank * 100_000 + i) for i in range(args.instances)]
+    return t, cj, cfg, x0s, meta_of(cfg)
+
+
+def config_dict(args, cfg):
+    return {"workload": f"rollout {args.instances}x {args.side}x{args.side} grids, {args.ticks} ticks, "
+                        f"mass+energy projection, 8 drops/instance",
+            "model": f"jacobi2000 dim {args.dim}, {args.layers} layers, 4 heads, stencil r1 d1, seed 0",
+            "grid": [args.side, args.side], "instances_per_step": args.instances, "ticks": args.ticks,
+            "l2": "per-tick working set > 129 MB L2 (no flush needed)", "parallelism": "replicas"}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, out: Path):
+        self.out = out
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.out, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+            self.f.close()
+
+    def summary(self, gpu_index: int = 0):
+        try:
+            rows = [r.split(", ") for r in self.out.read_text().strip().splitlines()]
+        except OSError:
+            return None
+        rows = [r for r in rows if len(r) >= 9 and r[0].strip() == str(gpu_index)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def ncu_traffic() -> dict:
+    """Per-launch DRAM bytes of kernels from the committed ncu summary
+    (profiles/ncu_traffic.txt: `kernel bytes_per_launch` lines)."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def kernel_work(name: str, B: int, cells: int, D: int, F: int):
+    """Algorithmic work of one launch of a kernel over the whole batch:
+    ("flop", useful FLOPs) for contractions, ("byte", compulsory bytes) for
+    memory-bound kernels. R tokens = B cells / 16, N cells = B cells."""
+    R, N = B * cells // 16, B * cells
+    flop = {"tc_qkv": 2 * R * D * 3 * D, "tc_proj_ln": 2 * R * D * D, "tc_mlp": 4 * R * D * F,
+            "tc_token_mix": 18 * R * D * D, "tc_to_cells": 2 * R * D * 32, "tc_conv1": 2 * N * 35 * 9 * 32,
+            "f32_ln_qkv": 2 * R * D * 3 * D, "f32_proj": 2 * R * D * D, "f32_ln_ff1": 2 * R * D * F,
+            "f32_ff2": 2 * R * F * D, "f32_token_mix": 18 * R * D * D, "f32_to_cells": 2 * R * D * 32,
+            "f32_conv1": 2 * N * 35 * 9 * 32, "bf_conv2_step": 2 * N * 32 * 9 * 3, "f32_conv2_step": 2 * N * 32 * 9 * 3}
+    byte = {"bf_attention": R * (3 * D * 2 + D * 2), "bf_embed": N * 12 + R * (4 * D + 2 * D),
+            "bf_upsample": R * 32 * 4 + N * (12 + 96), "projection": N * 12 * 4 + N * 12,
+            "f32_attention": R * (3 * D * 4 + D * 4), "f32_embed": N * 12 + R * 4 * D,
+            "f32_upsample_concat": R * 32 * 4 + N * (12 + 144), "f32_final_ln": R * D * 8}
+    if name in flop:
+        return "flop", flop[name]
+    if name in byte:
+        return "byte", byte[name]
+    return None, None
+
+
+def cpu_sample(cfg, t, x0, meta, ticks: int):
+    """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
+    masked scan) on all host cores, over `ticks` ticks of one instance."""
+    from oracle import oracle
+
+    oracle.set_threads(os.cpu_count() or 1)
+    oracle.set_attention_mode("scan")
+    m = oracle.OracleModel(cfg, t)
+    t0 = time.perf_counter()
+    m.rollout(x0, meta, ticks, oracle.MASS | oracle.ENERGY)
+    dt = time.perf_counter() - t0
+    return cfg.nx * cfg.ny * ticks / dt, oracle.get_threads(), dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t, cj, cfg, x0s, meta = workload(args)
+    from oracle import oracle
+
+    oracle.build()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, cores, dt = cpu_sample(cfg, t, x0s[i % len(x0s)], meta, args.cpu_sample_ticks)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = f"1 instance x {args.cpu_sample_ticks} tick(s) of the {args.side}x{args.side} workload per step"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * cfg.nx * cfg.ny * args.cpu_sample_ticks / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(args, cfg), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.checkpoint import write_safetensors_bytes
+
+    t, cj, cfg, x0s, meta = workload(args)
+    prec = engine.BF16 if args.precision == "bf16" else engine.FP32
+    model = engine.Model.from_bytes(write_safetensors_bytes(t), cj, prec)
+    cells = cfg.nx * cfg.ny
+    B, H = args.instances, args.ticks
+    batch = engine.Batch([model], max_instances=B, max_cells=B * cells)
+    me = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+    host_items = [(0, x, meta, H, me) for x in x0s]
+
+    # device-resident inputs
+    dx0 = [torch.from_numpy(x).cuda() for x in x0s]
+    dmeta = torch.from_numpy(meta).cuda()
+    dout = [torch.empty_like(x) for x in dx0]
+    dev_items = [(0, x.data_ptr(), dmeta.data_ptr(), H, me, o.data_ptr()) for x, o in zip(dx0, dout)]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        batch.rollout(dev_items, device=True, stream=sptr)
+    barrier()
+    clocks = Clocks(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv")
+    (ROOT / "gpurun_out").mkdir(exist_ok=True)
+    with clocks:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            batch.rollout(dev_items, device=True, stream=sptr)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    work = B * cells * H * world
+    value = work / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    for _ in range(2):
+        batch.rollout(host_items)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.rollout(host_items)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    h2d = B * (x0s[0].nbytes + meta.nbytes)
+    d2h = B * (x0s[0].nbytes + 32)
+
+    # the plain FP32 single-request path, one rollout at a time
+    plain = engine.Model.from_bytes(write_safetensors_bytes(t), cj, engine.FP32)
+    plain.rollout(x0s[0], meta, H, me)
+    n_plain = min(B, 8)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        plain.rollout(x0s[i], meta, H, me)
+    plain_s = (time.perf_counter() - t0) / n_plain
+    plain_value = cells * H / plain_s
+
+    # per-kernel device times (events on the launching stream, outside graphs)
+    prof = batch.profile(dev_items, device=True)
+    launches_per_step = sum(n for n, _ in prof.values())
+    pk, pk_kind = peaks()
+    total_ms = sum(v[1] for v in prof.values())
+    table = {}
+    for kname, (nl, tot) in prof.items():
+        kind, amount = kernel_work(kname, B, cells, args.dim, 4 * args.dim)
+        avg_s = tot / nl / 1e3
+        if kind == "flop":
+            table[kname] = {"tflops": amount / avg_s / 1e12, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
+        elif kind == "byte":
+            table[kname] = {"gbs": amount / avg_s / 1e9, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
+    name, (nl, tot_ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    kind, amount = kernel_work(name, B, cells, args.dim, 4 * args.dim)
+    avg_s = tot_ms / nl / 1e3
+    traffic = ncu_traffic().get(name)
+    if kind == "flop" and name.startswith("tc_"):
+        peak = pk["bf16_tflops"]
+        roof = {"bound": "tensor", "kernel": name, "achieved": amount / avg_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": amount / avg_s / 1e12 / peak, "traffic": traffic,
+                "peak_kind": f"{pk_kind} bf16 dense burst", "flop_per_launch": amount}
+    elif kind == "flop":
+        peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        roof = {"bound": "fp32-simt", "kernel": name, "achieved": amount / avg_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": amount / avg_s / 1e12 / peak, "traffic": traffic,
+                "peak_kind": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x max SM clock)",
+                "flop_per_launch": amount}
+    else:
+        peak = pk["hbm_gbs"]
+        roof = {"bound": "hbm", "kernel": name, "achieved": amount / avg_s / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": amount / avg_s / 1e9 / peak, "traffic": traffic, "peak_kind": f"{pk_kind} copy bandwidth",
+                "bytes_per_launch": amount}
+    roof.update({"avg_launch_ms": avg_s * 1e3, "share": tot_ms / total_ms})
+
+    cpu = None
+    if rank == 0:
+        v, cores, dt = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"1 instance x {args.cpu_sample_ticks} tick(s), {dt:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32" if prec == engine.FP32 else "bf16", "data": "synthetic",
+                "config": config_dict(args, cfg),
+                "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
+                               "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local),
+                "gpu_launches": launches_per_step * args.steps,
+                "kernels": table, "peaks": pk_kind}
+        print(json.dumps(line), flush=True)
+    batch.close()
+    model.close()
+    plain.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

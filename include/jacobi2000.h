@@ -110,6 +110,49 @@ jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta,
                             int32_t ticks, uint32_t flags, float* d_final,
                             double* d_energies, void* stream);
 
+/* ---- Batched rollouts ----
+ * The reference runs one state per call (batch size 1, crates/engine/src/lib.rs:1-4);
+ * this runs many rollouts together, as the batched loops of
+ * crates/engine-cli/src/eval.rs:126-176 would if their trajectories were
+ * stepped side by side. A batch is created over a list of models that share
+ * every hyper-parameter, mask, normalizer, g and energy_r_max (a checkpoint
+ * family: one model per grid size, or a forward and a reverse checkpoint).
+ * Instances whose models share every tensor but `pos` run in the same
+ * launches; each model group gets its own launches. */
+typedef struct jc_batch jc_batch;
+
+typedef struct {
+    int32_t model;        /* index into the batch's model list */
+    int32_t ticks;        /* rollout length, >= 0 */
+    uint32_t flags;       /* JC_PROJECT_* for this instance */
+    int32_t reserved;     /* must be 0 */
+    const float* x0;      /* initial state [channels, ny, nx] of that model's grid */
+    const float* meta;    /* [meta_dim] */
+    float* final_state;   /* receives the state after `ticks` ticks */
+    double* energy;       /* optional [2]: final energy, max relative energy violation */
+} jc_instance;
+
+/* max_instances / max_cells bound one jc_batch_rollout call; the workspace is
+ * allocated here, once. */
+jc_status jc_batch_create(jc_model* const* models, int32_t n_models, int32_t max_instances,
+                          int64_t max_cells, jc_batch** out);
+void jc_batch_destroy(jc_batch* b);
+
+/* Runs every instance to its own horizon; blocks until the results are
+ * written. device_pointers = 0: x0/meta/final_state are host memory (copied
+ * in and out inside the call); 1: they are device memory. `stream` is a
+ * cudaStream_t (null = the batch's own stream). */
+jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
+                           int32_t device_pointers, void* stream);
+
+/* Instrumentation, with no counterpart in the reference: runs the instances
+ * once, outside any graph, with CUDA events around every kernel launch, and
+ * writes one "name,launches,total_ms" line per kernel into `report`
+ * (NUL-terminated, truncated to `cap` bytes). Final states are not copied
+ * out. */
+jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n,
+                           int32_t device_pointers, char* report, size_t cap);
+
 /* Host-side projections, engine::project (crates/engine/src/project.rs:22-54),
  * with f64 compensated sums. n = cells per channel; x is [3, n]. */
 double jc_mass(const float* x, int64_t n);

@@ -7,10 +7,6 @@
 #include "../../include/jacobi2000.h"
 #include "runtime.hpp"
 
-struct jc_model {
-    jc::Model* m;
-};
-
 namespace {
 thread_local std::string g_last_error;
 
@@ -121,6 +117,45 @@ jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta,
     if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
     if (!d_x0 || !d_meta) return fail(JC_BAD_ARGUMENT, "null buffer");
     return guard([&] { m->m->rollout_device(d_x0, d_meta, ticks, flags, d_final, d_energies, (cudaStream_t)stream); });
+}
+
+jc_status jc_batch_create(jc_model* const* models, int32_t n_models, int32_t max_instances, int64_t max_cells,
+                          jc_batch** out) {
+    if (!out) return fail(JC_BAD_ARGUMENT, "out is null");
+    *out = nullptr;
+    return guard([&] {
+        jc::Batch* b = new jc::Batch(models, n_models, max_instances, max_cells);
+        *out = new jc_batch{b};
+    });
+}
+
+void jc_batch_destroy(jc_batch* b) {
+    if (!b) return;
+    try {
+        delete b->b;
+    } catch (...) {
+    }
+    delete b;
+}
+
+jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n, int32_t device_pointers,
+                           void* stream) {
+    if (!b) return fail(JC_BAD_ARGUMENT, "batch is null");
+    return guard([&] { b->b->rollout(instances, n, device_pointers != 0, (cudaStream_t)stream); });
+}
+
+jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n, int32_t device_pointers,
+                           char* report, size_t cap) {
+    if (!b || !report || cap == 0) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] {
+        auto s = b->b->profile(instances, n, device_pointers != 0);
+        std::string out;
+        for (auto& kv : s)
+            out += kv.first + "," + std::to_string(kv.second.first) + "," + std::to_string(kv.second.second) + "\n";
+        size_t k = std::min(out.size(), cap - 1);
+        std::memcpy(report, out.data(), k);
+        report[k] = '\0';
+    });
 }
 
 double jc_mass(const float* x, int64_t n) {

@@ -12,6 +12,8 @@ namespace jc {
 // [row0, row0 + tx*ty)); cell-level channel-last buffers likewise own cells
 // [cell0, cell0 + nx*ny). `state` is the instance's normalized
 // [channels, ny, nx] f32 state.
+// Instances of a launch are sorted by row0 and cell0 (both ascending), so a
+// row or cell finds its instance by binary search.
 struct InstDev {
     int row0;         // first token row
     int tx, ty;       // token grid
@@ -21,9 +23,14 @@ struct InstDev {
     float* out;       // where the tick writes (next state or increment)
     const float* pos; // [tx*ty, dim]
     const float* meta;// [meta_dim]
-    int proj;         // projection slot index (per-instance scalars)
-    int pad_;
+    unsigned flags;   // projection flags of this instance (1 mass, 2 energy)
+    int tile0;        // first 16x16 cell tile of this instance in the launch
+    int tt0;          // first 8x16 token tile (tensor-core token conv)
+    int ct0;          // first 8x16 cell tile (tensor-core cell conv)
 };
+
+constexpr int kCellTile = 16;  // side of the cell tiles of the cell-level kernels
+constexpr int kConvTX = 8, kConvTY = 16;  // tensor-core conv tiles: 8 wide, 16 high (M = 128)
 
 // Per-instance projection scalars, f64 (one slot per instance).
 struct ProjSlot {
@@ -48,6 +55,24 @@ __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
+}
+
+// Index of the instance owning token row r: the last i with inst[i].row0 <= r.
+__device__ __forceinline__ int inst_of_row(const InstDev* inst, int n, int r) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].row0 <= r) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int inst_of_cell(const InstDev* inst, int n, long long c) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].cell0 <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Exact-erf GELU, 0.5 x (1 + erf(x / sqrt 2)) (crates/engine/src/cpu.rs:67-74),

@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <string>
+#include <vector>
+
 #include "common.cuh"
 
 namespace jc {
@@ -37,17 +41,28 @@ struct WeightsF32 {
     const float *c2_w, *c2_b;         // [C, HD, 3, 3] as stored, [C]
 };
 
-// A packed launch over several instances, with its workspace.
+// A packed launch over the first n_inst instances of `inst`, with the
+// workspace it writes. R, NC and n_tiles cover exactly those instances.
 struct Pack {
     int n_inst;
-    int R;            // total token rows
-    long long NC;     // total cells
-    InstDev* inst;    // device array [n_inst]
-    int* row_inst;    // device [R]
-    int* cell_inst;   // device [NC]
-    ProjSlot* proj;   // device [n_inst]
+    int R;            // token rows
+    long long NC;     // cells
+    int n_tiles;      // 16x16 cell tiles
+    int n_ttiles;     // 8x16 token tiles
+    int n_ctiles;     // 8x16 cell tiles
+    InstDev* inst;    // device array, sorted by row0 / cell0 / tile0
+    ProjSlot* proj;   // device array parallel to inst
+    void* tmaps;      // device array: 2 tensor maps per instance (BF16 path)
+    int* err;         // device flag set when a device-side wait times out
     // FP32 workspace
     float *x, *qkv, *attn, *ff1, *xn, *t1, *z0, *zc, *c1;
+    // BF16-path workspace: token-level buffers (row stride in bytes) and
+    // cell-level buffers (cell stride in bytes)
+    static constexpr int kTokBufs = 4, kCellBufs = 2;
+    char* bt[kTokBufs];
+    int bt_stride[kTokBufs];
+    char* bc[kCellBufs];
+    int bc_stride[kCellBufs];
 };
 
 enum TickMode { kWriteIncrement = 0, kWriteNextState = 1 };
@@ -56,8 +71,37 @@ enum TickMode { kWriteIncrement = 0, kWriteNextState = 1 };
 // state to each instance's `out`.
 void forward_f32(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cudaStream_t s);
 
-// Projection of every instance's `out` state (mass, then energy), f64 sums.
-// init = 1 records mass0 and the energy of the state without changing it.
-void projection(const Dims& d, const Pack& p, uint32_t flags, int init, cudaStream_t s);
+// Projection of every instance's state (mass, then energy, per the instance's
+// flags), f64 sums. init = 1 records mass0 and the energy of the state.
+void projection(const Dims& d, const Pack& p, int init, cudaStream_t s);
+
+// Optional per-launch timing with CUDA events (profiling only; never active
+// during graph capture). Kernels are timed by name on the launching stream.
+struct KernelTimer {
+    struct Rec {
+        const char* name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    cudaStream_t stream = nullptr;
+    const char* open = nullptr;
+    cudaEvent_t open_ev = nullptr;
+    void begin(const char* name, cudaStream_t s);
+    void end();
+    // name -> (launches, total ms); synchronizes.
+    std::map<std::string, std::pair<int, double>> summary();
+    ~KernelTimer();
+};
+extern thread_local KernelTimer* g_ktimer;
+
+struct KScope {
+    KScope(const char* name, cudaStream_t s) {
+        if (g_ktimer) g_ktimer->begin(name, s);
+    }
+    ~KScope() {
+        if (g_ktimer) g_ktimer->end();
+    }
+};
 
 }  // namespace jc

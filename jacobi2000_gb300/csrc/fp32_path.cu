@@ -12,6 +12,55 @@
 
 namespace jc {
 
+thread_local KernelTimer* g_ktimer = nullptr;
+
+void KernelTimer::begin(const char* name, cudaStream_t s) {
+    stream = s;
+    open = name;
+    if (pool.empty()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        pool.push_back(e);
+    }
+    open_ev = pool.back();
+    pool.pop_back();
+    cudaEventRecord(open_ev, s);
+}
+
+void KernelTimer::end() {
+    if (!open) return;
+    cudaEvent_t e;
+    if (pool.empty()) cudaEventCreate(&e);
+    else { e = pool.back(); pool.pop_back(); }
+    cudaEventRecord(e, stream);
+    recs.push_back(Rec{open, open_ev, e});
+    open = nullptr;
+}
+
+std::map<std::string, std::pair<int, double>> KernelTimer::summary() {
+    std::map<std::string, std::pair<int, double>> out;
+    for (auto& r : recs) {
+        cudaEventSynchronize(r.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        auto& v = out[r.name];
+        v.first += 1;
+        v.second += ms;
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    recs.clear();
+    return out;
+}
+
+KernelTimer::~KernelTimer() {
+    for (auto& r : recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
 static void check_launch(const char* what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -19,22 +68,25 @@ static void check_launch(const char* what) {
 
 namespace f32k {
 
-// Patchify + embed + pos + meta (cpu.rs:253-280). One CTA per TOK rows;
+// Patchify + embed + pos + meta (cpu.rs:253-280). One CTA per 16 rows;
 // threads stride over the D outputs. Token t = ty*tx + tx, feature
 // c*P*P + py*P + px.
 constexpr int kEmbedTok = 16;
 
 __global__ void embed_kernel(Dims d, const float* __restrict__ We, const float* __restrict__ be,
                              const float* __restrict__ Wm, const float* __restrict__ bm, const InstDev* inst,
-                             const int* row_inst, int R, float* __restrict__ x) {
+                             int n_inst, int R, float* __restrict__ x) {
     extern __shared__ float patch[];  // [kEmbedTok][C*P*P]
+    __shared__ int rinst[kEmbedTok];
     const int pd = d.C * d.P * d.P;
     const int r0 = blockIdx.x * kEmbedTok;
+    if (threadIdx.x < kEmbedTok) rinst[threadIdx.x] = r0 + (int)threadIdx.x < R ? inst_of_row(inst, n_inst, r0 + threadIdx.x) : 0;
+    __syncthreads();
     for (int e = threadIdx.x; e < kEmbedTok * pd; e += blockDim.x) {
         int i = e / pd, f = e % pd, r = r0 + i;
         float v = 0.f;
         if (r < R) {
-            const InstDev& I = inst[row_inst[r]];
+            const InstDev& I = inst[rinst[i]];
             int t = r - I.row0, c = f / (d.P * d.P), py = (f / d.P) % d.P, px = f % d.P;
             int y = (t / I.tx) * d.P + py, xx = (t % I.tx) * d.P + px;
             v = I.state[((size_t)c * I.ny + y) * I.nx + xx];
@@ -45,7 +97,7 @@ __global__ void embed_kernel(Dims d, const float* __restrict__ We, const float* 
     for (int e = threadIdx.x; e < kEmbedTok * d.D; e += blockDim.x) {
         int i = e / d.D, o = e % d.D, r = r0 + i;
         if (r >= R) continue;
-        const InstDev& I = inst[row_inst[r]];
+        const InstDev& I = inst[rinst[i]];
         float acc = be[o];
         const float* p = patch + i * pd;
         for (int f = 0; f < pd; f++) acc = fmaf(p[f], We[(size_t)f * d.D + o], acc);
@@ -56,7 +108,7 @@ __global__ void embed_kernel(Dims d, const float* __restrict__ We, const float* 
 }
 
 // Stencil-masked multi-head attention (cpu.rs:97-164, mask.rs:18-30). One
-// warp per (row, head); lanes over the head's features. Candidate keys are
+// warp per (row, head); lanes over the head's features (head width <= 64). Candidate keys are
 // enumerated in increasing key index (the order the reference's scan meets
 // them): scores, max, exp(s - max) with the denominator, then
 // out = sum (e / denom) v. qkv is [R, 3D] (q | k | v).
@@ -75,14 +127,14 @@ __device__ __forceinline__ int candidate_row(const Dims& d, const InstDev& I, in
     return I.row0 + ky * I.tx + kx;
 }
 
-__global__ void attention_kernel(Dims d, const float* __restrict__ qkv, const InstDev* inst, const int* row_inst,
-                                 int R, float* __restrict__ out) {
+__global__ void attention_kernel(Dims d, const float* __restrict__ qkv, const InstDev* inst, int n_inst, int R,
+                                 float* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int wg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int row = wg / d.heads, head = wg % d.heads;
     if (row >= R) return;
     const int hd = d.D / d.heads, D3 = 3 * d.D;
-    const InstDev& I = inst[row_inst[row]];
+    const InstDev& I = inst[inst_of_row(inst, n_inst, row)];
     const int t = row - I.row0, qy = t / I.tx, qx = t % I.tx;
     const float scale = 1.0f / sqrtf((float)hd);
     const float* q = qkv + (size_t)row * D3 + head * hd;
@@ -93,24 +145,32 @@ __global__ void attention_kernel(Dims d, const float* __restrict__ qkv, const In
     auto score = [&](int kr) {
         const float* k = qkv + (size_t)kr * D3 + d.D + head * hd;
         float p = (lane < hd ? qv0 * k[lane] : 0.f) + (lane + 32 < hd ? qv1 * k[lane + 32] : 0.f);
-        for (int e = lane + 64; e < hd; e += 32) p += q[e] * k[e];
         return warp_sum(p) * scale;
     };
+    // scores of the first 32 candidates stay in registers (lane j holds
+    // candidate j); later candidates are recomputed
+    float sreg = -INFINITY;
     float smax = -INFINITY;
     for (int j = 0; j < nc; j++) {
         int kr = candidate_row(d, I, qy, qx, j);
-        if (kr >= 0) smax = fmaxf(smax, score(kr));
+        if (kr < 0) continue;
+        float s = score(kr);
+        if (j < 32 && lane == j) sreg = s;
+        smax = fmaxf(smax, s);
     }
+    auto score_j = [&](int j, int kr) {
+        return j < 32 ? __shfl_sync(0xffffffffu, sreg, j) : score(kr);
+    };
     float denom = 0.f;
     for (int j = 0; j < nc; j++) {
         int kr = candidate_row(d, I, qy, qx, j);
-        if (kr >= 0) denom += expf(score(kr) - smax);
+        if (kr >= 0) denom += expf(score_j(j, kr) - smax);
     }
     float o0 = 0.f, o1 = 0.f;
     for (int j = 0; j < nc; j++) {
         int kr = candidate_row(d, I, qy, qx, j);
         if (kr < 0) continue;
-        float e = expf(score(kr) - smax);
+        float e = expf(score_j(j, kr) - smax);
         if (e == 0.f) continue;
         float wn = e / denom;
         const float* v = qkv + (size_t)kr * D3 + 2 * d.D + head * hd;
@@ -141,59 +201,88 @@ __global__ void layernorm_kernel(const float* __restrict__ x, const float* __res
 // Upsample z0 (token level, [rows, HD]) by P along y then x with edge
 // replicate and weights (i + 0.5)/P (cpu.rs:211-245), and concatenate the
 // state channels (cpu.rs:339-342): zc [cells, kZcStride], one thread per cell.
-__global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst,
-                                       const int* cell_inst, long long NC, float* __restrict__ zc) {
+__global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst, int n_inst,
+                                       long long NC, float* __restrict__ zc) {
     long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= NC) return;
-    const InstDev& I = inst[cell_inst[cell]];
+    const InstDev& I = inst[inst_of_cell(inst, n_inst, cell)];
     long long cl = cell - I.cell0;
     int y = (int)(cl / I.nx), x = (int)(cl % I.nx);
     int yt = y / d.P, iy = y % d.P, xt = x / d.P, ix = x % d.P;
     int yt2 = min(yt + 1, I.ty - 1), xt2 = min(xt + 1, I.tx - 1);
     float wy = ((float)iy + 0.5f) / (float)d.P, wx = ((float)ix + 0.5f) / (float)d.P;
-    const float* a = z0 + (size_t)(I.row0 + yt * I.tx + xt) * d.HD;
-    const float* b = z0 + (size_t)(I.row0 + yt * I.tx + xt2) * d.HD;
-    const float* c = z0 + (size_t)(I.row0 + yt2 * I.tx + xt) * d.HD;
-    const float* e = z0 + (size_t)(I.row0 + yt2 * I.tx + xt2) * d.HD;
-    float* o = zc + (size_t)cell * kZcStride;
-    for (int ch = 0; ch < d.HD; ch++) {
-        float z1a = a[ch] * (1.0f - wy) + c[ch] * wy;  // upsample_y at column xt
-        float z1b = b[ch] * (1.0f - wy) + e[ch] * wy;  // upsample_y at column xt2
-        o[ch] = z1a * (1.0f - wx) + z1b * wx;          // upsample_x
+    const float4* a = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt) * d.HD);
+    const float4* b = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt2) * d.HD);
+    const float4* c = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt) * d.HD);
+    const float4* e = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt2) * d.HD);
+    float4* o = reinterpret_cast<float4*>(zc + (size_t)cell * kZcStride);
+    const float uy = 1.0f - wy, ux = 1.0f - wx;
+#pragma unroll 4
+    for (int q = 0; q < d.HD / 4; q++) {
+        float4 A = a[q], B = b[q], Cc = c[q], E = e[q], r;
+        // upsample_y at columns xt and xt2, then upsample_x
+        r.x = (A.x * uy + Cc.x * wy) * ux + (B.x * uy + E.x * wy) * wx;
+        r.y = (A.y * uy + Cc.y * wy) * ux + (B.y * uy + E.y * wy) * wx;
+        r.z = (A.z * uy + Cc.z * wy) * ux + (B.z * uy + E.z * wy) * wx;
+        r.w = (A.w * uy + Cc.w * wy) * ux + (B.w * uy + E.w * wy) * wx;
+        o[q] = r;
     }
     size_t plane = (size_t)I.nx * I.ny;
-    for (int ch = 0; ch < d.C; ch++) o[d.HD + ch] = I.state[ch * plane + cl];
-    for (int ch = d.HD + d.C; ch < kZcStride; ch++) o[ch] = 0.f;
+    float tail[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int ch = 0; ch < d.C; ch++) tail[ch] = I.state[ch * plane + cl];
+    o[d.HD / 4] = make_float4(tail[0], tail[1], tail[2], tail[3]);
 }
 
 // head.conv2 (3x3, HD -> C, cpu.rs:348-349) then the step's residual
-// (cpu.rs:84-88), one thread per cell. c1 is [cells, HD].
-__global__ void conv2_step_kernel(Dims d, const float* __restrict__ c1, const float* __restrict__ w2,
-                                  const float* __restrict__ b2, const InstDev* inst, const int* cell_inst,
-                                  long long NC, int mode) {
-    extern __shared__ float ws[];  // [C][HD][9]
-    for (int i = threadIdx.x; i < d.C * d.HD * 9; i += blockDim.x) ws[i] = w2[i];
+// (cpu.rs:84-88). One CTA per 16x16 cell tile: the tile's c1 values plus a
+// one-cell halo are staged in shared memory; one thread per cell.
+__global__ void __launch_bounds__(256)
+conv2_step_kernel(Dims d, const float* __restrict__ c1, const float* __restrict__ w2, const float* __restrict__ b2,
+                  const InstDev* inst, int n_inst, int mode) {
+    extern __shared__ __align__(16) float sm[];
+    constexpr int S = kCellTile + 2;
+    const int HD = d.HD;
+    float* tile = sm;                  // [S][S][HD]
+    float* ws = sm + S * S * HD;       // [C][HD][9]
+    // instance and tile of this CTA
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].tile0 <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const InstDev& I = inst[lo];
+    const int tiles_x = (I.nx + kCellTile - 1) / kCellTile;
+    const int tl = blockIdx.x - I.tile0;
+    const int y0 = (tl / tiles_x) * kCellTile, x0 = (tl % tiles_x) * kCellTile;
+    for (int i = threadIdx.x; i < d.C * HD * 9; i += blockDim.x) ws[i] = w2[i];
+    const int q4 = HD / 4;
+    for (int e = threadIdx.x; e < S * S * q4; e += blockDim.x) {
+        int q = e % q4, p = e / q4, sy = p / S, sx = p % S;
+        int y = y0 + sy - 1, x = x0 + sx - 1;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (y >= 0 && x >= 0 && y < I.ny && x < I.nx)
+            v = reinterpret_cast<const float4*>(c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD)[q];
+        reinterpret_cast<float4*>(tile + (size_t)p * HD)[q] = v;
+    }
     __syncthreads();
-    long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= NC) return;
-    const InstDev& I = inst[cell_inst[cell]];
-    long long cl = cell - I.cell0;
-    int y = (int)(cl / I.nx), x = (int)(cl % I.nx);
+    const int ty = threadIdx.x / kCellTile, tx = threadIdx.x % kCellTile;
+    const int y = y0 + ty, x = x0 + tx;
+    if (y >= I.ny || x >= I.nx) return;
     float acc[4];
     for (int co = 0; co < d.C; co++) acc[co] = b2[co];
-    for (int ci = 0; ci < d.HD; ci++) {
+    for (int ci = 0; ci < HD; ci++) {
+#pragma unroll
         for (int ky = 0; ky < 3; ky++) {
-            int iy = y + ky - 1;
-            if (iy < 0 || iy >= I.ny) continue;
+            if (y + ky - 1 < 0 || y + ky - 1 >= I.ny) continue;
+#pragma unroll
             for (int kx = 0; kx < 3; kx++) {
-                int ix = x + kx - 1;
-                if (ix < 0 || ix >= I.nx) continue;
-                float a = c1[(size_t)(I.cell0 + (long long)iy * I.nx + ix) * d.HD + ci];
-                for (int co = 0; co < d.C; co++) acc[co] = fmaf(a, ws[(co * d.HD + ci) * 9 + ky * 3 + kx], acc[co]);
+                if (x + kx - 1 < 0 || x + kx - 1 >= I.nx) continue;
+                float a = tile[((ty + ky) * S + tx + kx) * HD + ci];
+                for (int co = 0; co < d.C; co++) acc[co] = fmaf(a, ws[(co * HD + ci) * 9 + ky * 3 + kx], acc[co]);
             }
         }
     }
-    size_t plane = (size_t)I.nx * I.ny;
+    const size_t plane = (size_t)I.nx * I.ny, cl = (size_t)y * I.nx + x;
     for (int co = 0; co < d.C; co++) {
         float v = acc[co];
         if (mode == kWriteNextState) v = v + I.state[co * plane + cl];
@@ -241,11 +330,12 @@ __device__ void energy_terms(const Dims& d, const float* s, long long n, double*
 // Mass then energy projection (eval.rs:148-153 order; project.rs:33-54) of
 // one instance per CTA, with f64 compensated sums; the shift and scale are
 // rounded to f32 and applied with the reference's f32 update.
-__global__ void projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, uint32_t flags, int init) {
+__global__ void __launch_bounds__(512) projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init) {
     __shared__ double red[32];
     const InstDev& I = inst[blockIdx.x];
-    ProjSlot& S = slots[I.proj];
+    ProjSlot& S = slots[blockIdx.x];
     float* s = I.state;
+    const unsigned flags = I.flags;
     const long long n = (long long)I.nx * I.ny;
     if (init) {
         Neu m;
@@ -301,55 +391,67 @@ __global__ void projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, 
 
 }  // namespace f32k
 
-template <int BM, int BN, int TM, int TN, class AL, class EP>
-static void gemm(const AL& a, const float* W, const float* b, int R, int N, int K, const EP& e, cudaStream_t s) {
-    dim3 grid((N + BN - 1) / BN, (R + BM - 1) / BM);
-    f32k::gemm_kernel<BM, BN, 16, TM, TN, AL, EP><<<grid, (BM / TM) * (BN / TN), 0, s>>>(a, W, b, R, N, K, e);
-    check_launch("gemm_f32");
+template <int BN, class AL, class EP>
+static void gemm(const char* name, const AL& a, const float* W, const float* b, int R, int N, int K, const EP& e,
+                 cudaStream_t s) {
+    KScope k(name, s);
+    dim3 grid((N + BN - 1) / BN, (R + 63) / 64);
+    f32k::gemm_kernel<BN, AL, EP><<<grid, BN * 4, 0, s>>>(a, W, b, R, N, K, e);
+    check_launch(name);
 }
 
 void forward_f32(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cudaStream_t s) {
     using namespace f32k;
-    const int R = p.R, D = d.D;
+    const int R = p.R, D = d.D, n = p.n_inst;
     {
+        KScope k("f32_embed", s);
         int pd = d.C * d.P * d.P;
         embed_kernel<<<(R + kEmbedTok - 1) / kEmbedTok, 128, kEmbedTok * pd * sizeof(float), s>>>(
-            d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, p.inst, p.row_inst, R, p.x);
+            d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, p.inst, n, R, p.x);
         check_launch("embed");
     }
     for (int l = 0; l < d.L; l++) {
         const auto& B = w.blk[l];
-        gemm<64, 64, 4, 4>(ALayerNorm{p.x, B.n1g, B.n1b, R, D}, B.wqkv, B.bqkv, R, 3 * D, D,
-                           EStore{p.qkv, 3 * D}, s);
+        gemm<64>("f32_ln_qkv", ALayerNorm{p.x, B.n1g, B.n1b, R, D}, B.wqkv, B.bqkv, R, 3 * D, D,
+                 EStore{p.qkv, 3 * D}, s);
         {
+            KScope k("f32_attention", s);
             long long warps = (long long)R * d.heads;
-            attention_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(d, p.qkv, p.inst, p.row_inst, R, p.attn);
+            attention_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(d, p.qkv, p.inst, n, R, p.attn);
             check_launch("attention");
         }
-        gemm<64, 64, 4, 4>(APlain{p.attn, D, R, D}, B.wp, B.bp, R, D, D, EResid{p.x, D}, s);
-        gemm<64, 64, 4, 4>(ALayerNorm{p.x, B.n2g, B.n2b, R, D}, B.w1, B.b1, R, d.F, D, EGelu{p.ff1, d.F}, s);
-        gemm<64, 64, 4, 4>(APlain{p.ff1, d.F, R, d.F}, B.w2, B.b2, R, D, d.F, EResid{p.x, D}, s);
+        gemm<64>("f32_proj", APlain{p.attn, D, R, D}, B.wp, B.bp, R, D, D, EResid{p.x, D}, s);
+        gemm<64>("f32_ln_ff1", ALayerNorm{p.x, B.n2g, B.n2b, R, D}, B.w1, B.b1, R, d.F, D, EGelu{p.ff1, d.F}, s);
+        gemm<64>("f32_ff2", APlain{p.ff1, d.F, R, d.F}, B.w2, B.b2, R, D, d.F, EResid{p.x, D}, s);
     }
-    layernorm_kernel<<<(R + 7) / 8, 256, 0, s>>>(p.x, w.norm_g, w.norm_b, R, D, p.xn);
-    check_launch("layernorm");
-    gemm<64, 64, 4, 4>(ATokConv3{p.xn, p.row_inst, p.inst, R, D}, w.tm_w, w.tm_b, R, D, 9 * D,
-                       EGeluResidFrom{p.xn, p.t1, D}, s);
-    gemm<64, 32, 4, 2>(APlain{p.t1, D, R, D}, w.tc_w, w.tc_b, R, d.HD, D, EStore{p.z0, d.HD}, s);
-    const long long NC = p.NC;
-    upsample_concat_kernel<<<(unsigned)((NC + 255) / 256), 256, 0, s>>>(d, p.z0, p.inst, p.cell_inst, NC, p.zc);
-    check_launch("upsample_concat");
     {
-        int Rc = (int)NC;
-        gemm<64, 32, 4, 2>(ACellConv3{p.zc, p.cell_inst, p.inst, Rc, kZcStride, d.HD + d.C}, w.c1_w, w.c1_b, Rc,
-                           d.HD, 9 * kZcStride, EGelu{p.c1, d.HD}, s);
+        KScope k("f32_final_ln", s);
+        layernorm_kernel<<<(R + 7) / 8, 256, 0, s>>>(p.x, w.norm_g, w.norm_b, R, D, p.xn);
+        check_launch("layernorm");
     }
-    conv2_step_kernel<<<(unsigned)((NC + 127) / 128), 128, d.C * d.HD * 9 * sizeof(float), s>>>(
-        d, p.c1, w.c2_w, w.c2_b, p.inst, p.cell_inst, NC, mode);
-    check_launch("conv2_step");
+    gemm<64>("f32_token_mix", ATokConv3{p.xn, p.inst, n, R, D}, w.tm_w, w.tm_b, R, D, 9 * D,
+             EGeluResidFrom{p.xn, p.t1, D}, s);
+    gemm<32>("f32_to_cells", APlain{p.t1, D, R, D}, w.tc_w, w.tc_b, R, d.HD, D, EStore{p.z0, d.HD}, s);
+    const long long NC = p.NC;
+    {
+        KScope k("f32_upsample_concat", s);
+        upsample_concat_kernel<<<(unsigned)((NC + 255) / 256), 256, 0, s>>>(d, p.z0, p.inst, n, NC, p.zc);
+        check_launch("upsample_concat");
+    }
+    gemm<32>("f32_conv1", ACellConv3{p.zc, p.inst, n, (int)NC, kZcStride}, w.c1_w, w.c1_b, (int)NC, d.HD,
+             9 * kZcStride, EGelu{p.c1, d.HD}, s);
+    {
+        KScope k("f32_conv2_step", s);
+        constexpr int S = kCellTile + 2;
+        size_t smem = ((size_t)S * S * d.HD + (size_t)d.C * d.HD * 9) * sizeof(float);
+        conv2_step_kernel<<<p.n_tiles, kCellTile * kCellTile, smem, s>>>(d, p.c1, w.c2_w, w.c2_b, p.inst, n, mode);
+        check_launch("conv2_step");
+    }
 }
 
-void projection(const Dims& d, const Pack& p, uint32_t flags, int init, cudaStream_t s) {
-    f32k::projection_kernel<<<p.n_inst, 1024, 0, s>>>(d, p.inst, p.proj, flags, init);
+void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
+    KScope k("projection", s);
+    f32k::projection_kernel<<<p.n_inst, 512, 0, s>>>(d, p.inst, p.proj, init);
     check_launch("projection");
 }
 

@@ -1,8 +1,11 @@
 // Host runtime: checkpoint parsing (crates/engine/src/weights.rs,
-// config.rs), device weight layouts, the single-instance launch pack and the
-// tick loop (crates/engine-cli/src/eval.rs:144-157) captured as CUDA graphs.
+// config.rs), device weight layouts, launch workspaces, the tick loop
+// (crates/engine-cli/src/eval.rs:144-157) captured as CUDA graphs, and the
+// batch runner.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <string>
 
 #include "bf16_path.hpp"
@@ -146,13 +149,16 @@ jc_config parse_config(const char* json, const TensorMap& t) {
                                       " is not divisible by the patch size " + std::to_string(c.patch));
     if (c.channels != 3) throw Error(JC_BAD_SHAPE, "channels must be 3 (h, u, v)");
     if (c.dim <= 0 || c.heads <= 0 || c.dim % c.heads) throw Error(JC_BAD_SHAPE, "dim must be a multiple of heads");
+    if (c.dim % 4 || c.dim / c.heads > 64) throw Error(JC_LIMIT, "dim must be a multiple of 4 and dim/heads <= 64");
     if (c.layers <= 0 || c.layers > kMaxLayers) throw Error(JC_LIMIT, "layers must be in [1, 32]");
     if (c.meta_dim <= 0 || c.meta_dim > 64) throw Error(JC_LIMIT, "meta_dim must be in [1, 64]");
     if (c.mask_kind == 1 && (c.mask_radius < 0 || c.mask_dilation < 1))
         throw Error(JC_BAD_CHECKPOINT, "stencil radius must be >= 0 and dilation >= 1");
     c.head_dim = (int32_t)get(t, "head.to_cells.weight").shape.at(0);
     c.ff_inner = (int32_t)get(t, "blocks.0.ff1.weight").shape.at(1);
-    if (c.head_dim + c.channels > kZcStride) throw Error(JC_LIMIT, "cell-head width + channels must be <= 36");
+    if (c.head_dim % 4 || c.head_dim + c.channels > kZcStride)
+        throw Error(JC_LIMIT, "cell-head width must be a multiple of 4 and at most 33");
+    if (c.ff_inner % 4) throw Error(JC_LIMIT, "the MLP width must be a multiple of 4");
 
     const int64_t D = c.dim, F = c.ff_inner, HD = c.head_dim, C = c.channels, P = c.patch;
     const int64_t T = (int64_t)(c.nx / P) * (c.ny / P);
@@ -188,7 +194,7 @@ jc_config parse_config(const char* json, const TensorMap& t) {
 
 void* DeviceArena::alloc(size_t bytes) {
     void* p = nullptr;
-    cuda_check(cudaMalloc(&p, bytes ? bytes : 16), "cudaMalloc", JC_OVER_BUDGET);
+    cuda_check(cudaMalloc(&p, bytes ? (bytes + 255) / 256 * 256 : 256), "cudaMalloc", JC_OVER_BUDGET);
     ptrs.push_back(p);
     return p;
 }
@@ -199,8 +205,91 @@ float* DeviceArena::upload(const std::vector<float>& v) {
     return d;
 }
 
+void DeviceArena::release(void* p) {
+    auto it = std::find(ptrs.begin(), ptrs.end(), p);
+    if (it != ptrs.end()) {
+        cudaFree(p);
+        ptrs.erase(it);
+    }
+}
+
 DeviceArena::~DeviceArena() {
     for (void* p : ptrs) cudaFree(p);
+}
+
+int cell_tiles(int nx, int ny) {
+    return ((nx + kCellTile - 1) / kCellTile) * ((ny + kCellTile - 1) / kCellTile);
+}
+
+int conv_tiles(int w, int h) { return ((w + kConvTX - 1) / kConvTX) * ((h + kConvTY - 1) / kConvTY); }
+
+void Workspace::alloc(DeviceArena& a, const Dims& d, int rows, long long cells, int inst, const BF16Path* bf) {
+    max_rows = rows;
+    max_cells = cells;
+    max_inst = inst;
+    Pack& p = base;
+    p = Pack{};
+    const size_t R = (size_t)rows, NC = (size_t)cells;
+    p.inst = a.alloc_n<InstDev>(inst);
+    p.proj = a.alloc_n<ProjSlot>(inst);
+    p.x = a.alloc_n<float>(R * d.D);
+    p.z0 = a.alloc_n<float>(R * d.HD);
+    p.err = a.alloc_n<int>(1);
+    cuda_check(cudaMemset(p.err, 0, sizeof(int)), "cudaMemset");
+    if (bf) {
+        bf->alloc_workspace(a, d, p, rows, cells, inst);
+    } else {
+        p.qkv = a.alloc_n<float>(R * 3 * d.D);
+        p.attn = a.alloc_n<float>(R * d.D);
+        p.ff1 = a.alloc_n<float>(R * d.F);
+        p.xn = a.alloc_n<float>(R * d.D);
+        p.t1 = a.alloc_n<float>(R * d.D);
+        p.zc = a.alloc_n<float>(NC * kZcStride);
+        p.c1 = a.alloc_n<float>(NC * d.HD);
+    }
+    states = a.alloc_n<float>(3 * NC);
+    metas = a.alloc_n<float>((size_t)inst * 64);
+}
+
+void Workspace::check_timeout(cudaStream_t s) const {
+    int e = 0;
+    cuda_check(cudaMemcpyAsync(&e, base.err, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag", JC_MAP);
+    cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
+    if (e) {
+        cudaMemsetAsync(base.err, 0, sizeof(int), s);
+        cudaStreamSynchronize(s);
+        throw Error(JC_DEVICE_TIMEOUT, "a device-side wait exceeded its time limit; results of this call are invalid");
+    }
+}
+
+Pack Workspace::view(const Dims& d, int inst_base, int n, int row_base, int rows, long long cell_base,
+                     long long cells, int tiles, int ttiles, int ctiles) const {
+    Pack p = base;
+    auto off = [](float* q, size_t o) { return q ? q + o : q; };
+    p.n_inst = n;
+    p.R = rows;
+    p.NC = cells;
+    p.n_tiles = tiles;
+    p.n_ttiles = ttiles;
+    p.n_ctiles = ctiles;
+    if (base.tmaps) p.tmaps = static_cast<char*>(base.tmaps) + (size_t)inst_base * 2 * 128;
+    p.inst = base.inst + inst_base;
+    p.proj = base.proj + inst_base;
+    const size_t r = (size_t)row_base, c = (size_t)cell_base;
+    p.x = off(base.x, r * d.D);
+    p.qkv = off(base.qkv, r * 3 * d.D);
+    p.attn = off(base.attn, r * d.D);
+    p.ff1 = off(base.ff1, r * d.F);
+    p.xn = off(base.xn, r * d.D);
+    p.t1 = off(base.t1, r * d.D);
+    p.z0 = off(base.z0, r * d.HD);
+    p.zc = off(base.zc, c * kZcStride);
+    p.c1 = off(base.c1, c * d.HD);
+    for (int i = 0; i < Pack::kTokBufs; i++)
+        if (base.bt[i]) p.bt[i] = base.bt[i] + r * base.bt_stride[i];
+    for (int i = 0; i < Pack::kCellBufs; i++)
+        if (base.bc[i]) p.bc[i] = base.bc[i] + c * base.bc_stride[i];
+    return p;
 }
 
 static void require_device() {
@@ -218,48 +307,54 @@ static void require_device() {
                                       " sm_" + std::to_string(prop.major) + std::to_string(prop.minor));
 }
 
-Model::Model(const uint8_t* st, size_t st_len, const char* config_json, int prec) {
-    if (prec != JC_FP32 && prec != JC_BF16) throw Error(JC_BAD_ARGUMENT, "precision must be JC_FP32 or JC_BF16");
-    TensorMap t = parse_safetensors(st, st_len);
-    cfg = parse_config(config_json, t);
-    precision = prec;
-    require_device();
-
-    dims.D = cfg.dim;
-    dims.L = cfg.layers;
-    dims.heads = cfg.heads;
-    dims.F = cfg.ff_inner;
-    dims.HD = cfg.head_dim;
-    dims.C = cfg.channels;
-    dims.P = cfg.patch;
-    dims.meta_dim = cfg.meta_dim;
-    dims.mask_kind = cfg.mask_kind;
-    dims.radius = cfg.mask_radius;
-    dims.dilation = cfg.mask_dilation;
-    for (int i = 0; i < 3; i++) {
-        dims.norm_mean[i] = cfg.norm_mean[i];
-        dims.norm_std[i] = cfg.norm_std[i];
+static uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
+    const uint8_t* p = static_cast<const uint8_t*>(data);
+    for (size_t i = 0; i < n; i++) {
+        h ^= p[i];
+        h *= 1099511628211ull;
     }
-    dims.norm_depth = cfg.norm_depth;
-    dims.g = cfg.g;
-    dims.energy_r_max = cfg.energy_r_max;
+    return h;
+}
 
-    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+static Dims dims_of(const jc_config& cfg) {
+    Dims d{};
+    d.D = cfg.dim;
+    d.L = cfg.layers;
+    d.heads = cfg.heads;
+    d.F = cfg.ff_inner;
+    d.HD = cfg.head_dim;
+    d.C = cfg.channels;
+    d.P = cfg.patch;
+    d.meta_dim = cfg.meta_dim;
+    d.mask_kind = cfg.mask_kind;
+    d.radius = cfg.mask_radius;
+    d.dilation = cfg.mask_dilation;
+    for (int i = 0; i < 3; i++) {
+        d.norm_mean[i] = cfg.norm_mean[i];
+        d.norm_std[i] = cfg.norm_std[i];
+    }
+    d.norm_depth = cfg.norm_depth;
+    d.g = cfg.g;
+    d.energy_r_max = cfg.energy_r_max;
+    return d;
+}
 
+static void upload_weights(const TensorMap& t, const Dims& dims, DeviceArena& arena, DeviceWeights& w) {
     const int D = dims.D, HD = dims.HD, C = dims.C;
-    auto up = [&](const char* n) { return arena.upload(get(t, n).data); };
-    wf32.embed_w = up("embed.weight");
-    wf32.embed_b = up("embed.bias");
-    wf32.meta_w = up("meta.weight");
-    wf32.meta_b = up("meta.bias");
-    d_pos = up("pos");
+    WeightsF32& f = w.f32;
+    auto up = [&](const std::string& n) { return arena.upload(get(t, n).data); };
+    f.embed_w = up("embed.weight");
+    f.embed_b = up("embed.bias");
+    f.meta_w = up("meta.weight");
+    f.meta_b = up("meta.bias");
+    w.pos = up("pos");
     for (int l = 0; l < dims.L; l++) {
         std::string p = "blocks." + std::to_string(l) + ".";
-        auto& B = wf32.blk[l];
-        B.n1g = up((p + "norm1.gamma").c_str());
-        B.n1b = up((p + "norm1.beta").c_str());
-        // q, k, v concatenated along the output axis, as one [D, 3D] matrix
-        // (the fused q/k/v of crates/engine/src/gpu.rs:288-301).
+        auto& B = f.blk[l];
+        B.n1g = up(p + "norm1.gamma");
+        B.n1b = up(p + "norm1.beta");
+        // q, k, v concatenated along the output axis, one [D, 3D] matrix
+        // (the fused q/k/v of crates/engine/src/gpu.rs:288-301)
         const auto &wq = get(t, p + "q.weight").data, &wk = get(t, p + "k.weight").data,
                    &wv = get(t, p + "v.weight").data;
         std::vector<float> wqkv((size_t)D * 3 * D), bqkv(3 * D);
@@ -276,79 +371,91 @@ Model::Model(const uint8_t* st, size_t st_len, const char* config_json, int prec
         }
         B.wqkv = arena.upload(wqkv);
         B.bqkv = arena.upload(bqkv);
-        B.wp = up((p + "proj.weight").c_str());
-        B.bp = up((p + "proj.bias").c_str());
-        B.n2g = up((p + "norm2.gamma").c_str());
-        B.n2b = up((p + "norm2.beta").c_str());
-        B.w1 = up((p + "ff1.weight").c_str());
-        B.b1 = up((p + "ff1.bias").c_str());
-        B.w2 = up((p + "ff2.weight").c_str());
-        B.b2 = up((p + "ff2.bias").c_str());
+        B.wp = up(p + "proj.weight");
+        B.bp = up(p + "proj.bias");
+        B.n2g = up(p + "norm2.gamma");
+        B.n2b = up(p + "norm2.beta");
+        B.w1 = up(p + "ff1.weight");
+        B.b1 = up(p + "ff1.bias");
+        B.w2 = up(p + "ff2.weight");
+        B.b2 = up(p + "ff2.bias");
     }
-    wf32.norm_g = up("norm.gamma");
-    wf32.norm_b = up("norm.beta");
+    f.norm_g = up("norm.gamma");
+    f.norm_b = up("norm.beta");
     {
         // token_mix [co][ci][ky][kx] -> [(ky*3+kx)*D + ci][co]
-        const auto& w = get(t, "head.token_mix.weight").data;
+        const auto& src = get(t, "head.token_mix.weight").data;
         std::vector<float> r((size_t)9 * D * D);
         for (int co = 0; co < D; co++)
             for (int ci = 0; ci < D; ci++)
-                for (int k = 0; k < 9; k++) r[((size_t)k * D + ci) * D + co] = w[((size_t)co * D + ci) * 9 + k];
-        wf32.tm_w = arena.upload(r);
-        wf32.tm_b = up("head.token_mix.bias");
+                for (int k = 0; k < 9; k++) r[((size_t)k * D + ci) * D + co] = src[((size_t)co * D + ci) * 9 + k];
+        f.tm_w = arena.upload(r);
+        f.tm_b = up("head.token_mix.bias");
     }
     {
-        const auto& w = get(t, "head.to_cells.weight").data;  // [HD][D][1][1] -> [D][HD]
+        const auto& src = get(t, "head.to_cells.weight").data;  // [HD][D][1][1] -> [D][HD]
         std::vector<float> r((size_t)D * HD);
         for (int co = 0; co < HD; co++)
-            for (int ci = 0; ci < D; ci++) r[(size_t)ci * HD + co] = w[(size_t)co * D + ci];
-        wf32.tc_w = arena.upload(r);
-        wf32.tc_b = up("head.to_cells.bias");
+            for (int ci = 0; ci < D; ci++) r[(size_t)ci * HD + co] = src[(size_t)co * D + ci];
+        f.tc_w = arena.upload(r);
+        f.tc_b = up("head.to_cells.bias");
     }
     {
         // conv1 [HD][HD+C][3][3] -> [(tap*kZcStride + ci)][HD], zero rows for the pad channel
-        const auto& w = get(t, "head.conv1.weight").data;
+        const auto& src = get(t, "head.conv1.weight").data;
         const int cin = HD + C;
         std::vector<float> r((size_t)9 * kZcStride * HD, 0.0f);
         for (int co = 0; co < HD; co++)
             for (int ci = 0; ci < cin; ci++)
-                for (int k = 0; k < 9; k++) r[((size_t)k * kZcStride + ci) * HD + co] = w[((size_t)co * cin + ci) * 9 + k];
-        wf32.c1_w = arena.upload(r);
-        wf32.c1_b = up("head.conv1.bias");
+                for (int k = 0; k < 9; k++)
+                    r[((size_t)k * kZcStride + ci) * HD + co] = src[((size_t)co * cin + ci) * 9 + k];
+        f.c1_w = arena.upload(r);
+        f.c1_b = up("head.conv1.bias");
     }
-    wf32.c2_w = up("head.conv2.weight");
-    wf32.c2_b = up("head.conv2.bias");
+    f.c2_w = up("head.conv2.weight");
+    f.c2_b = up("head.conv2.bias");
+    uint64_t h = 1469598103934665603ull;
+    for (auto& kv : t) {
+        if (kv.first == "pos") continue;
+        h = fnv1a(h, kv.first.data(), kv.first.size());
+        h = fnv1a(h, kv.second.data.data(), kv.second.data.size() * 4);
+    }
+    w.shared_hash = h;
+}
 
-    if (precision == JC_BF16) bf16 = std::make_unique<BF16Path>(dims, t, arena);
+// ---------------------------------------------------------------------------
+// Model: one checkpoint, one grid, one request at a time.
 
-    // single-instance pack over the model's own grid
+Model::Model(const uint8_t* st, size_t st_len, const char* config_json, int prec) {
+    if (prec != JC_FP32 && prec != JC_BF16) throw Error(JC_BAD_ARGUMENT, "precision must be JC_FP32 or JC_BF16");
+    TensorMap t = parse_safetensors(st, st_len);
+    cfg = parse_config(config_json, t);
+    precision = prec;
+    require_device();
+    dims = dims_of(cfg);
+    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    upload_weights(t, dims, arena, w);
+    if (precision == JC_BF16) w.bf16 = std::make_unique<BF16Path>(dims, t, arena);
+
     const int tx = cfg.nx / cfg.patch, ty = cfg.ny / cfg.patch;
-    pack.n_inst = 1;
-    pack.R = tx * ty;
-    pack.NC = (long long)cfg.nx * cfg.ny;
-    state_len = (size_t)C * cfg.nx * cfg.ny;
-    alloc_pack_workspace(pack);
-    d_state = arena.alloc_n<float>(state_len);
-    d_inc = arena.alloc_n<float>(state_len);
-    d_meta = arena.alloc_n<float>(64);
-    host_inst.row0 = 0;
-    host_inst.tx = tx;
-    host_inst.ty = ty;
-    host_inst.nx = cfg.nx;
-    host_inst.ny = cfg.ny;
-    host_inst.cell0 = 0;
-    host_inst.pos = d_pos;
-    host_inst.meta = d_meta;
-    host_inst.proj = 0;
-    {
-        std::vector<int> zeros_r(pack.R, 0);
-        cuda_check(cudaMemcpy(pack.row_inst, zeros_r.data(), zeros_r.size() * sizeof(int), cudaMemcpyHostToDevice),
-                   "upload row table", JC_MAP);
-        std::vector<int> zeros_c((size_t)pack.NC, 0);
-        cuda_check(cudaMemcpy(pack.cell_inst, zeros_c.data(), zeros_c.size() * sizeof(int), cudaMemcpyHostToDevice),
-                   "upload cell table", JC_MAP);
-    }
-    cuda_check(cudaMallocHost(&h_pinned, (2 * state_len + 64) * sizeof(float)), "cudaMallocHost", JC_OVER_BUDGET);
+    const long long cells = (long long)cfg.nx * cfg.ny;
+    state_len = (size_t)dims.C * cells;
+    ws_.alloc(arena, dims, tx * ty, cells + 0, 1, w.bf16.get());
+    pack_ = ws_.view(dims, 0, 1, 0, tx * ty, 0, cells, cell_tiles(cfg.nx, cfg.ny), conv_tiles(tx, ty),
+                     conv_tiles(cfg.nx, cfg.ny));
+    inst_.row0 = 0;
+    inst_.tx = tx;
+    inst_.ty = ty;
+    inst_.nx = cfg.nx;
+    inst_.ny = cfg.ny;
+    inst_.cell0 = 0;
+    inst_.pos = w.pos;
+    inst_.tile0 = 0;
+    inst_.tt0 = 0;
+    inst_.ct0 = 0;
+    if (w.bf16) w.bf16->prepare(dims, pack_, &inst_, stream);
+    d_inc_ = arena.alloc_n<float>(state_len);
+    cuda_check(cudaMallocHost(&h_pinned_, (2 * state_len + 64) * sizeof(float)), "cudaMallocHost", JC_OVER_BUDGET);
 }
 
 Model::~Model() {
@@ -357,35 +464,7 @@ Model::~Model() {
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);
     }
-    if (h_pinned) cudaFreeHost(h_pinned);
-}
-
-void Model::alloc_pack_workspace(Pack& p) {
-    const size_t R = (size_t)p.R, NC = (size_t)p.NC;
-    const int D = dims.D;
-    p.inst = arena.alloc_n<InstDev>(p.n_inst);
-    p.row_inst = arena.alloc_n<int>(R);
-    p.cell_inst = arena.alloc_n<int>(NC);
-    p.proj = arena.alloc_n<ProjSlot>(p.n_inst);
-    p.x = arena.alloc_n<float>(R * D);
-    p.qkv = arena.alloc_n<float>(R * 3 * D);
-    p.attn = arena.alloc_n<float>(R * D);
-    p.ff1 = arena.alloc_n<float>(R * dims.F);
-    p.xn = arena.alloc_n<float>(R * D);
-    p.t1 = arena.alloc_n<float>(R * D);
-    p.z0 = arena.alloc_n<float>(R * dims.HD);
-    p.zc = arena.alloc_n<float>(NC * kZcStride);
-    p.c1 = arena.alloc_n<float>(NC * dims.HD);
-}
-
-void Model::set_single_instance(float* state, float* out, const float* meta) {
-    InstDev i = host_inst;
-    i.state = state;
-    i.out = out;
-    i.meta = meta;
-    // pageable source: the call returns once the bytes are staged
-    cuda_check(cudaMemcpyAsync(pack.inst, &i, sizeof(i), cudaMemcpyHostToDevice, stream), "instance descriptor",
-               JC_MAP);
+    if (h_pinned_) cudaFreeHost(h_pinned_);
 }
 
 void Model::meta_of(float* out) const {
@@ -396,26 +475,39 @@ void Model::meta_of(float* out) const {
     out[4] = std::log(cfg.nu + 1e-6f);
 }
 
-void Model::forward_pack(const Pack& p, int mode, cudaStream_t s) {
-    if (precision == JC_BF16) bf16->forward(dims, wf32, p, mode, s);
-    else forward_f32(dims, wf32, p, mode, s);
+void Model::forward_pack(const Pack& p, int mode, cudaStream_t s) const {
+    if (precision == JC_BF16) w.bf16->forward(dims, w.f32, p, mode, s);
+    else forward_f32(dims, w.f32, p, mode, s);
+}
+
+void Model::put_instance(float* state, float* out, const float* meta, uint32_t flags, cudaStream_t s) {
+    InstDev i = inst_;
+    i.state = state;
+    i.out = out;
+    i.meta = meta;
+    i.flags = flags;
+    // pageable source: the call returns once the bytes are staged
+    cuda_check(cudaMemcpyAsync(pack_.inst, &i, sizeof(i), cudaMemcpyHostToDevice, s), "instance descriptor", JC_MAP);
 }
 
 void Model::forward_host(const float* state, const float* meta, float* inc) {
     if (!state || !meta || !inc) throw Error(JC_BAD_ARGUMENT, "null buffer");
-    float* hs = h_pinned;
-    float* hm = h_pinned + 2 * state_len;
-    std::memcpy(hs, state, state_len * sizeof(float));
-    std::memcpy(hm, meta, cfg.meta_dim * sizeof(float));
-    cuda_check(cudaMemcpyAsync(d_state, hs, state_len * sizeof(float), cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
-    cuda_check(cudaMemcpyAsync(d_meta, hm, cfg.meta_dim * sizeof(float), cudaMemcpyHostToDevice, stream), "H2D",
-               JC_MAP);
-    set_single_instance(d_state, d_inc, d_meta);
-    forward_pack(pack, kWriteIncrement, stream);
-    cuda_check(cudaMemcpyAsync(hs + state_len, d_inc, state_len * sizeof(float), cudaMemcpyDeviceToHost, stream),
-               "D2H", JC_MAP);
+    float* hs = h_pinned_;
+    float* ho = h_pinned_ + state_len;
+    float* hm = h_pinned_ + 2 * state_len;
+    float* d_state = ws_.states;
+    float* d_meta = ws_.metas;
+    float* d_inc = d_inc_;
+    std::memcpy(hs, state, state_len * 4);
+    std::memcpy(hm, meta, cfg.meta_dim * 4);
+    cuda_check(cudaMemcpyAsync(d_state, hs, state_len * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
+    cuda_check(cudaMemcpyAsync(d_meta, hm, cfg.meta_dim * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
+    put_instance(d_state, d_inc, d_meta, 0, stream);
+    forward_pack(pack_, kWriteIncrement, stream);
+    cuda_check(cudaMemcpyAsync(ho, d_inc, state_len * 4, cudaMemcpyDeviceToHost, stream), "D2H", JC_MAP);
     cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize", JC_POLL);
-    std::memcpy(inc, hs + state_len, state_len * sizeof(float));
+    ws_.check_timeout(stream);
+    std::memcpy(inc, ho, state_len * 4);
 }
 
 void Model::step_host(const float* state, const float* meta, float* next) {
@@ -423,24 +515,42 @@ void Model::step_host(const float* state, const float* meta, float* next) {
     for (size_t i = 0; i < state_len; i++) next[i] += state[i];  // cpu.rs:84-88
 }
 
-void Model::enqueue_rollout(int ticks, uint32_t flags, double* d_energies_out, float* d_traj, cudaStream_t s) {
-    projection(dims, pack, flags, 1, s);
-    if (d_energies_out)
-        cuda_check(cudaMemcpyAsync(d_energies_out, &pack.proj[0].energy, sizeof(double), cudaMemcpyDeviceToDevice, s),
-                   "energy record");
-    if (d_traj) cuda_check(cudaMemcpyAsync(d_traj, d_state, state_len * 4, cudaMemcpyDeviceToDevice, s), "traj");
+void Model::enqueue_rollout(int ticks, double* e, float* traj, cudaStream_t s) {
+    projection(dims, pack_, 1, s);
+    if (e) cuda_check(cudaMemcpyAsync(e, &pack_.proj[0].energy, 8, cudaMemcpyDeviceToDevice, s), "energy record");
+    if (traj) cuda_check(cudaMemcpyAsync(traj, ws_.states, state_len * 4, cudaMemcpyDeviceToDevice, s), "traj");
     for (int t = 1; t <= ticks; t++) {
-        forward_pack(pack, kWriteNextState, s);
-        projection(dims, pack, flags, 0, s);
-        if (d_energies_out)
-            cuda_check(cudaMemcpyAsync(d_energies_out + t, &pack.proj[0].energy, sizeof(double),
-                                       cudaMemcpyDeviceToDevice, s),
+        forward_pack(pack_, kWriteNextState, s);
+        projection(dims, pack_, 0, s);
+        if (e)
+            cuda_check(cudaMemcpyAsync(e + t, &pack_.proj[0].energy, 8, cudaMemcpyDeviceToDevice, s),
                        "energy record");
-        if (d_traj)
-            cuda_check(cudaMemcpyAsync(d_traj + (size_t)t * state_len, d_state, state_len * 4,
+        if (traj)
+            cuda_check(cudaMemcpyAsync(traj + (size_t)t * state_len, ws_.states, state_len * 4,
                                        cudaMemcpyDeviceToDevice, s),
                        "traj");
     }
+}
+
+cudaGraphExec_t Model::graph_for(const GraphKey& key, double* e, float* traj) {
+    auto it = graphs_.find(key);
+    if (it != graphs_.end()) return it->second;
+    cudaGraph_t g;
+    cuda_check(cudaStreamBeginCapture(key.s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try {
+        enqueue_rollout(key.ticks, e, traj, key.s);
+    } catch (...) {
+        cudaStreamEndCapture(key.s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    cuda_check(cudaStreamEndCapture(key.s, &g), "end capture");
+    cudaGraphExec_t ge;
+    cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    cuda_check(err, "graph instantiate");
+    graphs_.emplace(key, ge);
+    return ge;
 }
 
 void Model::rollout_device(const float* d_x0, const float* d_meta_in, int ticks, uint32_t flags, float* d_final,
@@ -448,38 +558,13 @@ void Model::rollout_device(const float* d_x0, const float* d_meta_in, int ticks,
     if (ticks < 0) throw Error(JC_BAD_ARGUMENT, "ticks must be >= 0");
     if (flags & ~3u) throw Error(JC_BAD_ARGUMENT, "unknown rollout flag");
     if (!s) s = stream;
-    if (d_x0 != d_state)
-        cuda_check(cudaMemcpyAsync(d_state, d_x0, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy x0");
-    if (d_meta_in != d_meta)
-        cuda_check(cudaMemcpyAsync(d_meta, d_meta_in, cfg.meta_dim * 4, cudaMemcpyDeviceToDevice, s), "copy meta");
-    {
-        InstDev i = host_inst;
-        i.state = d_state;
-        i.out = d_state;
-        i.meta = d_meta;
-        cuda_check(cudaMemcpyAsync(pack.inst, &i, sizeof(i), cudaMemcpyHostToDevice, s), "instance descriptor",
-                   JC_MAP);
-    }
-    GraphKey key{ticks, flags, d_energies_out, nullptr, s};
-    auto it = graphs_.find(key);
-    if (it == graphs_.end()) {
-        cudaGraph_t g;
-        cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-        try {
-            enqueue_rollout(ticks, flags, d_energies_out, nullptr, s);
-        } catch (...) {
-            cudaStreamEndCapture(s, &g);
-            throw;
-        }
-        cuda_check(cudaStreamEndCapture(s, &g), "end capture");
-        cudaGraphExec_t ge;
-        cuda_check(cudaGraphInstantiate(&ge, g, 0), "graph instantiate");
-        cudaGraphDestroy(g);
-        it = graphs_.emplace(key, ge).first;
-    }
-    cuda_check(cudaGraphLaunch(it->second, s), "graph launch");
-    if (d_final && d_final != d_state)
-        cuda_check(cudaMemcpyAsync(d_final, d_state, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy final");
+    cuda_check(cudaMemcpyAsync(ws_.states, d_x0, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy x0");
+    cuda_check(cudaMemcpyAsync(ws_.metas, d_meta_in, cfg.meta_dim * 4, cudaMemcpyDeviceToDevice, s), "copy meta");
+    put_instance(ws_.states, ws_.states, ws_.metas, flags, s);
+    cuda_check(cudaGraphLaunch(graph_for(GraphKey{ticks, d_energies_out, nullptr, s}, d_energies_out, nullptr), s),
+               "graph launch");
+    if (d_final)
+        cuda_check(cudaMemcpyAsync(d_final, ws_.states, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy final");
 }
 
 void Model::rollout_host(const float* x0, const float* meta, int ticks, uint32_t flags, float* final_state,
@@ -487,70 +572,353 @@ void Model::rollout_host(const float* x0, const float* meta, int ticks, uint32_t
     if (!x0 || !meta || !final_state) throw Error(JC_BAD_ARGUMENT, "null buffer");
     if (ticks < 0) throw Error(JC_BAD_ARGUMENT, "ticks must be >= 0");
     if (flags & ~3u) throw Error(JC_BAD_ARGUMENT, "unknown rollout flag");
-    if (energies && ticks + 1 > energies_cap) {
-        energies_cap = ticks + 1;
-        d_energies = arena.alloc_n<double>((size_t)energies_cap);
+    if (energies && ticks + 1 > energies_cap_) {
+        if (d_energies_) arena.release(d_energies_);
+        energies_cap_ = ticks + 1;
+        d_energies_ = arena.alloc_n<double>((size_t)energies_cap_);
     }
-    float* hs = h_pinned;
-    float* hm = h_pinned + 2 * state_len;
+    float* hs = h_pinned_;
+    float* ho = h_pinned_ + state_len;
+    float* hm = h_pinned_ + 2 * state_len;
     std::memcpy(hs, x0, state_len * 4);
     std::memcpy(hm, meta, cfg.meta_dim * 4);
-    cuda_check(cudaMemcpyAsync(d_state, hs, state_len * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
-    cuda_check(cudaMemcpyAsync(d_meta, hm, cfg.meta_dim * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
-    {
-        InstDev i = host_inst;
-        i.state = d_state;
-        i.out = d_state;
-        i.meta = d_meta;
-        cuda_check(cudaMemcpyAsync(pack.inst, &i, sizeof(i), cudaMemcpyHostToDevice, stream), "descriptor", JC_MAP);
-    }
-    float* d_traj = nullptr;
-    if (traj) d_traj = arena.alloc_n<float>((size_t)(ticks + 1) * state_len);
-    GraphKey key{ticks, flags, energies ? d_energies : nullptr, d_traj, stream};
-    auto it = graphs_.find(key);
-    if (it == graphs_.end()) {
-        cudaGraph_t g;
-        cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        try {
-            enqueue_rollout(ticks, flags, energies ? d_energies : nullptr, d_traj, stream);
-        } catch (...) {
-            cudaStreamEndCapture(stream, &g);
-            throw;
+    cuda_check(cudaMemcpyAsync(ws_.states, hs, state_len * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
+    cuda_check(cudaMemcpyAsync(ws_.metas, hm, cfg.meta_dim * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
+    put_instance(ws_.states, ws_.states, ws_.metas, flags, stream);
+    float* d_traj = traj ? arena.alloc_n<float>((size_t)(ticks + 1) * state_len) : nullptr;
+    double* e = energies ? d_energies_ : nullptr;
+    GraphKey key{ticks, e, d_traj, stream};
+    try {
+        cuda_check(cudaGraphLaunch(graph_for(key, e, d_traj), stream), "graph launch");
+        cuda_check(cudaMemcpyAsync(ho, ws_.states, state_len * 4, cudaMemcpyDeviceToHost, stream), "D2H", JC_MAP);
+        if (energies)
+            cuda_check(cudaMemcpyAsync(energies, d_energies_, (size_t)(ticks + 1) * 8, cudaMemcpyDeviceToHost, stream),
+                       "D2H", JC_MAP);
+        if (traj)
+            cuda_check(cudaMemcpyAsync(traj, d_traj, (size_t)(ticks + 1) * state_len * 4, cudaMemcpyDeviceToHost,
+                                       stream),
+                       "D2H", JC_MAP);
+        cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize", JC_POLL);
+        ws_.check_timeout(stream);
+    } catch (...) {
+        if (d_traj) {
+            auto it = graphs_.find(key);
+            if (it != graphs_.end()) {
+                cudaGraphExecDestroy(it->second);
+                graphs_.erase(it);
+            }
+            arena.release(d_traj);
         }
-        cuda_check(cudaStreamEndCapture(stream, &g), "end capture");
-        cudaGraphExec_t ge;
-        cuda_check(cudaGraphInstantiate(&ge, g, 0), "graph instantiate");
-        cudaGraphDestroy(g);
-        it = graphs_.emplace(key, ge).first;
+        throw;
     }
-    cuda_check(cudaGraphLaunch(it->second, stream), "graph launch");
-    cuda_check(cudaMemcpyAsync(hs + state_len, d_state, state_len * 4, cudaMemcpyDeviceToHost, stream), "D2H", JC_MAP);
-    if (energies)
-        cuda_check(cudaMemcpyAsync(energies, d_energies, (size_t)(ticks + 1) * 8, cudaMemcpyDeviceToHost, stream),
-                   "D2H", JC_MAP);
-    if (traj)
-        cuda_check(cudaMemcpyAsync(traj, d_traj, (size_t)(ticks + 1) * state_len * 4, cudaMemcpyDeviceToHost, stream),
-                   "D2H", JC_MAP);
-    cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize", JC_POLL);
-    std::memcpy(final_state, hs + state_len, state_len * 4);
-    if (traj) {
-        // drop the per-call trajectory buffer's graph (its pointer is not reused)
+    std::memcpy(final_state, ho, state_len * 4);
+    if (d_traj) {
+        // the trajectory buffer is per call: drop it and its graph
+        auto it = graphs_.find(key);
         cudaGraphExecDestroy(it->second);
         graphs_.erase(it);
-        cudaFree(d_traj);
-        arena.ptrs.pop_back();
+        arena.release(d_traj);
     }
 }
 
 void Model::forward_device(const float* d_state_in, const float* d_meta_in, float* d_inc_out, cudaStream_t s) {
     if (!d_state_in || !d_meta_in || !d_inc_out) throw Error(JC_BAD_ARGUMENT, "null buffer");
     if (!s) s = stream;
-    InstDev i = host_inst;
-    i.state = const_cast<float*>(d_state_in);
-    i.out = d_inc_out;
-    i.meta = d_meta_in;
-    cuda_check(cudaMemcpyAsync(pack.inst, &i, sizeof(i), cudaMemcpyHostToDevice, s), "descriptor", JC_MAP);
-    forward_pack(pack, kWriteIncrement, s);
+    put_instance(const_cast<float*>(d_state_in), d_inc_out, d_meta_in, 0, s);
+    forward_pack(pack_, kWriteIncrement, s);
+}
+
+std::map<std::string, std::pair<int, double>> Model::profile_forward(int iters) {
+    KernelTimer kt;
+    put_instance(ws_.states, d_inc_, ws_.metas, 0, stream);
+    g_ktimer = &kt;
+    try {
+        for (int i = 0; i < iters; i++) forward_pack(pack_, kWriteIncrement, stream);
+    } catch (...) {
+        g_ktimer = nullptr;
+        throw;
+    }
+    g_ktimer = nullptr;
+    return kt.summary();
+}
+
+// ---------------------------------------------------------------------------
+// Batch
+
+Batch::Batch(jc_model* const* models, int n_models, int max_inst, long long max_cells) {
+    if (!models || n_models <= 0) throw Error(JC_BAD_ARGUMENT, "a batch needs at least one model");
+    if (max_inst <= 0 || max_cells <= 0) throw Error(JC_BAD_ARGUMENT, "max_instances and max_cells must be > 0");
+    for (int i = 0; i < n_models; i++) {
+        if (!models[i]) throw Error(JC_BAD_ARGUMENT, "null model in the list");
+        models_.push_back(models[i]->m);
+    }
+    const Model& m0 = *models_[0];
+    dims_ = m0.dims;
+    precision_ = m0.precision;
+    for (Model* m : models_) {
+        const Dims& d = m->dims;
+        bool same = d.D == dims_.D && d.L == dims_.L && d.heads == dims_.heads && d.F == dims_.F &&
+                    d.HD == dims_.HD && d.C == dims_.C && d.P == dims_.P && d.meta_dim == dims_.meta_dim &&
+                    d.mask_kind == dims_.mask_kind && d.radius == dims_.radius && d.dilation == dims_.dilation &&
+                    d.norm_depth == dims_.norm_depth && d.g == dims_.g && d.energy_r_max == dims_.energy_r_max &&
+                    m->precision == precision_;
+        for (int i = 0; i < 3; i++)
+            same = same && d.norm_mean[i] == dims_.norm_mean[i] && d.norm_std[i] == dims_.norm_std[i];
+        if (!same)
+            throw Error(JC_BAD_ARGUMENT,
+                        "models of a batch must share hyper-parameters, mask, normalizer, g, energy_r_max and precision");
+    }
+    for (int i = 0; i < n_models; i++) {
+        int g = i;
+        for (int j = 0; j < i; j++)
+            if (models_[j]->w.shared_hash == models_[i]->w.shared_hash) {
+                g = group_of_[j];
+                break;
+            }
+        group_of_.push_back(g);
+    }
+    const int pp = dims_.P * dims_.P;
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    ws_.alloc(arena_, dims_, (int)(max_cells / pp) + 1, max_cells, max_inst, m0.w.bf16.get());
+    cuda_check(cudaMallocHost(&h_states_, 3 * (size_t)max_cells * 4), "cudaMallocHost", JC_OVER_BUDGET);
+    cuda_check(cudaMallocHost(&h_metas_, (size_t)max_inst * 64 * 4), "cudaMallocHost", JC_OVER_BUDGET);
+    cuda_check(cudaMallocHost(&h_slots_, (size_t)max_inst * sizeof(ProjSlot)), "cudaMallocHost", JC_OVER_BUDGET);
+}
+
+Batch::~Batch() {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+    if (h_states_) cudaFreeHost(h_states_);
+    if (h_metas_) cudaFreeHost(h_metas_);
+    if (h_slots_) cudaFreeHost(h_slots_);
+}
+
+Batch::Plan Batch::plan(const jc_instance* in, int n) const {
+    if (n < 0 || (n > 0 && !in)) throw Error(JC_BAD_ARGUMENT, "bad instance list");
+    if (n > ws_.max_inst) throw Error(JC_OVER_BUDGET, "more instances than the batch was created for");
+    Plan p;
+    // group order: first appearance
+    std::vector<int> gorder;
+    for (int i = 0; i < n; i++) {
+        const jc_instance& x = in[i];
+        if (x.model < 0 || x.model >= (int)models_.size()) throw Error(JC_BAD_ARGUMENT, "instance model index out of range");
+        if (x.ticks < 0) throw Error(JC_BAD_ARGUMENT, "instance ticks must be >= 0");
+        if (x.flags & ~3u) throw Error(JC_BAD_ARGUMENT, "unknown instance flag");
+        if (!x.x0 || !x.meta || !x.final_state) throw Error(JC_BAD_ARGUMENT, "null instance buffer");
+        int g = group_of_[x.model];
+        if (std::find(gorder.begin(), gorder.end(), g) == gorder.end()) gorder.push_back(g);
+    }
+    int inst_base = 0, row_base = 0;
+    long long cell_base = 0, state_off = 0;
+    for (int g : gorder) {
+        std::vector<int> idx;
+        for (int i = 0; i < n; i++)
+            if (group_of_[in[i].model] == g) idx.push_back(i);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return in[a].ticks > in[b].ticks; });
+        Plan::Group G;
+        G.model = g;
+        G.inst_base = inst_base;
+        G.n = (int)idx.size();
+        G.row_base = row_base;
+        G.cell_base = cell_base;
+        G.cell_base_i = 0;
+        int rows = 0, tiles = 0, ttiles = 0, ctiles = 0;
+        long long cells = 0;
+        for (int i : idx) {
+            const Model& m = *models_[in[i].model];
+            InstDev d{};
+            d.row0 = rows;
+            d.tx = m.cfg.nx / m.cfg.patch;
+            d.ty = m.cfg.ny / m.cfg.patch;
+            d.nx = m.cfg.nx;
+            d.ny = m.cfg.ny;
+            d.cell0 = cells;
+            d.state = ws_.states + state_off;
+            d.out = d.state;
+            d.pos = m.w.pos;
+            d.meta = ws_.metas + (size_t)(inst_base + (int)p.order.size() - G.inst_base) * 64;
+            d.flags = in[i].flags;
+            d.tile0 = tiles;
+            d.tt0 = ttiles;
+            d.ct0 = ctiles;
+            p.inst.push_back(d);
+            p.order.push_back(i);
+            p.state_off.push_back(state_off);
+            rows += d.tx * d.ty;
+            cells += (long long)d.nx * d.ny;
+            tiles += cell_tiles(d.nx, d.ny);
+            ttiles += conv_tiles(d.tx, d.ty);
+            ctiles += conv_tiles(d.nx, d.ny);
+            state_off += 3LL * d.nx * d.ny;
+            G.ticks.push_back(in[i].ticks);
+            G.rows.push_back(rows);
+            G.cells.push_back(cells);
+            G.tiles.push_back(tiles);
+            G.ttiles.push_back(ttiles);
+            G.ctiles.push_back(ctiles);
+            p.max_ticks = std::max(p.max_ticks, in[i].ticks);
+        }
+        inst_base += G.n;
+        row_base += rows;
+        cell_base += cells;
+        if (row_base > ws_.max_rows || cell_base > ws_.max_cells)
+            throw Error(JC_OVER_BUDGET, "the instances need more cells than the batch was created for");
+        p.groups.push_back(std::move(G));
+    }
+    // meta slots follow the packed order
+    for (size_t k = 0; k < p.inst.size(); k++) p.inst[k].meta = ws_.metas + k * 64;
+    return p;
+}
+
+void Batch::enqueue(const Plan& p, cudaStream_t s) const {
+    for (const auto& G : p.groups) {
+        if (G.n == 0) continue;
+        Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
+                          G.tiles.back(), G.ttiles.back(), G.ctiles.back());
+        projection(dims_, v, 1, s);
+    }
+    for (int t = 1; t <= p.max_ticks; t++) {
+        for (const auto& G : p.groups) {
+            int na = 0;
+            while (na < G.n && G.ticks[na] >= t) na++;
+            if (na == 0) continue;
+            Pack v = ws_.view(dims_, G.inst_base, na, G.row_base, G.rows[na - 1], G.cell_base, G.cells[na - 1],
+                              G.tiles[na - 1], G.ttiles[na - 1], G.ctiles[na - 1]);
+            models_[G.model]->forward_pack(v, kWriteNextState, s);
+            projection(dims_, v, 0, s);
+        }
+    }
+}
+
+void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t s) {
+    if (!s) s = stream_;
+    Plan p = plan(in, n);
+    if (n == 0) return;
+    const int md = dims_.meta_dim;
+    long long total = 0;
+    for (size_t k = 0; k < p.order.size(); k++) {
+        const jc_instance& x = in[p.order[k]];
+        const InstDev& d = p.inst[k];
+        size_t len = 3 * (size_t)d.nx * d.ny;
+        if (device_ptrs) {
+            cuda_check(cudaMemcpyAsync(ws_.states + p.state_off[k], x.x0, len * 4, cudaMemcpyDeviceToDevice, s),
+                       "copy x0");
+            cuda_check(cudaMemcpyAsync(ws_.metas + k * 64, x.meta, md * 4, cudaMemcpyDeviceToDevice, s), "copy meta");
+        } else {
+            std::memcpy(h_states_ + p.state_off[k], x.x0, len * 4);
+            std::memcpy(h_metas_ + k * 64, x.meta, md * 4);
+        }
+        total = p.state_off[k] + (long long)len;
+    }
+    if (!device_ptrs) {
+        cuda_check(cudaMemcpyAsync(ws_.states, h_states_, (size_t)total * 4, cudaMemcpyHostToDevice, s), "H2D", JC_MAP);
+        cuda_check(cudaMemcpyAsync(ws_.metas, h_metas_, p.order.size() * 64 * 4, cudaMemcpyHostToDevice, s), "H2D",
+                   JC_MAP);
+    }
+    cuda_check(cudaMemcpyAsync(ws_.base.inst, p.inst.data(), p.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
+                               s),
+               "instance descriptors", JC_MAP);
+    prepare_maps(p, s);
+    std::vector<long long> key;
+    key.push_back((long long)(uintptr_t)s);
+    for (const auto& G : p.groups) {
+        key.push_back(-1 - G.model);
+        for (size_t k = 0; k < G.ticks.size(); k++) {
+            const InstDev& d = p.inst[G.inst_base + k];
+            key.push_back(((long long)d.nx << 40) | ((long long)d.ny << 20) | G.ticks[k]);
+            key.push_back((long long)(uintptr_t)d.pos);
+        }
+    }
+    auto it = graphs_.find(key);
+    if (it == graphs_.end()) {
+        cudaGraph_t g;
+        cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try {
+            enqueue(p, s);
+        } catch (...) {
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        cuda_check(cudaStreamEndCapture(s, &g), "end capture");
+        cudaGraphExec_t ge;
+        cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(err, "graph instantiate");
+        it = graphs_.emplace(key, ge).first;
+    }
+    cuda_check(cudaGraphLaunch(it->second, s), "graph launch");
+    if (device_ptrs) {
+        for (size_t k = 0; k < p.order.size(); k++) {
+            const InstDev& d = p.inst[k];
+            cuda_check(cudaMemcpyAsync(in[p.order[k]].final_state, ws_.states + p.state_off[k],
+                                       3 * (size_t)d.nx * d.ny * 4, cudaMemcpyDeviceToDevice, s),
+                       "copy final");
+        }
+    } else {
+        cuda_check(cudaMemcpyAsync(h_states_, ws_.states, (size_t)total * 4, cudaMemcpyDeviceToHost, s), "D2H",
+                   JC_MAP);
+    }
+    cuda_check(cudaMemcpyAsync(h_slots_, ws_.base.proj, p.order.size() * sizeof(ProjSlot), cudaMemcpyDeviceToHost, s),
+               "D2H", JC_MAP);
+    cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
+    ws_.check_timeout(s);
+    for (size_t k = 0; k < p.order.size(); k++) {
+        const jc_instance& x = in[p.order[k]];
+        const InstDev& d = p.inst[k];
+        if (!device_ptrs) std::memcpy(x.final_state, h_states_ + p.state_off[k], 3 * (size_t)d.nx * d.ny * 4);
+        if (x.energy) {
+            x.energy[0] = h_slots_[k].energy;
+            x.energy[1] = h_slots_[k].max_viol;
+        }
+    }
+}
+
+std::map<std::string, std::pair<int, double>> Batch::profile(const jc_instance* in, int n, bool device_ptrs) {
+    (void)device_ptrs;
+    Plan p = plan(in, n);
+    cudaStream_t s = stream_;
+    for (size_t k = 0; k < p.order.size(); k++) {
+        const jc_instance& x = in[p.order[k]];
+        const InstDev& d = p.inst[k];
+        size_t len = 3 * (size_t)d.nx * d.ny;
+        cuda_check(cudaMemcpyAsync(ws_.states + p.state_off[k], x.x0, len * 4,
+                                   device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
+                   "copy x0");
+        cuda_check(cudaMemcpyAsync(ws_.metas + k * 64, x.meta, dims_.meta_dim * 4,
+                                   device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
+                   "copy meta");
+    }
+    cuda_check(cudaMemcpyAsync(ws_.base.inst, p.inst.data(), p.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
+                               s),
+               "instance descriptors", JC_MAP);
+    prepare_maps(p, s);
+    KernelTimer kt;
+    g_ktimer = &kt;
+    try {
+        enqueue(p, s);
+    } catch (...) {
+        g_ktimer = nullptr;
+        throw;
+    }
+    g_ktimer = nullptr;
+    auto out = kt.summary();
+    ws_.check_timeout(s);
+    return out;
+}
+
+void Batch::prepare_maps(const Plan& p, cudaStream_t s) const {
+    const Model& m0 = *models_[0];
+    if (!m0.w.bf16) return;
+    for (const auto& G : p.groups) {
+        if (G.n == 0) continue;
+        Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
+                          G.tiles.back(), G.ttiles.back(), G.ctiles.back());
+        m0.w.bf16->prepare(dims_, v, p.inst.data() + G.inst_base, s);
+    }
 }
 
 }  // namespace jc

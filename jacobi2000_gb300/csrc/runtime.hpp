@@ -1,5 +1,5 @@
 // Host runtime of the engine: checkpoint parsing, device weights, launch
-// packs and the rollout loop.
+// workspaces, the rollout loop and the batch runner.
 #pragma once
 
 #include <map>
@@ -36,17 +36,49 @@ TensorMap parse_safetensors(const uint8_t* p, size_t n);
 // (grid divisible by the patch, every tensor present with its expected shape).
 jc_config parse_config(const char* json, const TensorMap& t);
 
-// A device allocation owned by a Model.
+// Device allocations owned by one object, freed with it.
 struct DeviceArena {
     std::vector<void*> ptrs;
     void* alloc(size_t bytes);
     template <class T>
     T* alloc_n(size_t n) { return static_cast<T*>(alloc(n * sizeof(T))); }
     float* upload(const std::vector<float>& v);
+    void release(void* p);
     ~DeviceArena();
 };
 
 class BF16Path;  // tensor-core forward (bf16_path.cu)
+class Model;
+
+// Launch workspace for packs of up to max_rows token rows, max_cells cells
+// and max_inst instances, plus the state/meta slabs of those instances.
+struct Workspace {
+    int max_rows = 0, max_inst = 0;
+    long long max_cells = 0;
+    Pack base{};            // pointers at offset 0; packs are views into it
+    float* states = nullptr;  // [3 * max_cells]
+    float* metas = nullptr;   // [max_inst * 64]
+    void alloc(DeviceArena& a, const Dims& d, int rows, long long cells, int inst, const BF16Path* bf);
+    // A pack view over rows [row_base, ...), cells [cell_base, ...) and
+    // instances [inst_base, inst_base + n), with the given tile counts.
+    Pack view(const Dims& d, int inst_base, int n, int row_base, int rows, long long cell_base, long long cells,
+              int tiles, int ttiles, int ctiles) const;
+    // Throws JC_DEVICE_TIMEOUT (and clears the flag) when a device-side wait
+    // gave up since the last check; `s` must be idle.
+    void check_timeout(cudaStream_t s) const;
+};
+
+// Tile counts of one instance's grids.
+int cell_tiles(int nx, int ny);   // 16x16 cells
+int conv_tiles(int w, int h);     // 8x16 positions
+
+// Device weights of one checkpoint.
+struct DeviceWeights {
+    WeightsF32 f32{};
+    const float* pos = nullptr;  // [T, D]
+    std::unique_ptr<BF16Path> bf16;
+    uint64_t shared_hash = 0;    // hash of every tensor but `pos`
+};
 
 class Model {
    public:
@@ -57,6 +89,9 @@ class Model {
     Dims dims{};
     int precision = JC_FP32;
     cudaStream_t stream = nullptr;
+    DeviceArena arena;
+    DeviceWeights w;
+    size_t state_len = 0;
 
     void meta_of(float* out) const;
     void forward_host(const float* state, const float* meta, float* inc);
@@ -66,41 +101,83 @@ class Model {
     void forward_device(const float* d_state, const float* d_meta, float* d_inc, cudaStream_t s);
     void rollout_device(const float* d_x0, const float* d_meta, int ticks, uint32_t flags, float* d_final,
                         double* d_energies, cudaStream_t s);
+    // Per-kernel device time of `iters` forwards of this model's grid.
+    std::map<std::string, std::pair<int, double>> profile_forward(int iters);
 
     // Forward of every instance of a pack with this model's weights.
-    void forward_pack(const Pack& p, int mode, cudaStream_t s);
-
-    // Device weights.
-    DeviceArena arena;
-    WeightsF32 wf32{};
-    const float* d_pos = nullptr;  // [T, D]
-    std::unique_ptr<BF16Path> bf16;
-
-    // Single-instance pack over this model's own grid.
-    Pack pack{};
-    InstDev host_inst{};
-    float *d_state = nullptr, *d_inc = nullptr, *d_meta = nullptr;
-    double* d_energies = nullptr;
-    int energies_cap = 0;
-    float* h_pinned = nullptr;  // staging for host calls: state | meta | out
-    size_t state_len = 0;
+    void forward_pack(const Pack& p, int mode, cudaStream_t s) const;
 
    private:
-    void alloc_pack_workspace(Pack& p);
-    void set_single_instance(float* state, float* out, const float* meta);
-    void enqueue_rollout(int ticks, uint32_t flags, double* d_energies_out, float* d_traj, cudaStream_t s);
-    // cached rollout graphs: key = (ticks, flags, energies?, traj?)
+    Workspace ws_;
+    Pack pack_{};
+    InstDev inst_{};
+    float* d_inc_ = nullptr;
+    double* d_energies_ = nullptr;
+    int energies_cap_ = 0;
+    float* h_pinned_ = nullptr;  // staging for host calls: state | out | meta
+    void put_instance(float* state, float* out, const float* meta, uint32_t flags, cudaStream_t s);
+    void enqueue_rollout(int ticks, double* d_energies_out, float* d_traj, cudaStream_t s);
     struct GraphKey {
-        int ticks; uint32_t flags; const void* e; const void* t; cudaStream_t s;
+        int ticks;
+        const void* e;
+        const void* t;
+        cudaStream_t s;
         bool operator<(const GraphKey& o) const {
             if (ticks != o.ticks) return ticks < o.ticks;
-            if (flags != o.flags) return flags < o.flags;
             if (e != o.e) return e < o.e;
             if (t != o.t) return t < o.t;
             return s < o.s;
         }
     };
     std::map<GraphKey, cudaGraphExec_t> graphs_;
+    cudaGraphExec_t graph_for(const GraphKey& k, double* e, float* t);
+};
+
+// Many instances of (possibly) different grids, one launch sequence per tick.
+// Instances whose models share every tensor but `pos` share launches.
+class Batch {
+   public:
+    Batch(jc_model* const* models, int n_models, int max_inst, long long max_cells);
+    ~Batch();
+    void rollout(const jc_instance* inst, int n, bool device_ptrs, cudaStream_t s);
+    std::map<std::string, std::pair<int, double>> profile(const jc_instance* inst, int n, bool device_ptrs);
+
+   private:
+    std::vector<Model*> models_;
+    std::vector<int> group_of_;  // model -> weight group (index of its first model)
+    Dims dims_{};
+    int precision_ = JC_FP32;
+    DeviceArena arena_;
+    Workspace ws_;
+    cudaStream_t stream_ = nullptr;
+    float* h_states_ = nullptr;  // pinned [3 * max_cells]
+    float* h_metas_ = nullptr;   // pinned [max_inst * 64]
+    ProjSlot* h_slots_ = nullptr;
+    struct Plan {
+        std::vector<int> order;     // caller index of each packed instance
+        std::vector<InstDev> inst;  // packed descriptors
+        struct Group {
+            int model, inst_base, n, row_base, cell_base_i;
+            long long cell_base;
+            std::vector<int> ticks;     // per packed instance, descending
+            std::vector<int> rows, tiles, ttiles, ctiles;
+            std::vector<long long> cells;  // prefix ends
+        };
+        std::vector<Group> groups;
+        std::vector<long long> state_off;  // per packed instance, floats
+        int max_ticks = 0;
+    };
+    Plan plan(const jc_instance* inst, int n) const;
+    void enqueue(const Plan& p, cudaStream_t s) const;
+    void prepare_maps(const Plan& p, cudaStream_t s) const;
+    std::map<std::vector<long long>, cudaGraphExec_t> graphs_;
 };
 
 }  // namespace jc
+
+struct jc_model {
+    jc::Model* m;
+};
+struct jc_batch {
+    jc::Batch* b;
+};

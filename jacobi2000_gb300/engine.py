@@ -194,3 +194,101 @@ def project_energy(x, prev_energy: float, config: JcConfig, cells: int) -> np.nd
     y = np.array(x, dtype=np.float32, copy=True)
     load_library().jc_project_energy(y.reshape(-1), float(prev_energy), C.byref(config), int(cells))
     return y
+
+
+class JcInstance(C.Structure):
+    _fields_ = [("model", C.c_int32), ("ticks", C.c_int32), ("flags", C.c_uint32), ("reserved", C.c_int32),
+                ("x0", C.c_void_p), ("meta", C.c_void_p), ("final_state", C.c_void_p), ("energy", C.c_void_p)]
+
+
+def _declare_batch(L):
+    if getattr(L, "_batch_declared", False):
+        return
+    vp = C.c_void_p
+    L.jc_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int64, C.POINTER(vp)]
+    L.jc_batch_create.restype = C.c_int
+    L.jc_batch_destroy.argtypes = [vp]
+    L.jc_batch_destroy.restype = None
+    L.jc_batch_rollout.argtypes = [vp, C.POINTER(JcInstance), C.c_int32, C.c_int32, vp]
+    L.jc_batch_rollout.restype = C.c_int
+    L.jc_batch_profile.argtypes = [vp, C.POINTER(JcInstance), C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]
+    L.jc_batch_profile.restype = C.c_int
+    L._batch_declared = True
+
+
+EXPORTED += ["jc_batch_create", "jc_batch_destroy", "jc_batch_rollout", "jc_batch_profile"]
+
+
+class Batch:
+    """Many rollouts stepped together (jc_batch_*). ``models`` share every
+    hyper-parameter; instances are (model index, x0, meta, ticks, flags)."""
+
+    def __init__(self, models, max_instances: int, max_cells: int):
+        L = load_library()
+        _declare_batch(L)
+        self._L = L
+        self.models = list(models)
+        arr = (C.c_void_p * len(self.models))(*[m._h.value for m in self.models])
+        h = C.c_void_p()
+        _check(L.jc_batch_create(arr, len(self.models), int(max_instances), int(max_cells), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.jc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _instances(self, items, device: bool):
+        n = len(items)
+        arr = (JcInstance * n)()
+        keep = []
+        outs = []
+        for k, it in enumerate(items):
+            mi, x0, meta, ticks = it[0], it[1], it[2], it[3]
+            flags = it[4] if len(it) > 4 else PROJECT_MASS | PROJECT_ENERGY
+            m = self.models[mi]
+            e = np.zeros(2, dtype=np.float64)
+            if device:
+                # (x0, meta, final) are device pointers (ints)
+                x0p, metap, outp = int(x0), int(meta), int(it[5])
+                out = None
+            else:
+                xa = m._state(x0)
+                ma = m._meta(meta)
+                out = np.empty(m.shape, dtype=np.float32)
+                keep += [xa, ma]
+                x0p, metap, outp = xa.ctypes.data, ma.ctypes.data, out.ctypes.data
+            arr[k] = JcInstance(int(mi), int(ticks), int(flags), 0, x0p, metap, outp, e.ctypes.data)
+            keep.append(e)
+            outs.append((out, e))
+        return arr, keep, outs
+
+    def rollout(self, items, device: bool = False, stream: int | None = None):
+        """Returns [(final_state, final_energy, max_violation)] in input order
+        (final_state is None with device pointers)."""
+        arr, keep, outs = self._instances(items, device)
+        _check(self._L.jc_batch_rollout(self._h, arr, len(items), int(device), stream))
+        return [(o, float(e[0]), float(e[1])) for o, e in outs]
+
+    def profile(self, items, device: bool = False) -> dict:
+        """{kernel name: (launches, total device ms)} for one run of ``items``."""
+        arr, keep, outs = self._instances(items, device)
+        buf = C.create_string_buffer(1 << 16)
+        _check(self._L.jc_batch_profile(self._h, arr, len(items), int(device), buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split(",")
+            out[name] = (int(n), float(ms))
+        return out
