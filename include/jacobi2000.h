@@ -153,6 +153,24 @@ jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
 jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n,
                            int32_t device_pointers, char* report, size_t cap);
 
+/* The forward pass of jc_forward_device, with f32 arithmetic, for callers that
+ * cannot allocate device memory at call time: code recording a CUDA stream
+ * capture (cudaMalloc cannot be captured and breaks a global or thread-local
+ * capture) and processes whose own pool allocator owns the whole device.
+ * This entry point has no counterpart in the reference. It allocates nothing:
+ * every intermediate buffer lives in one fixed 12 MiB device array inside
+ * the library, which every GPU that loads the library holds until the process
+ * exits. Grids whose buffers exceed 12 MiB are refused with JC_LIMIT (the
+ * dim 128, 4-layer model fits grids up to 128 x 128 cells). All calls share
+ * that array: calls that overlap on the GPU (on different streams, or from
+ * different threads) race and corrupt each other's results; serialise them.
+ * The first call on each device looks up the array's device address, so make
+ * that first call before any stream capture begins. Pointers are device
+ * pointers; `stream` is a cudaStream_t (null = the legacy default stream);
+ * the call enqueues and returns. */
+jc_status jc_forward_device_noalloc(jc_model* m, const float* d_state, const float* d_meta,
+                                    float* d_increment, void* stream);
+
 /* Host-side projections, engine::project (crates/engine/src/project.rs:22-54),
  * with f64 compensated sums. n = cells per channel; x is [3, n]. */
 double jc_mass(const float* x, int64_t n);

@@ -119,6 +119,12 @@ jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta,
     return guard([&] { m->m->rollout_device(d_x0, d_meta, ticks, flags, d_final, d_energies, (cudaStream_t)stream); });
 }
 
+jc_status jc_forward_device_noalloc(jc_model* m, const float* d_state, const float* d_meta, float* d_increment,
+                                    void* stream) {
+    if (!m) return fail(JC_BAD_ARGUMENT, "model is null");
+    return guard([&] { jc::forward_noalloc(*m->m, d_state, d_meta, d_increment, (cudaStream_t)stream); });
+}
+
 jc_status jc_batch_create(jc_model* const* models, int32_t n_models, int32_t max_instances, int64_t max_cells,
                           jc_batch** out) {
     if (!out) return fail(JC_BAD_ARGUMENT, "out is null");

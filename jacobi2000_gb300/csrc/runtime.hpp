@@ -173,6 +173,10 @@ class Batch {
     std::map<std::vector<long long>, cudaGraphExec_t> graphs_;
 };
 
+// The FP32 forward of m's own grid with every buffer in the library's fixed
+// no-alloc scratch array (noalloc.cu); allocates nothing.
+void forward_noalloc(const Model& m, const float* d_state, const float* d_meta, float* d_inc, cudaStream_t s);
+
 }  // namespace jc
 
 struct jc_model {

@@ -216,7 +216,8 @@ def _declare_batch(L):
     L._batch_declared = True
 
 
-EXPORTED += ["jc_batch_create", "jc_batch_destroy", "jc_batch_rollout", "jc_batch_profile"]
+EXPORTED += ["jc_batch_create", "jc_batch_destroy", "jc_batch_rollout", "jc_batch_profile",
+             "jc_forward_device_noalloc"]
 
 
 class Batch:
