@@ -18,7 +18,7 @@ LIB = PKG / "libjacobi2000.so"
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr",
          "-I", str(ROOT / "include")]
 
 SOURCES = ["fp32_path.cu", "bf16_path.cu", "runtime.cu", "noalloc.cu", "capi.cpp"]

@@ -18,6 +18,7 @@
 // addressed through a shifted shared-memory descriptor.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <stdexcept>
@@ -115,71 +116,86 @@ constexpr int kHaloPlane = (kHaloW * kHaloH * 16 + 127) / 128 * 128;
 
 __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 
-// Token embedding and the first LayerNorm. One warp per token row; lane
-// handles outputs lane + 32 j.
+// Token embedding and the first LayerNorm (cpu.rs:253-280, 289). One CTA per
+// 64 token rows: the embed weights and the 64 patches are staged in shared
+// memory (patches gathered x-contiguously from the state), then one warp per
+// token computes its D outputs (lane handles o = lane + 32 j), adds pos and
+// the meta linear, writes x (f32) and LayerNorm(x) (bf16).
+constexpr int kEmbedRows = 64;
+
 template <int DPL>
 __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __restrict__ We,
                                                        const float* __restrict__ be, const float* __restrict__ Wm,
                                                        const float* __restrict__ bm, const float* __restrict__ g,
                                                        const float* __restrict__ b, const InstDev* inst, int n_inst,
                                                        int R, float* __restrict__ x, bf16* __restrict__ ln) {
-    const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (r >= R) return;
-    const InstDev& I = inst[inst_of_row(inst, n_inst, r)];
-    const int t = r - I.row0, pd = d.C * d.P * d.P;
-    const int ty0 = (t / I.tx) * d.P, tx0 = (t % I.tx) * d.P;
-    float p0 = 0.f, p1 = 0.f;
-    {
-        int f = lane;
-        if (f < pd) {
-            int c = f / (d.P * d.P), py = (f / d.P) % d.P, px = f % d.P;
-            p0 = I.state[((size_t)c * I.ny + ty0 + py) * I.nx + tx0 + px];
+    extern __shared__ float esm[];
+    const int D = d.D, P = d.P, pd = d.C * P * P;
+    float* sW = esm;                 // [pd][D]
+    float* sP = esm + (size_t)pd * D;  // [kEmbedRows][pd]
+    __shared__ int rinst[kEmbedRows];
+    const int r0 = blockIdx.x * kEmbedRows;
+    for (int i = threadIdx.x; i < pd * D; i += blockDim.x) sW[i] = We[i];
+    if (threadIdx.x < kEmbedRows)
+        rinst[threadIdx.x] = r0 + (int)threadIdx.x < R ? inst_of_row(inst, n_inst, r0 + threadIdx.x) : -1;
+    __syncthreads();
+    for (int e = threadIdx.x; e < kEmbedRows * pd; e += blockDim.x) {
+        const int px = e % P, i = (e / P) % kEmbedRows, cpy = e / (P * kEmbedRows);
+        const int c = cpy / P, py = cpy % P;
+        float v = 0.f;
+        if (rinst[i] >= 0) {
+            const InstDev& I = inst[rinst[i]];
+            const int t = r0 + i - I.row0;
+            const int y = (t / I.tx) * P + py, xx = (t % I.tx) * P + px;
+            v = I.state[((size_t)c * I.ny + y) * I.nx + xx];
         }
-        f = lane + 32;
-        if (f < pd) {
-            int c = f / (d.P * d.P), py = (f / d.P) % d.P, px = f % d.P;
-            p1 = I.state[((size_t)c * I.ny + ty0 + py) * I.nx + tx0 + px];
-        }
+        sP[i * pd + c * P * P + py * P + px] = v;
     }
-    const int D = d.D;
-    float v[DPL];
-#pragma unroll
-    for (int j = 0; j < DPL; j++) {
-        int o = lane + 32 * j;
-        v[j] = o < D ? be[o] : 0.f;
-    }
-    for (int f = 0; f < pd; f++) {
-        float p = __shfl_sync(0xffffffffu, f < 32 ? p0 : p1, f & 31);
-        const float* w = We + (size_t)f * D;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = warp; i < kEmbedRows; i += (int)(blockDim.x >> 5)) {
+        const int r = r0 + i;
+        if (r >= R) break;
+        const InstDev& I = inst[rinst[i]];
+        const int t = r - I.row0;
+        float v[DPL];
 #pragma unroll
         for (int j = 0; j < DPL; j++) {
-            int o = lane + 32 * j;
-            if (o < D) v[j] = fmaf(p, w[o], v[j]);
+            const int o = lane + 32 * j;
+            v[j] = o < D ? be[o] : 0.f;
         }
-    }
-    float s = 0.f;
+        const float* pp = sP + i * pd;
+        for (int f = 0; f < pd; f++) {
+            const float pv = pp[f];
 #pragma unroll
-    for (int j = 0; j < DPL; j++) {
-        int o = lane + 32 * j;
-        if (o < D) {
-            float m = bm[o];
-            for (int f = 0; f < d.meta_dim; f++) m = fmaf(I.meta[f], Wm[(size_t)f * D + o], m);
-            v[j] = (v[j] + I.pos[(size_t)t * D + o]) + m;
-            x[(size_t)r * D + o] = v[j];
-            s += v[j];
+            for (int j = 0; j < DPL; j++) {
+                const int o = lane + 32 * j;
+                if (o < D) v[j] = fmaf(pv, sW[f * D + o], v[j]);
+            }
         }
-    }
-    const float mean = warp_sum(s) / (float)D;
-    float q = 0.f;
+        float sum = 0.f;
 #pragma unroll
-    for (int j = 0; j < DPL; j++)
-        if (lane + 32 * j < D) q += (v[j] - mean) * (v[j] - mean);
-    const float rstd = 1.0f / sqrtf(warp_sum(q) / (float)D + 1e-5f);
+        for (int j = 0; j < DPL; j++) {
+            const int o = lane + 32 * j;
+            if (o < D) {
+                float m = bm[o];
+                for (int f = 0; f < d.meta_dim; f++) m = fmaf(I.meta[f], Wm[(size_t)f * D + o], m);
+                v[j] = (v[j] + I.pos[(size_t)t * D + o]) + m;
+                x[(size_t)r * D + o] = v[j];
+                sum += v[j];
+            }
+        }
+        const float mean = warp_sum(sum) / (float)D;
+        float q = 0.f;
 #pragma unroll
-    for (int j = 0; j < DPL; j++) {
-        int o = lane + 32 * j;
-        if (o < D) ln[(size_t)r * D + o] = __float2bfloat16((v[j] - mean) * rstd * g[o] + b[o]);
+        for (int j = 0; j < DPL; j++)
+            if (lane + 32 * j < D) q += (v[j] - mean) * (v[j] - mean);
+        const float rstd = 1.0f / sqrtf(warp_sum(q) / (float)D + 1e-5f);
+#pragma unroll
+        for (int j = 0; j < DPL; j++) {
+            const int o = lane + 32 * j;
+            if (o < D) ln[(size_t)r * D + o] = __float2bfloat16((v[j] - mean) * rstd * g[o] + b[o]);
+        }
     }
 }
 
@@ -283,6 +299,93 @@ __global__ void __launch_bounds__(256) bf_attention_kernel(Dims d, const bf16* _
     BfVec<FPL>::store(out + (size_t)r * D + lane * FPL, acc);
 }
 
+// Radius-1 stencil (3 x 3 candidates, any dilation), unrolled: the nine key
+// and value vectors are loaded up front as packed bf16 words, then scores,
+// max, exp, denominator and the (e / denom)-weighted sum follow the
+// reference's order (cpu.rs:121-158).
+template <int FPL>
+__global__ void __launch_bounds__(256) bf_attention_r1_kernel(Dims d, const bf16* __restrict__ qkv,
+                                                              const InstDev* inst, int n_inst, int R,
+                                                              bf16* __restrict__ out) {
+    constexpr int W = FPL / 2 > 0 ? FPL / 2 : 1;  // 32-bit words per lane per vector
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (r >= R) return;
+    const int D = d.D, D3 = 3 * D;
+    const int lph = 32 / d.heads;
+    const InstDev& I = inst[inst_of_row(inst, n_inst, r)];
+    const int t = r - I.row0, qy = t / I.tx, qx = t % I.tx, dil = d.dilation;
+    const float scale = 1.0f / sqrtf((float)(D / d.heads));
+    float q[FPL];
+    BfVec<FPL>::load(qkv + (size_t)r * D3 + lane * FPL, q);
+    uint32_t kw[9][W], vw[9][W];
+    bool in[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int ky = qy + (j / 3 - 1) * dil, kx = qx + (j % 3 - 1) * dil;
+        in[j] = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
+        const size_t kr = in[j] ? (size_t)(I.row0 + ky * I.tx + kx) : (size_t)r;
+        const bf16* kp = qkv + kr * D3 + D + lane * FPL;
+        const bf16* vp = kp + D;
+        if (FPL == 1) {
+            kw[j][0] = *reinterpret_cast<const uint16_t*>(kp);
+            vw[j][0] = *reinterpret_cast<const uint16_t*>(vp);
+        } else if (FPL == 4) {
+            const uint2 a = *reinterpret_cast<const uint2*>(kp), b = *reinterpret_cast<const uint2*>(vp);
+            kw[j][0] = a.x; kw[j][W > 1 ? 1 : 0] = a.y;
+            vw[j][0] = b.x; vw[j][W > 1 ? 1 : 0] = b.y;
+        } else {
+            const uint4 a = *reinterpret_cast<const uint4*>(kp), b = *reinterpret_cast<const uint4*>(vp);
+            const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < W; i++) { kw[j][i] = aw[i]; vw[j][i] = bw[i]; }
+        }
+    }
+    auto unpack = [&](const uint32_t* w, float* f) {
+        if (FPL == 1) {
+            f[0] = __uint_as_float(w[0] << 16);
+        } else {
+#pragma unroll
+            for (int i = 0; i < W; i++) {
+                f[2 * i] = __uint_as_float(w[i] << 16);
+                f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+            }
+        }
+    };
+    float sc[9];
+    float smax = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        float k[FPL];
+        unpack(kw[j], k);
+        float p = 0.f;
+#pragma unroll
+        for (int i = 0; i < FPL; i++) p = fmaf(q[i], k[i], p);
+        for (int o = 1; o < lph; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+        sc[j] = p * scale;
+        if (in[j]) smax = fmaxf(smax, sc[j]);
+    }
+    float denom = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        sc[j] = in[j] ? __expf(sc[j] - smax) : 0.f;
+        denom += sc[j];
+    }
+    const float inv = 1.0f / denom;
+    float acc[FPL];
+#pragma unroll
+    for (int i = 0; i < FPL; i++) acc[i] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        float v[FPL];
+        unpack(vw[j], v);
+        const float wn = sc[j] * inv;
+#pragma unroll
+        for (int i = 0; i < FPL; i++) acc[i] = fmaf(wn, v[i], acc[i]);
+    }
+    BfVec<FPL>::store(out + (size_t)r * D + lane * FPL, acc);
+}
+
 // z0 (f32 [rows, HD]) -> zc (bf16 [cells, 48]): upsample along y then x
 // (cpu.rs:211-245), state channels appended (cpu.rs:339-342), zero padding.
 __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst, int n_inst,
@@ -331,65 +434,6 @@ __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const I
     }
 }
 
-// head.conv2 (3x3, HD -> C) on f32 c1, then the step's residual. One CTA per
-// 16x16 cell tile; c1 with a one-cell halo staged channel-major in shared
-// memory (conflict-free: consecutive threads read consecutive cells).
-__global__ void __launch_bounds__(256) bf_conv2_step_kernel(Dims d, const float* __restrict__ c1,
-                                                            const float* __restrict__ w2,
-                                                            const float* __restrict__ b2, const InstDev* inst,
-                                                            int n_inst, int mode) {
-    constexpr int S = kCellTile + 2;
-    extern __shared__ float sm2[];
-    const int HD = d.HD;
-    float* tile = sm2;             // [HD][S][S]
-    float* ws = sm2 + HD * S * S;  // [C][HD][9]
-    int lo = 0, hi = n_inst - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (inst[mid].tile0 <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
-    }
-    const InstDev& I = inst[lo];
-    const int tiles_x = (I.nx + kCellTile - 1) / kCellTile;
-    const int tl = blockIdx.x - I.tile0;
-    const int y0 = (tl / tiles_x) * kCellTile, x0 = (tl % tiles_x) * kCellTile;
-    for (int i = threadIdx.x; i < d.C * HD * 9; i += blockDim.x) ws[i] = w2[i];
-    const int q8 = HD / 8;
-    for (int e = threadIdx.x; e < S * S * q8; e += blockDim.x) {
-        int q = e % q8, p = e / q8, sy = p / S, sx = p % S;
-        int y = y0 + sy - 1, x = x0 + sx - 1;
-        float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (y >= 0 && x >= 0 && y < I.ny && x < I.nx) {
-            const float4* src = reinterpret_cast<const float4*>(c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 8 * q);
-            float4 a = src[0], b = src[1];
-            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-        }
-#pragma unroll
-        for (int i = 0; i < 8; i++) tile[(8 * q + i) * S * S + p] = v[i];
-    }
-    __syncthreads();
-    const int ty = threadIdx.x / kCellTile, tx = threadIdx.x % kCellTile;
-    const int y = y0 + ty, x = x0 + tx;
-    if (y >= I.ny || x >= I.nx) return;
-    float acc[4];
-    for (int co = 0; co < d.C; co++) acc[co] = b2[co];
-    for (int ci = 0; ci < HD; ci++) {
-        const float* tp = tile + ci * S * S;
-#pragma unroll
-        for (int ky = 0; ky < 3; ky++)
-#pragma unroll
-            for (int kx = 0; kx < 3; kx++) {
-                float a = tp[(ty + ky) * S + tx + kx];  // zero outside the grid
-                for (int co = 0; co < d.C; co++) acc[co] = fmaf(a, ws[(co * HD + ci) * 9 + ky * 3 + kx], acc[co]);
-            }
-    }
-    const size_t plane = (size_t)I.nx * I.ny, cl = (size_t)y * I.nx + x;
-    for (int co = 0; co < d.C; co++) {
-        float v = acc[co];
-        if (mode == kWriteNextState) v = v + I.state[co * plane + cl];
-        I.out[co * plane + cl] = v;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // tensor-core kernels
 
@@ -403,49 +447,133 @@ __device__ __forceinline__ void store_bf16x16(bf16* p, const float* v) {
     BfVec<8>::store(p + 8, v + 8);
 }
 
-// x[row] += acc + bias over D columns, then LayerNorm of the new row into
-// `ln` (bf16). Three passes over TMEM so no row is held in registers. Every
-// lane runs the same TMEM loads (they are warp-collective); lanes whose row
-// is past the end (valid = false) neither read x nor write.
-__device__ void resid_ln_epilogue(uint32_t taddr, int D, bool valid, const float* __restrict__ bias,
-                                  float* __restrict__ xrow, const float* __restrict__ g, const float* __restrict__ b,
-                                  bf16* __restrict__ lnrow) {
-    float s = 0.f;
-    for (int c = 0; c < D; c += 16) {
+// Exact-form GELU, 0.5 x (1 + erf(x / sqrt 2)), with erf from Abramowitz &
+// Stegun 7.1.26 (|error| <= 1.5e-7 for the formula; the reciprocal and
+// exponential use the hardware approximations). Used where the result is
+// rounded to bf16 or feeds bf16 arithmetic.
+__device__ __forceinline__ float gelu_fast(float x) {
+    const float z = fabsf(x) * 0.70710678118654752440f;
+    const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+    const float poly =
+        t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
+    const float erf_abs = 1.0f - poly * __expf(-z * z);
+    const float erf_x = copysignf(erf_abs, x);
+    return 0.5f * x * (1.0f + erf_x);
+}
+
+__device__ __forceinline__ int slot_swz(int r, int D) { return D >= 128 ? (r & 31) : (r & (D / 4 - 1)); }
+
+// Stage columns [c0, c1) of this thread's TMEM lane (tile row `r`) into the
+// shared f32 tile [128][D]; float4 slot q of row r is stored at slot
+// q ^ slot_swz(r, D), which keeps both the row-per-thread writes here and the
+// row-per-warp reads below free of bank conflicts.
+__device__ __forceinline__ void stage_rows(uint32_t ta, int r, int D, int c0, int c1, float* tile) {
+    for (int c = c0; c < c1; c += 16) {
         float a[16];
-        tc::tmem_ld16(taddr + c, a);
-        if (valid) {
+        tc::tmem_ld16(ta + c, a);
 #pragma unroll
-            for (int i = 0; i < 16; i++) s += xrow[c + i] + (a[i] + bias[c + i]);
+        for (int i = 0; i < 4; i++) {
+            const int q = c / 4 + i;
+            reinterpret_cast<float4*>(tile + (size_t)r * D)[q ^ slot_swz(r, D)] =
+                make_float4(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]);
         }
     }
-    const float mean = s / (float)D;
-    float q = 0.f;
-    for (int c = 0; c < D; c += 16) {
-        float a[16];
-        tc::tmem_ld16(taddr + c, a);
-        if (valid) {
+}
+
+// One warp per tile row: x[row] += acc + bias, then LayerNorm of the new row
+// (two-pass mean and biased variance, eps 1e-5) into `ln` as bf16. Lane l
+// handles float4 slots l + 32 j, so x and ln are read and written coalesced.
+template <int SPL>  // float4 slots per lane: D / 128
+__device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
+                              float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
+                              bf16* __restrict__ ln, int warp, int nwarps) {
+    const int lane = threadIdx.x & 31;
+    float4 bb[SPL], gg[SPL], be[SPL];
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-                float v = xrow[c + i] + (a[i] + bias[c + i]);
-                q += (v - mean) * (v - mean);
+    for (int j = 0; j < SPL; j++) {
+        const int q = lane + 32 * j;
+        bb[j] = reinterpret_cast<const float4*>(bias)[q];
+        gg[j] = reinterpret_cast<const float4*>(g)[q];
+        be[j] = reinterpret_cast<const float4*>(b)[q];
+    }
+    constexpr int G = 4;  // rows in flight per warp
+    for (int r0 = warp * G; r0 < 128; r0 += nwarps * G) {
+        float4 a[G][SPL], xv[G][SPL];
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const int r = r0 + k, row = m0 + r;
+#pragma unroll
+            for (int j = 0; j < SPL; j++) {
+                const int q = lane + 32 * j;
+                a[k][j] = reinterpret_cast<const float4*>(tile + (size_t)r * D)[q ^ (r & 31)];
+                xv[k][j] = row < R ? reinterpret_cast<const float4*>(x + (size_t)row * D)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const int row = m0 + r0 + k;
+            if (row >= R) break;
+            float4 v[SPL];
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < SPL; j++) {
+                v[j] = make_float4(xv[k][j].x + (a[k][j].x + bb[j].x), xv[k][j].y + (a[k][j].y + bb[j].y),
+                                   xv[k][j].z + (a[k][j].z + bb[j].z), xv[k][j].w + (a[k][j].w + bb[j].w));
+                s += (v[j].x + v[j].y) + (v[j].z + v[j].w);
+            }
+            const float mean = warp_sum(s) / (float)D;
+            float q2 = 0.f;
+#pragma unroll
+            for (int j = 0; j < SPL; j++) {
+                const float e0 = v[j].x - mean, e1 = v[j].y - mean, e2 = v[j].z - mean, e3 = v[j].w - mean;
+                q2 += (e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3);
+            }
+            const float rstd = 1.0f / sqrtf(warp_sum(q2) / (float)D + 1e-5f);
+#pragma unroll
+            for (int j = 0; j < SPL; j++) {
+                const int q = lane + 32 * j;
+                reinterpret_cast<float4*>(x + (size_t)row * D)[q] = v[j];
+                float o[4] = {(v[j].x - mean) * rstd * gg[j].x + be[j].x, (v[j].y - mean) * rstd * gg[j].y + be[j].y,
+                              (v[j].z - mean) * rstd * gg[j].z + be[j].z, (v[j].w - mean) * rstd * gg[j].w + be[j].w};
+                BfVec<4>::store(ln + (size_t)row * D + 4 * q, o);
             }
         }
     }
-    const float rstd = 1.0f / sqrtf(q / (float)D + 1e-5f);
-    for (int c = 0; c < D; c += 16) {
-        float a[16], o[16];
-        tc::tmem_ld16(taddr + c, a);
-        if (!valid) continue;
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            float v = xrow[c + i] + (a[i] + bias[c + i]);
-            a[i] = v;
-            o[i] = (v - mean) * rstd * g[c + i] + b[c + i];
+}
+
+// D-dispatch of rows_resid_ln (D = 128 SPL 1, 256 SPL 2; D = 32 uses the
+// first 8 lanes of one slot each).
+__device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
+                                  const float* g, const float* b, bf16* ln, int warp, int nwarps) {
+    if (D == 256) rows_resid_ln<2>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps);
+    else if (D == 128) rows_resid_ln<1>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps);
+    else {
+        // narrow rows (D = 32): lanes 0..7 each own one float4 slot
+        const int lane = threadIdx.x & 31;
+        for (int r = warp; r < 128; r += nwarps) {
+            const int row = m0 + r;
+            if (row >= R) break;
+            const bool on = lane < D / 4;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (on) {
+                const float4 a = reinterpret_cast<const float4*>(tile + (size_t)r * D)[lane ^ (r & (D / 4 - 1))];
+                const float4 xv = reinterpret_cast<const float4*>(x + (size_t)row * D)[lane];
+                const float4 bb = reinterpret_cast<const float4*>(bias)[lane];
+                v = make_float4(xv.x + (a.x + bb.x), xv.y + (a.y + bb.y), xv.z + (a.z + bb.z), xv.w + (a.w + bb.w));
+            }
+            const float mean = warp_sum((v.x + v.y) + (v.z + v.w)) / (float)D;
+            float q2 = 0.f;
+            if (on) q2 = (v.x - mean) * (v.x - mean) + (v.y - mean) * (v.y - mean) + (v.z - mean) * (v.z - mean) +
+                         (v.w - mean) * (v.w - mean);
+            const float rstd = 1.0f / sqrtf(warp_sum(q2) / (float)D + 1e-5f);
+            if (on) {
+                const float4 gg = reinterpret_cast<const float4*>(g)[lane], be = reinterpret_cast<const float4*>(b)[lane];
+                reinterpret_cast<float4*>(x + (size_t)row * D)[lane] = v;
+                float o[4] = {(v.x - mean) * rstd * gg.x + be.x, (v.y - mean) * rstd * gg.y + be.y,
+                              (v.z - mean) * rstd * gg.z + be.z, (v.w - mean) * rstd * gg.w + be.w};
+                BfVec<4>::store(ln + (size_t)row * D + 4 * lane, o);
+            }
         }
-#pragma unroll
-        for (int i = 0; i < 16; i++) xrow[c + i] = a[i];
-        store_bf16x16(lnrow + c, o);
     }
 }
 
@@ -518,8 +646,12 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
         const uint32_t ta = lane_addr(tmem);
         const int n0 = nb * BN;
         if (EPI == EPI_RESID_LN) {
-            const size_t rr = row < R ? (size_t)row : 0;
-            resid_ln_epilogue(ta, BN, row < R, ep.bias, ep.x + rr * BN, ep.g, ep.b, ep.out_bf + rr * BN);
+            // every MMA and TMA write is complete: the operand tiles' shared
+            // memory now holds the f32 accumulator tile
+            float* tile = reinterpret_cast<float*>(smem);
+            stage_rows(ta, threadIdx.x, BN, 0, BN, tile);
+            __syncthreads();
+            rows_resid_ln_any(tile, BN, m0, R, ep.bias, ep.x, ep.g, ep.b, ep.out_bf, warp, 4);
         } else {
             for (int c = 0; c < BN; c += 16) {
                 float a[16];
@@ -546,25 +678,33 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
 // Fused MLP: x += gelu(LN2(x) @ W1 + b1) @ W2 + b2, then LayerNorm of the new
 // x (the next block's norm1, or the final norm) into `ln`. Per chunk of NC
 // hidden columns: S = A @ W1_chunk (TMEM), h = gelu(S + b1) written to
-// shared memory as bf16, O += h @ W2_chunk (TMEM). The hidden activations
-// never leave the SM.
-__global__ void __launch_bounds__(128) tc_mlp_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                     const bf16* __restrict__ W1, const bf16* __restrict__ W2,
-                                                     const float* __restrict__ b1, const float* __restrict__ b2,
-                                                     int D, int F, int NC, int R, float* __restrict__ x,
-                                                     const float* __restrict__ g, const float* __restrict__ b,
-                                                     bf16* __restrict__ ln, int* err) {
+// shared memory as bf16 by all 8 warps (two per TMEM lane quarter, one
+// column half each), O += h @ W2_chunk (TMEM). The hidden activations never
+// leave the SM. The residual + LayerNorm epilogue stages O through shared
+// memory and runs one warp per row.
+constexpr int kMlpThreads = 256;
+
+__global__ void __launch_bounds__(kMlpThreads) tc_mlp_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                             const bf16* __restrict__ W1, const bf16* __restrict__ W2,
+                                                             const float* __restrict__ b1,
+                                                             const float* __restrict__ b2, int D, int F, int NC, int R,
+                                                             float* __restrict__ x, const float* __restrict__ g,
+                                                             const float* __restrict__ b, bf16* __restrict__ ln,
+                                                             int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;                           // [D/8][128][8]
     uint8_t* sB1 = sA + (size_t)D * 256;          // [D/8][NC][8]
     uint8_t* sB2 = sB1 + (size_t)D * NC * 2;      // [NC/8][D][8]
     uint8_t* sH = sB2 + (size_t)D * NC * 2;       // [NC/8][128][8]
+    __shared__ float sb1[1024];
     __shared__ uint64_t bar_a, bar_w, bar_s, bar_o;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
-    const int warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quarter = warp & 3, half = warp >> 2;
     const int m0 = blockIdx.x * 128;
-    const uint32_t ncols = 512;  // O in columns [0, D), S in [256, 256 + NC)
+    const uint32_t ncols = D <= 128 ? 256 : 512;
+    const uint32_t s_col = D <= 128 ? 128 : 256;  // O in [0, D), S in [s_col, s_col + NC)
     if (threadIdx.x == 0) {
         tc::mbar_init(&bar_a, 1);
         tc::mbar_init(&bar_w, 1);
@@ -577,11 +717,12 @@ __global__ void __launch_bounds__(128) tc_mlp_kernel(const __grid_constant__ CUt
             atomicExch(err, 2);
         }
     }
+    for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    const uint32_t tO = tmem_base, tS = tmem_base + 256;
+    const uint32_t tO = tmem_base, tS = tmem_base + s_col;
     const uint32_t a0 = tc::smem_u32(sA), w1s = tc::smem_u32(sB1), w2s = tc::smem_u32(sB2), hs = tc::smem_u32(sH);
     if (threadIdx.x == 0 && !failed) {
         tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
@@ -611,13 +752,14 @@ __global__ void __launch_bounds__(128) tc_mlp_kernel(const __grid_constant__ CUt
         if (!ok) break;
         {
             // h = gelu(S + b1) -> bf16 -> shared memory in the core-matrix layout
-            const int r = threadIdx.x;
+            const int r = quarter * 32 + lane;
             const uint32_t ta = lane_addr(tS);
-            for (int c = 0; c < NC; c += 16) {
+            const int c0 = half * (NC / 2), c1 = c0 + NC / 2;
+            for (int c = c0; c < c1; c += 16) {
                 float a[16];
                 tc::tmem_ld16(ta + c, a);
 #pragma unroll
-                for (int i = 0; i < 16; i++) a[i] = gelu_erf(a[i] + b1[j * NC + c + i]);
+                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + sb1[j * NC + c + i]);
                 BfVec<8>::store(reinterpret_cast<bf16*>(sH + (size_t)(c / 8) * 2048 + r * 16), a);
                 BfVec<8>::store(reinterpret_cast<bf16*>(sH + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
             }
@@ -638,10 +780,11 @@ __global__ void __launch_bounds__(128) tc_mlp_kernel(const __grid_constant__ CUt
         tc::tc_fence_after();
     }
     if (ok) {
-        const int row = m0 + threadIdx.x;
-        const uint32_t ta = lane_addr(tO);
-        const size_t rr = row < R ? (size_t)row : 0;
-        resid_ln_epilogue(ta, D, row < R, b2, x + rr * D, g, b, ln + rr * D);
+        // every MMA is complete: reuse the operand shared memory for the f32 O tile
+        float* tile = reinterpret_cast<float*>(smem);
+        stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
+        __syncthreads();
+        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpThreads / 32);
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -762,12 +905,12 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
                 for (int i = 0; i < 16; i++) {
                     const int ch = n0 + c + i;
                     const float xn = bf2f(*reinterpret_cast<const bf16*>(centre + (size_t)(ch / 8) * kHaloPlane + (ch % 8) * 2));
-                    a[i] = xn + gelu_erf(a[i] + bias[ch]);
+                    a[i] = xn + gelu_fast(a[i] + bias[ch]);
                 }
                 store_bf16x16(static_cast<bf16*>(out) + (size_t)pos * N + n0 + c, a);
             } else {
 #pragma unroll
-                for (int i = 0; i < 16; i++) a[i] = gelu_erf(a[i] + bias[n0 + c + i]);
+                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + bias[n0 + c + i]);
                 float4* o = reinterpret_cast<float4*>(static_cast<float*>(out) + (size_t)pos * N + n0 + c);
 #pragma unroll
                 for (int i = 0; i < 4; i++) o[i] = make_float4(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]);
@@ -817,7 +960,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
         throw Error(JC_LIMIT,
                     "the BF16 path needs dim a multiple of 32 and <= 256, heads dividing 32, a cell-head width of 32, "
                     "3 channels and patch 4");
-    nc_mlp = D <= 128 ? 128 : 64;
+    nc_mlp = 64;
     bn_qkv = (3 * D) % 128 == 0 ? 128 : 3 * D;
     bn_tm = D <= 128 ? D : 64;
     if (F % nc_mlp) throw Error(JC_LIMIT, "the MLP width must be a multiple of the MLP chunk");
@@ -898,6 +1041,9 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_mlp_kernel, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
+    set_smem(bf_embed_kernel<1>, 100 * 1024);
+    set_smem(bf_embed_kernel<4>, 100 * 1024);
+    set_smem(bf_embed_kernel<8>, 100 * 1024);
 }
 
 void BF16Path::alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows, long long cells, int max_inst) const {
@@ -940,10 +1086,11 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     const unsigned gm = (unsigned)((R + 127) / 128);
     {
         KScope k("bf_embed", s);
-        const unsigned blocks = (unsigned)((R + 7) / 8);
-        if (D <= 32) bf_embed_kernel<1><<<blocks, 256, 0, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
-        else if (D <= 128) bf_embed_kernel<4><<<blocks, 256, 0, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
-        else bf_embed_kernel<8><<<blocks, 256, 0, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
+        const unsigned blocks = (unsigned)((R + kEmbedRows - 1) / kEmbedRows);
+        const size_t smem = ((size_t)d.C * d.P * d.P * D + (size_t)kEmbedRows * d.C * d.P * d.P) * sizeof(float);
+        if (D <= 32) bf_embed_kernel<1><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
+        else if (D <= 128) bf_embed_kernel<4><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
+        else bf_embed_kernel<8><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
         check_launch("bf_embed");
     }
     for (int l = 0; l < d.L; l++) {
@@ -960,16 +1107,26 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             KScope k("bf_attention", s);
             const unsigned blocks = (unsigned)((R + 7) / 8);
             const int fpl = D / 32;
-            if (fpl == 1) bf_attention_kernel<1><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            else if (fpl == 4) bf_attention_kernel<4><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            else if (fpl == 8) bf_attention_kernel<8><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            else throw Error(JC_LIMIT, "the BF16 attention supports dim 32, 128 or 256");
+            const bool r1 = d.mask_kind == 1 && d.radius == 1;
+            if (fpl == 1) {
+                if (r1) bf_attention_r1_kernel<1><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+                else bf_attention_kernel<1><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+            } else if (fpl == 4) {
+                if (r1) bf_attention_r1_kernel<4><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+                else bf_attention_kernel<4><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+            } else if (fpl == 8) {
+                if (r1) bf_attention_r1_kernel<8><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+                else bf_attention_kernel<8><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
+            } else {
+                throw Error(JC_LIMIT, "the BF16 attention supports dim 32, 128 or 256");
+            }
             check_launch("bf_attention");
         }
         {
             KScope k("tc_proj_ln", s);
             GemmEpi ep{B.bp, ln, nullptr, p.x, B.n2g, B.n2b, D};
-            tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, (size_t)D * 256 + (size_t)D * D * 2, s>>>(
+            const size_t smem = std::max((size_t)D * 256 + (size_t)D * D * 2, (size_t)128 * D * 4);
+            tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(
                 m_attn, wp[l], D, D, R, ep, p.err);
             check_launch("tc_proj_ln");
         }
@@ -978,8 +1135,8 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             const int NC = nc_mlp;
             const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
             const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
-            size_t smem = (size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256;
-            tc_mlp_kernel<<<gm, 128, smem, s>>>(m_ln, w1[l], w2[l], B.b1, B.b2, D, d.F, NC, R, p.x, ng, nbeta, ln,
+            const size_t smem = std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
+            tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1[l], w2[l], B.b1, B.b2, D, d.F, NC, R, p.x, ng, nbeta, ln,
                                                 p.err);
             check_launch("tc_mlp");
         }
@@ -1012,13 +1169,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             reinterpret_cast<const CUtensorMap*>(p.tmaps), 1, wc1, w.c1_b, kZcCh, d.HD, d.HD, p.inst, n, c1, p.err);
         check_launch("tc_conv1");
     }
-    {
-        KScope k("bf_conv2_step", s);
-        constexpr int S = kCellTile + 2;
-        size_t smem = ((size_t)d.HD * S * S + (size_t)d.C * d.HD * 9) * sizeof(float);
-        bf_conv2_step_kernel<<<p.n_tiles, kCellTile * kCellTile, smem, s>>>(d, c1, w.c2_w, w.c2_b, p.inst, n, mode);
-        check_launch("bf_conv2_step");
-    }
+    conv2_step(d, c1, w, p, mode, "bf_conv2_step", s);
 }
 
 }  // namespace jc

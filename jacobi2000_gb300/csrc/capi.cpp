@@ -42,15 +42,18 @@ struct Neu {
     double val() const { return s + c; }
 };
 
+// project.rs:9-19: per-cell terms in f32 as the reference forms them (this
+// file is compiled without multiply-add contraction), accumulated in f64 with
+// Neumaier compensation.
 void pk(const float* x, const jc_config* c, int64_t n, double* P, double* K) {
     Neu p, k;
-    const double hoff = (double)c->norm_mean[0] + (double)c->norm_depth;
+    const float hoff = c->norm_mean[0] + c->norm_depth;
     for (int64_t i = 0; i < n; i++) {
-        double h = (double)x[i] * c->norm_std[0] + hoff;
-        double u = (double)x[n + i] * c->norm_std[1] + c->norm_mean[1];
-        double v = (double)x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
-        p.add(0.5 * (double)c->g * h * h);
-        k.add(0.5 * h * (u * u + v * v));
+        float h = x[i] * c->norm_std[0] + hoff;
+        float u = x[n + i] * c->norm_std[1] + c->norm_mean[1];
+        float v = x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
+        p.add((double)(0.5f * c->g * h * h));
+        k.add((double)(0.5f * h * (u * u + v * v)));
     }
     *P = p.val();
     *K = k.val();

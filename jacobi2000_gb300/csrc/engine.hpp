@@ -50,6 +50,7 @@ struct Pack {
     int n_tiles;      // 16x16 cell tiles
     int n_ttiles;     // 8x16 token tiles
     int n_ctiles;     // 8x16 cell tiles
+    long long max_inst_cells;  // cells of the largest instance
     InstDev* inst;    // device array, sorted by row0 / cell0 / tile0
     ProjSlot* proj;   // device array parallel to inst
     void* tmaps;      // device array: 2 tensor maps per instance (BF16 path)
@@ -70,6 +71,10 @@ enum TickMode { kWriteIncrement = 0, kWriteNextState = 1 };
 // FP32 forward of every instance of `p`; writes the increment or the next
 // state to each instance's `out`.
 void forward_f32(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cudaStream_t s);
+
+// head.conv2 + the step's residual over f32 c1 [cells, HD] (both paths).
+void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack& p, int mode, const char* name,
+                cudaStream_t s);
 
 // Projection of every instance's state (mass, then energy, per the instance's
 // flags), f64 sums. init = 1 records mass0 and the energy of the state.

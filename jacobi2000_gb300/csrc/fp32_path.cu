@@ -4,11 +4,16 @@
 // reference (bias first, sequential reductions in key order for the
 // attention softmax), so results agree with the reference's f32 CPU path to
 // rounding.
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
+#include <cooperative_groups.h>
+
 #include "engine.hpp"
 #include "fp32_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace jc {
 
@@ -59,6 +64,10 @@ KernelTimer::~KernelTimer() {
         cudaEventDestroy(r.b);
     }
     for (auto e : pool) cudaEventDestroy(e);
+}
+
+static void cuda_check_attr(cudaError_t e) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
 }
 
 static void check_launch(const char* what) {
@@ -234,17 +243,18 @@ __global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, con
 }
 
 // head.conv2 (3x3, HD -> C, cpu.rs:348-349) then the step's residual
-// (cpu.rs:84-88). One CTA per 16x16 cell tile: the tile's c1 values plus a
-// one-cell halo are staged in shared memory; one thread per cell.
-__global__ void __launch_bounds__(256)
-conv2_step_kernel(Dims d, const float* __restrict__ c1, const float* __restrict__ w2, const float* __restrict__ b2,
-                  const InstDev* inst, int n_inst, int mode) {
-    extern __shared__ __align__(16) float sm[];
+// (cpu.rs:84-88), for C = 3 and HD = 32. One CTA per 16x16 cell tile: the
+// tile's c1 values plus a one-cell halo are staged channel-major in shared
+// memory (consecutive threads read consecutive cells: no bank conflicts), the
+// weights as [ci][tap] float4 (3 outputs + 0). One thread per cell.
+template <int C, int HD>
+__global__ void __launch_bounds__(256) conv2_step_kernel(const float* __restrict__ c1, const float* __restrict__ w2,
+                                                         const float* __restrict__ b2, const InstDev* inst,
+                                                         int n_inst, int mode) {
+    static_assert(C <= 4, "conv2 keeps its outputs in one float4 weight row");
     constexpr int S = kCellTile + 2;
-    const int HD = d.HD;
-    float* tile = sm;                  // [S][S][HD]
-    float* ws = sm + S * S * HD;       // [C][HD][9]
-    // instance and tile of this CTA
+    __shared__ float tile[HD][S * S];
+    __shared__ float4 ws[HD][9];
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -254,36 +264,49 @@ conv2_step_kernel(Dims d, const float* __restrict__ c1, const float* __restrict_
     const int tiles_x = (I.nx + kCellTile - 1) / kCellTile;
     const int tl = blockIdx.x - I.tile0;
     const int y0 = (tl / tiles_x) * kCellTile, x0 = (tl % tiles_x) * kCellTile;
-    for (int i = threadIdx.x; i < d.C * HD * 9; i += blockDim.x) ws[i] = w2[i];
-    const int q4 = HD / 4;
-    for (int e = threadIdx.x; e < S * S * q4; e += blockDim.x) {
-        int q = e % q4, p = e / q4, sy = p / S, sx = p % S;
-        int y = y0 + sy - 1, x = x0 + sx - 1;
+    for (int i = threadIdx.x; i < HD * 9; i += blockDim.x) {
+        const int ci = i / 9, tap = i % 9;
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int co = 0; co < C; co++) w[co] = w2[(co * HD + ci) * 9 + tap];
+        ws[ci][tap] = make_float4(w[0], w[1], w[2], w[3]);
+    }
+    constexpr int Q = HD / 4;
+    for (int e = threadIdx.x; e < S * S * Q; e += blockDim.x) {
+        const int q = e % Q, p = e / Q, sy = p / S, sx = p % S;
+        const int y = y0 + sy - 1, x = x0 + sx - 1;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (y >= 0 && x >= 0 && y < I.ny && x < I.nx)
             v = reinterpret_cast<const float4*>(c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD)[q];
-        reinterpret_cast<float4*>(tile + (size_t)p * HD)[q] = v;
+        tile[4 * q + 0][p] = v.x;
+        tile[4 * q + 1][p] = v.y;
+        tile[4 * q + 2][p] = v.z;
+        tile[4 * q + 3][p] = v.w;
     }
     __syncthreads();
     const int ty = threadIdx.x / kCellTile, tx = threadIdx.x % kCellTile;
     const int y = y0 + ty, x = x0 + tx;
     if (y >= I.ny || x >= I.nx) return;
-    float acc[4];
-    for (int co = 0; co < d.C; co++) acc[co] = b2[co];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int co = 0; co < C; co++) acc[co] = b2[co];
+#pragma unroll 4
     for (int ci = 0; ci < HD; ci++) {
 #pragma unroll
-        for (int ky = 0; ky < 3; ky++) {
-            if (y + ky - 1 < 0 || y + ky - 1 >= I.ny) continue;
+        for (int ky = 0; ky < 3; ky++)
 #pragma unroll
             for (int kx = 0; kx < 3; kx++) {
-                if (x + kx - 1 < 0 || x + kx - 1 >= I.nx) continue;
-                float a = tile[((ty + ky) * S + tx + kx) * HD + ci];
-                for (int co = 0; co < d.C; co++) acc[co] = fmaf(a, ws[(co * HD + ci) * 9 + ky * 3 + kx], acc[co]);
+                const float a = tile[ci][(ty + ky) * S + tx + kx];  // zero outside the grid
+                const float4 w = ws[ci][ky * 3 + kx];
+                acc[0] = fmaf(a, w.x, acc[0]);
+                acc[1] = fmaf(a, w.y, acc[1]);
+                acc[2] = fmaf(a, w.z, acc[2]);
+                acc[3] = fmaf(a, w.w, acc[3]);
             }
-        }
     }
     const size_t plane = (size_t)I.nx * I.ny, cl = (size_t)y * I.nx + x;
-    for (int co = 0; co < d.C; co++) {
+#pragma unroll
+    for (int co = 0; co < C; co++) {
         float v = acc[co];
         if (mode == kWriteNextState) v = v + I.state[co * plane + cl];
         I.out[co * plane + cl] = v;
@@ -309,84 +332,188 @@ __device__ double block_sum_d(double v, double* red) {
     return r;
 }
 
-// Potential and kinetic energy sums (project.rs:9-19), per-cell terms in f64
-// from the stored f32 values, Neumaier-compensated per thread.
-__device__ void energy_terms(const Dims& d, const float* s, long long n, double* P, double* K, double* red) {
-    Neu p, k;
-    p.init();
-    k.init();
-    const double hoff = (double)d.norm_mean[0] + (double)d.norm_depth;
-    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-        double h = (double)s[i] * d.norm_std[0] + hoff;
-        double u = (double)s[n + i] * d.norm_std[1] + d.norm_mean[1];
-        double v = (double)s[2 * n + i] * d.norm_std[2] + d.norm_mean[2];
-        p.add(0.5 * (double)d.g * h * h);
-        k.add(0.5 * h * (u * u + v * v));
-    }
-    *P = block_sum_d(p.val(), red);
-    *K = block_sum_d(k.val(), red);
+// Mass then energy projection (eval.rs:148-153 order; project.rs:33-54). One
+// thread-block cluster of kProjCluster CTAs per instance; each CTA keeps its
+// slice of the state in shared memory (when it fits) for the three passes:
+//   1. sum h                                   -> mass shift (f32)
+//   2. apply the shift; sum potential, kinetic -> energy scale (f32)
+//   3. apply the scale; sum potential, kinetic -> energy of the stored state
+// Per-cell terms use the reference's f32 arithmetic (project.rs:9-19,
+// unfused). Each thread sums its few cells with Kahan compensation in f32;
+// the per-thread sums are combined in f64 (a fixed-order block tree, then the
+// cluster's partials in rank order through distributed shared memory), so
+// every CTA and every run sees the same totals. f64 is used only for these
+// combinations (the FP64 rate of this GPU is a small fraction of its FP32
+// rate, so per-cell f64 arithmetic would dominate the kernel).
+constexpr int kProjCluster = 8;
+constexpr int kProjThreads = 512;
+constexpr int kProjSmemCells = 16384;  // 192 KB of state per CTA at most
+
+__device__ __forceinline__ void pk_terms(const Dims& d, float xh, float xu, float xv, float& pot, float& kin) {
+    const float h = __fadd_rn(__fmul_rn(xh, d.norm_std[0]), __fadd_rn(d.norm_mean[0], d.norm_depth));
+    const float u = __fadd_rn(__fmul_rn(xu, d.norm_std[1]), d.norm_mean[1]);
+    const float v = __fadd_rn(__fmul_rn(xv, d.norm_std[2]), d.norm_mean[2]);
+    pot = __fmul_rn(__fmul_rn(__fmul_rn(0.5f, d.g), h), h);
+    kin = __fmul_rn(__fmul_rn(0.5f, h), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
 }
 
-// Mass then energy projection (eval.rs:148-153 order; project.rs:33-54) of
-// one instance per CTA, with f64 compensated sums; the shift and scale are
-// rounded to f32 and applied with the reference's f32 update.
-__global__ void __launch_bounds__(512) projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init) {
+// Kahan-compensated f32 accumulator for a thread's cells.
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float v) {
+        const float y = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+};
+
+// Sum of the cluster's per-CTA partials, in rank order: thread r reads rank
+// r's values through distributed shared memory, thread 0 adds them in order.
+__device__ void cluster_total(cg::cluster_group& cluster, double* mine, const double* local, int nv, double* out) {
+    __shared__ double gathered[kProjCluster][4];
+    if (threadIdx.x < nv) mine[threadIdx.x] = local[threadIdx.x];
+    cluster.sync();
+    if (threadIdx.x < kProjCluster) {
+        const double* peer = cluster.map_shared_rank(mine, (int)threadIdx.x);
+        for (int v = 0; v < nv; v++) gathered[threadIdx.x][v] = peer[v];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int v = 0; v < nv; v++) {
+            double t = 0.0;
+            for (int r = 0; r < kProjCluster; r++) t += gathered[r][v];
+            out[v] = t;
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __cluster_dims__(kProjCluster, 1, 1) __launch_bounds__(kProjThreads)
+projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int cap) {
+    extern __shared__ float sst[];  // [3][cap]: this CTA's slice when it fits
     __shared__ double red[32];
-    const InstDev& I = inst[blockIdx.x];
-    ProjSlot& S = slots[blockIdx.x];
+    __shared__ double part[3][4];   // per-phase partials, read by the other CTAs of the cluster
+    __shared__ double tot[4];
+    __shared__ double local[4];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int ii = blockIdx.x / kProjCluster, rank = (int)cluster.block_rank();
+    const InstDev& I = inst[ii];
+    ProjSlot& S = slots[ii];
     float* s = I.state;
-    const unsigned flags = I.flags;
+    const unsigned flags = init ? 0u : I.flags;
     const long long n = (long long)I.nx * I.ny;
+    const long long c0 = n * rank / kProjCluster, c1 = n * (rank + 1) / kProjCluster;
+    const int m = (int)(c1 - c0);
+    const bool staged = m <= cap;
+    // this CTA's cells, in shared memory if they fit, else in place
+    float* H = staged ? sst : s + c0;
+    float* U = staged ? sst + cap : s + n + c0;
+    float* V = staged ? sst + 2 * cap : s + 2 * n + c0;
+    if (staged) {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            H[i] = s[c0 + i];
+            U[i] = s[n + c0 + i];
+            V[i] = s[2 * n + c0 + i];
+        }
+        __syncthreads();
+    }
+    const double prev = S.energy;
+    // pass 1: mass
+    double M = 0.0;
+    if (init || (flags & 1u)) {
+        Kahan a;
+        a.init();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) a.add(H[i]);
+        if (threadIdx.x == 0) local[0] = 0.0;
+        double blk = block_sum_d(a.val(), red);
+        if (threadIdx.x == 0) local[0] = blk;
+        __syncthreads();
+        cluster_total(cluster, part[0], local, 1, tot);
+        M = tot[0];
+    }
+    // pass 2: mass shift, then potential and kinetic energy
+    {
+        const float delta = (flags & 1u) ? (float)(S.mass0 - M / (double)n) : 0.0f;
+        Kahan p, k;
+        p.init();
+        k.init();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            float h = H[i];
+            if (flags & 1u) {
+                h = __fadd_rn(h, delta);
+                H[i] = h;
+            }
+            float pot, kin;
+            pk_terms(d, h, U[i], V[i], pot, kin);
+            p.add(pot);
+            k.add(kin);
+        }
+        double P = block_sum_d(p.val(), red), K = block_sum_d(k.val(), red);
+        if (threadIdx.x == 0) { local[0] = P; local[1] = K; }
+        __syncthreads();
+        cluster_total(cluster, part[1], local, 2, tot);
+    }
+    double P = tot[0], K = tot[1];
     if (init) {
-        Neu m;
-        m.init();
-        for (long long i = threadIdx.x; i < n; i += blockDim.x) m.add((double)s[i]);
-        double M = block_sum_d(m.val(), red) / (double)n;
-        double P, K;
-        energy_terms(d, s, n, &P, &K, red);
-        if (threadIdx.x == 0) {
-            S.mass0 = M;
+        if (rank == 0 && threadIdx.x == 0) {
+            S.mass0 = M / (double)n;
             S.energy = P + K;
             S.max_viol = 0.0;
             S.last_scale = 1.0;
         }
-        return;
-    }
-    const double prev = S.energy;
-    if (flags & 1u) {
-        Neu m;
-        m.init();
-        for (long long i = threadIdx.x; i < n; i += blockDim.x) m.add((double)s[i]);
-        double M = block_sum_d(m.val(), red) / (double)n;
-        float delta = (float)(S.mass0 - M);
-        for (long long i = threadIdx.x; i < n; i += blockDim.x) s[i] = __fadd_rn(s[i], delta);
-        __syncthreads();
-    }
-    double P, K;
-    if (flags & 2u) {
-        energy_terms(d, s, n, &P, &K, red);
-        double bound = prev * (double)d.energy_r_max;
-        double budget = bound - P;
-        if (!(budget > 0.0)) budget = 0.0;
-        double sc = sqrt(budget / (K > 1e-12 ? K : 1e-12));
-        sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
-        float s32 = (float)sc;
-        for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-            float u = __fadd_rn(__fmul_rn(s[n + i], d.norm_std[1]), d.norm_mean[1]);
-            float v = __fadd_rn(__fmul_rn(s[2 * n + i], d.norm_std[2]), d.norm_mean[2]);
-            s[n + i] = __fdiv_rn(__fsub_rn(__fmul_rn(u, s32), d.norm_mean[1]), d.norm_std[1]);
-            s[2 * n + i] = __fdiv_rn(__fsub_rn(__fmul_rn(v, s32), d.norm_mean[2]), d.norm_std[2]);
+    } else {
+        // pass 3: energy scale of (u, v), then the energy of the stored state
+        if (flags & 2u) {
+            const double bound = prev * (double)d.energy_r_max;
+            double budget = bound - P;
+            if (!(budget > 0.0)) budget = 0.0;
+            double sc = sqrt(budget / (K > 1e-12 ? K : 1e-12));
+            sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
+            const float s32 = (float)sc;
+            Kahan p, k;
+            p.init();
+            k.init();
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                float u = __fadd_rn(__fmul_rn(U[i], d.norm_std[1]), d.norm_mean[1]);
+                float v = __fadd_rn(__fmul_rn(V[i], d.norm_std[2]), d.norm_mean[2]);
+                u = __fdiv_rn(__fsub_rn(__fmul_rn(u, s32), d.norm_mean[1]), d.norm_std[1]);
+                v = __fdiv_rn(__fsub_rn(__fmul_rn(v, s32), d.norm_mean[2]), d.norm_std[2]);
+                U[i] = u;
+                V[i] = v;
+                float pot, kin;
+                pk_terms(d, H[i], u, v, pot, kin);
+                p.add(pot);
+                k.add(kin);
+            }
+            double P2 = block_sum_d(p.val(), red), K2 = block_sum_d(k.val(), red);
+            if (threadIdx.x == 0) { local[0] = P2; local[1] = K2; }
+            __syncthreads();
+            cluster_total(cluster, part[2], local, 2, tot);
+            P = tot[0];
+            K = tot[1];
+            if (rank == 0 && threadIdx.x == 0) S.last_scale = sc;
         }
-        if (threadIdx.x == 0) S.last_scale = sc;
+        if (rank == 0 && threadIdx.x == 0) {
+            const double E = P + K;
+            const double viol = (E - prev * (double)d.energy_r_max) / prev;
+            if (viol > S.max_viol) S.max_viol = viol;
+            S.energy = E;
+        }
+    }
+    if (staged && (flags & 3u)) {
         __syncthreads();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            if (flags & 1u) s[c0 + i] = H[i];
+            if (flags & 2u) {
+                s[n + c0 + i] = U[i];
+                s[2 * n + c0 + i] = V[i];
+            }
+        }
     }
-    energy_terms(d, s, n, &P, &K, red);
-    if (threadIdx.x == 0) {
-        double E = P + K;
-        double viol = (E - prev * (double)d.energy_r_max) / prev;
-        if (viol > S.max_viol) S.max_viol = viol;
-        S.energy = E;
-    }
+    cluster.sync();  // peers may still read this CTA's partials
 }
 
 }  // namespace f32k
@@ -440,18 +567,31 @@ void forward_f32(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cu
     }
     gemm<32>("f32_conv1", ACellConv3{p.zc, p.inst, n, (int)NC, kZcStride}, w.c1_w, w.c1_b, (int)NC, d.HD,
              9 * kZcStride, EGelu{p.c1, d.HD}, s);
-    {
-        KScope k("f32_conv2_step", s);
-        constexpr int S = kCellTile + 2;
-        size_t smem = ((size_t)S * S * d.HD + (size_t)d.C * d.HD * 9) * sizeof(float);
-        conv2_step_kernel<<<p.n_tiles, kCellTile * kCellTile, smem, s>>>(d, p.c1, w.c2_w, w.c2_b, p.inst, n, mode);
-        check_launch("conv2_step");
-    }
+    conv2_step(d, p.c1, w, p, mode, "f32_conv2_step", s);
+}
+
+void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack& p, int mode, const char* name,
+                cudaStream_t s) {
+    KScope k(name, s);
+    if (d.C != 3 || d.HD != 32) throw std::runtime_error("conv2 is built for 3 channels and a cell-head width of 32");
+    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, kCellTile * kCellTile, 0, s>>>(c1, w.c2_w, w.c2_b, p.inst, p.n_inst,
+                                                                              mode);
+    check_launch(name);
 }
 
 void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
     KScope k("projection", s);
-    f32k::projection_kernel<<<p.n_inst, 512, 0, s>>>(d, p.inst, p.proj, init);
+    static bool attr = false;
+    if (!attr) {
+        cuda_check_attr(cudaFuncSetAttribute(f32k::projection_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             3 * f32k::kProjSmemCells * 4));
+        attr = true;
+    }
+    // shared memory for the largest slice of this launch, up to the cap
+    const long long slice = (p.max_inst_cells + f32k::kProjCluster - 1) / f32k::kProjCluster;
+    const int cap = (int)std::min<long long>(std::max<long long>(slice, 1), f32k::kProjSmemCells);
+    f32k::projection_kernel<<<p.n_inst * f32k::kProjCluster, f32k::kProjThreads, (size_t)3 * cap * 4, s>>>(
+        d, p.inst, p.proj, init, cap);
     check_launch("projection");
 }
 

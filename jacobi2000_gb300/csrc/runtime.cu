@@ -443,6 +443,7 @@ Model::Model(const uint8_t* st, size_t st_len, const char* config_json, int prec
     ws_.alloc(arena, dims, tx * ty, cells + 0, 1, w.bf16.get());
     pack_ = ws_.view(dims, 0, 1, 0, tx * ty, 0, cells, cell_tiles(cfg.nx, cfg.ny), conv_tiles(tx, ty),
                      conv_tiles(cfg.nx, cfg.ny));
+    pack_.max_inst_cells = cells;
     inst_.row0 = 0;
     inst_.tx = tx;
     inst_.ty = ty;
@@ -725,6 +726,7 @@ Batch::Plan Batch::plan(const jc_instance* in, int n) const {
         G.row_base = row_base;
         G.cell_base = cell_base;
         G.cell_base_i = 0;
+        G.max_cells = 0;
         int rows = 0, tiles = 0, ttiles = 0, ctiles = 0;
         long long cells = 0;
         for (int i : idx) {
@@ -759,6 +761,7 @@ Batch::Plan Batch::plan(const jc_instance* in, int n) const {
             G.tiles.push_back(tiles);
             G.ttiles.push_back(ttiles);
             G.ctiles.push_back(ctiles);
+            G.max_cells = std::max(G.max_cells, (long long)d.nx * d.ny);
             p.max_ticks = std::max(p.max_ticks, in[i].ticks);
         }
         inst_base += G.n;
@@ -778,6 +781,7 @@ void Batch::enqueue(const Plan& p, cudaStream_t s) const {
         if (G.n == 0) continue;
         Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
                           G.tiles.back(), G.ttiles.back(), G.ctiles.back());
+        v.max_inst_cells = G.max_cells;
         projection(dims_, v, 1, s);
     }
     for (int t = 1; t <= p.max_ticks; t++) {
@@ -787,6 +791,7 @@ void Batch::enqueue(const Plan& p, cudaStream_t s) const {
             if (na == 0) continue;
             Pack v = ws_.view(dims_, G.inst_base, na, G.row_base, G.rows[na - 1], G.cell_base, G.cells[na - 1],
                               G.tiles[na - 1], G.ttiles[na - 1], G.ctiles[na - 1]);
+            v.max_inst_cells = G.max_cells;
             models_[G.model]->forward_pack(v, kWriteNextState, s);
             projection(dims_, v, 0, s);
         }

@@ -158,7 +158,7 @@ class Batch {
         std::vector<InstDev> inst;  // packed descriptors
         struct Group {
             int model, inst_base, n, row_base, cell_base_i;
-            long long cell_base;
+            long long cell_base, max_cells;
             std::vector<int> ticks;     // per packed instance, descending
             std::vector<int> rows, tiles, ttiles, ctiles;
             std::vector<long long> cells;  // prefix ends

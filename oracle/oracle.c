@@ -134,9 +134,9 @@ void orc_project_energy_f32(float* x, float prev_energy, const orc_config* c, in
 }
 
 /* ---- projections with f64 compensated (Neumaier) sums ----
- * The same formulas; every per-cell term is formed in double from the stored
- * f32 values, summed with Neumaier compensation; the resulting shift and
- * scale are rounded to f32 and applied with the reference's f32 update. */
+ * The same formulas; every per-cell term is formed in f32 as the reference
+ * forms it and summed in f64 with Neumaier compensation; the resulting shift
+ * and scale are rounded to f32 and applied with the reference's f32 update. */
 
 typedef struct { double s, c; } nsum;
 static void nadd(nsum* a, double v) {
@@ -148,15 +148,16 @@ static void nadd(nsum* a, double v) {
 static double nval(const nsum* a) { return a->s + a->c; }
 
 static void pk_sum64(const float* x, const orc_config* c, int n, double* p, double* k) {
+    /* per-cell terms exactly as project.rs:9-19 computes them (f32); only the
+     * accumulation is f64 */
     nsum ps = {0, 0}, ks = {0, 0};
-    const double h_off = (double)c->norm_mean[0] + (double)c->norm_depth;
-    const double g = c->g;
+    const float h_off = c->norm_mean[0] + c->norm_depth;
     for (int i = 0; i < n; i++) {
-        double h = (double)x[i] * c->norm_std[0] + h_off;
-        double u = (double)x[n + i] * c->norm_std[1] + c->norm_mean[1];
-        double v = (double)x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
-        nadd(&ps, 0.5 * g * h * h);
-        nadd(&ks, 0.5 * h * (u * u + v * v));
+        float h = x[i] * c->norm_std[0] + h_off;
+        float u = x[n + i] * c->norm_std[1] + c->norm_mean[1];
+        float v = x[2 * n + i] * c->norm_std[2] + c->norm_mean[2];
+        nadd(&ps, (double)(0.5f * c->g * h * h));
+        nadd(&ks, (double)(0.5f * h * (u * u + v * v)));
     }
     *p = nval(&ps);
     *k = nval(&ks);
