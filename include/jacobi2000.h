@@ -145,6 +145,74 @@ void jc_batch_destroy(jc_batch* b);
 jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
                            int32_t device_pointers, void* stream);
 
+/* ---- Serving ----
+ * A request loop with continuous batching: requests of different grid sizes
+ * and tasks that arrive while others run are admitted at the next tick as the
+ * workspace and the device memory budget allow, and share the same launches;
+ * their states stay on the device until they finish. Tasks:
+ *   FORWARD:     ticks steps of the forward model from x = X_0, projected
+ *                (the eval.rs:144-157 loop);
+ *   REWIND:      ticks steps of the reverse model from x = X_H, projected
+ *                (the web demo's rewind, crates/web/src/lib.rs:383-409);
+ *   RECONSTRUCT: x = values [ticks+1, 3, ny, nx], known = mask [ticks+1, ny, nx]
+ *                (1 = known cell, all channels); Jacobi sweeps
+ *                X_t <- known ? value : mean(step_F(X_{t-1}), step_R(X_{t+1}))
+ *                from X = 0 at unknown cells, until the largest change is
+ *                below tol or max_sweeps ran; no projection. No counterpart
+ *                in the reference. The result is the volume [ticks+1, 3, ny, nx]. */
+typedef struct jc_server jc_server;
+
+enum { JC_TASK_FORWARD = 0, JC_TASK_REWIND = 1, JC_TASK_RECONSTRUCT = 2 };
+
+typedef struct {
+    int32_t task;         /* JC_TASK_* */
+    int32_t grid;         /* index into the server's model lists */
+    int32_t ticks;        /* horizon H >= 1 */
+    uint32_t flags;       /* JC_PROJECT_* (forward and rewind) */
+    const float* x;       /* see above; copied by jc_server_submit */
+    const uint8_t* known; /* reconstruct only; copied */
+    const float* meta;    /* [meta_dim]; copied */
+    int32_t max_sweeps;   /* reconstruct */
+    float tol;            /* reconstruct: stop when max |change| < tol */
+} jc_request;
+
+typedef struct {
+    double latency_s;     /* submit to result */
+    double queue_s;       /* submit to admission */
+    int32_t sweeps;       /* reconstruct sweeps run */
+    float residual;       /* reconstruct: last max |change| */
+    double energy;        /* forward / rewind: final energy */
+    double max_violation; /* forward / rewind: max relative energy violation */
+    int64_t out_len;      /* floats written to `out` */
+} jc_result;
+
+typedef struct {
+    int64_t completed;
+    double cell_ticks;    /* sum of nx * ny * ticks of completed requests */
+    double busy_s;        /* time the loop spent in iterations */
+    double span_s;        /* first submit to last completion */
+    int32_t iterations, active, pending;
+} jc_server_stats;
+
+/* forward_models[i] and reverse_models[i] (reverse may be null: forward only)
+ * hold grid i; every model of one direction shares all tensors but `pos`.
+ * max_active_cells bounds the cells stepped per tick (the workspace is
+ * allocated for it here); hbm_fraction caps the device memory in use
+ * (requests wait in the queue while admitting them would exceed it). */
+jc_status jc_server_create(jc_model* const* forward_models, jc_model* const* reverse_models,
+                           int32_t n_grids, int64_t max_active_cells, double hbm_fraction,
+                           jc_server** out);
+/* Stops the loop after the current tick; pending and active requests are dropped. */
+void jc_server_destroy(jc_server* s);
+/* Copies the request's inputs and queues it; returns at once with its id. */
+jc_status jc_server_submit(jc_server* s, const jc_request* r, uint64_t* id);
+/* Blocks until request `id` is done (timeout_s < 0: no limit), writes its
+ * result to out (out_len floats available) and its statistics to info
+ * (either may be null), and forgets the request. */
+jc_status jc_server_wait(jc_server* s, uint64_t id, float* out, size_t out_len, jc_result* info,
+                         double timeout_s);
+jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out);
+
 /* Instrumentation, with no counterpart in the reference: runs the instances
  * once, outside any graph, with CUDA events around every kernel launch, and
  * writes one "name,launches,total_ms" line per kernel into `report`

@@ -153,6 +153,36 @@ jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
     return guard([&] { b->b->rollout(instances, n, device_pointers != 0, (cudaStream_t)stream); });
 }
 
+jc_status jc_server_create(jc_model* const* forward_models, jc_model* const* reverse_models, int32_t n_grids,
+                           int64_t max_active_cells, double hbm_fraction, jc_server** out) {
+    if (!out) return fail(JC_BAD_ARGUMENT, "out is null");
+    *out = nullptr;
+    return guard([&] { jc::server_create(forward_models, reverse_models, n_grids, max_active_cells, hbm_fraction, out); });
+}
+
+void jc_server_destroy(jc_server* s) {
+    if (!s) return;
+    try {
+        jc::server_destroy(s);
+    } catch (...) {
+    }
+}
+
+jc_status jc_server_submit(jc_server* s, const jc_request* r, uint64_t* id) {
+    if (!s || !r || !id) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] { *id = jc::server_submit(s, r); });
+}
+
+jc_status jc_server_wait(jc_server* s, uint64_t id, float* out, size_t out_len, jc_result* info, double timeout_s) {
+    if (!s) return fail(JC_BAD_ARGUMENT, "server is null");
+    return guard([&] { jc::server_wait(s, id, out, out_len, info, timeout_s); });
+}
+
+jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out) {
+    if (!s || !out) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] { jc::server_stats(s, out); });
+}
+
 jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n, int32_t device_pointers,
                            char* report, size_t cap) {
     if (!b || !report || cap == 0) return fail(JC_BAD_ARGUMENT, "null argument");

@@ -7,6 +7,14 @@
 
 namespace jc {
 
+// Per-instance projection scalars, f64 (one slot per instance).
+struct ProjSlot {
+    double mass0;       // target box mean of channel 0
+    double energy;      // energy of the current (projected) state
+    double max_viol;    // max relative energy violation so far
+    double last_scale;  // last energy-projection scale
+};
+
 // One grid instance inside a packed launch. Token-level buffers of all
 // instances are concatenated row-wise (instance i owns rows
 // [row0, row0 + tx*ty)); cell-level channel-last buffers likewise own cells
@@ -23,22 +31,15 @@ struct InstDev {
     float* out;       // where the tick writes (next state or increment)
     const float* pos; // [tx*ty, dim]
     const float* meta;// [meta_dim]
-    unsigned flags;   // projection flags of this instance (1 mass, 2 energy)
+    unsigned flags;   // projection flags: 1 mass, 2 energy, 4 no projection or energy record
     int tile0;        // first 16x16 cell tile of this instance in the launch
     int tt0;          // first 8x16 token tile (tensor-core token conv)
     int ct0;          // first 8x16 cell tile (tensor-core cell conv)
+    ProjSlot* slot;   // this instance's projection scalars (device); null = the pack's slot array
 };
 
 constexpr int kCellTile = 16;  // side of the cell tiles of the cell-level kernels
 constexpr int kConvTX = 8, kConvTY = 16;  // tensor-core conv tiles: 8 wide, 16 high (M = 128)
-
-// Per-instance projection scalars, f64 (one slot per instance).
-struct ProjSlot {
-    double mass0;       // target box mean of channel 0
-    double energy;      // energy of the current (projected) state
-    double max_viol;    // max relative energy violation so far
-    double last_scale;  // last energy-projection scale
-};
 
 #ifdef __CUDACC__
 __device__ __forceinline__ float warp_sum(float v) {

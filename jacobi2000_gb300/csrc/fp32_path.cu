@@ -401,7 +401,8 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
     cg::cluster_group cluster = cg::this_cluster();
     const int ii = blockIdx.x / kProjCluster, rank = (int)cluster.block_rank();
     const InstDev& I = inst[ii];
-    ProjSlot& S = slots[ii];
+    if (I.flags & 4u) return;  // no projection and no energy record for this instance
+    ProjSlot& S = I.slot ? *I.slot : slots[ii];
     float* s = I.state;
     const unsigned flags = init ? 0u : I.flags;
     const long long n = (long long)I.nx * I.ny;

@@ -173,6 +173,14 @@ class Batch {
     std::map<std::vector<long long>, cudaGraphExec_t> graphs_;
 };
 
+// Serving loop (server.cu).
+jc_status server_create(jc_model* const* fwd, jc_model* const* rev, int32_t n, int64_t max_cells, double frac,
+                        jc_server** out);
+void server_destroy(jc_server* s);
+uint64_t server_submit(jc_server* s, const jc_request* r);
+void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* info, double timeout);
+void server_stats(jc_server* s, jc_server_stats* st);
+
 // The FP32 forward of m's own grid with every buffer in the library's fixed
 // no-alloc scratch array (noalloc.cu); allocates nothing.
 void forward_noalloc(const Model& m, const float* d_state, const float* d_meta, float* d_inc, cudaStream_t s);

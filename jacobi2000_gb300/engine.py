@@ -293,3 +293,108 @@ class Batch:
             name, n, ms = line.split(",")
             out[name] = (int(n), float(ms))
         return out
+
+
+TASK_FORWARD, TASK_REWIND, TASK_RECONSTRUCT = 0, 1, 2
+
+
+class JcRequest(C.Structure):
+    _fields_ = [("task", C.c_int32), ("grid", C.c_int32), ("ticks", C.c_int32), ("flags", C.c_uint32),
+                ("x", C.c_void_p), ("known", C.c_void_p), ("meta", C.c_void_p), ("max_sweeps", C.c_int32),
+                ("tol", C.c_float)]
+
+
+class JcResult(C.Structure):
+    _fields_ = [("latency_s", C.c_double), ("queue_s", C.c_double), ("sweeps", C.c_int32), ("residual", C.c_float),
+                ("energy", C.c_double), ("max_violation", C.c_double), ("out_len", C.c_int64)]
+
+
+class JcServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("cell_ticks", C.c_double), ("busy_s", C.c_double), ("span_s", C.c_double),
+                ("iterations", C.c_int32), ("active", C.c_int32), ("pending", C.c_int32)]
+
+
+EXPORTED += ["jc_server_create", "jc_server_destroy", "jc_server_submit", "jc_server_wait", "jc_server_get_stats"]
+
+
+def _declare_server(L):
+    if getattr(L, "_server_declared", False):
+        return
+    vp = C.c_void_p
+    L.jc_server_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int32, C.c_int64, C.c_double, C.POINTER(vp)]
+    L.jc_server_create.restype = C.c_int
+    L.jc_server_destroy.argtypes = [vp]
+    L.jc_server_destroy.restype = None
+    L.jc_server_submit.argtypes = [vp, C.POINTER(JcRequest), C.POINTER(C.c_uint64)]
+    L.jc_server_submit.restype = C.c_int
+    L.jc_server_wait.argtypes = [vp, C.c_uint64, vp, C.c_size_t, C.POINTER(JcResult), C.c_double]
+    L.jc_server_wait.restype = C.c_int
+    L.jc_server_get_stats.argtypes = [vp, C.POINTER(JcServerStats)]
+    L.jc_server_get_stats.restype = C.c_int
+    L._server_declared = True
+
+
+class Server:
+    """Continuous-batching request loop (jc_server_*). ``forward_models[i]``
+    and ``reverse_models[i]`` hold grid i."""
+
+    def __init__(self, forward_models, reverse_models=None, max_active_cells: int = 1 << 22,
+                 hbm_fraction: float = 0.8):
+        L = load_library()
+        _declare_server(L)
+        self._L = L
+        self.forward_models = list(forward_models)
+        self.reverse_models = list(reverse_models) if reverse_models else None
+        n = len(self.forward_models)
+        fa = (C.c_void_p * n)(*[m._h.value for m in self.forward_models])
+        ra = (C.c_void_p * n)(*[m._h.value for m in self.reverse_models]) if self.reverse_models else None
+        h = C.c_void_p()
+        _check(L.jc_server_create(fa, ra, n, int(max_active_cells), float(hbm_fraction), C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.jc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _submit(self, req: JcRequest) -> int:
+        i = C.c_uint64()
+        _check(self._L.jc_server_submit(self._h, C.byref(req), C.byref(i)))
+        return int(i.value)
+
+    def submit(self, task: int, grid: int, x, meta, ticks: int, flags: int = PROJECT_MASS | PROJECT_ENERGY,
+               known=None, max_sweeps: int = 4, tol: float = 1e-3) -> int:
+        xa = np.ascontiguousarray(x, dtype=np.float32)
+        ma = np.ascontiguousarray(meta, dtype=np.float32)
+        ka = np.ascontiguousarray(known, dtype=np.uint8) if known is not None else None
+        req = JcRequest(int(task), int(grid), int(ticks), int(flags), xa.ctypes.data,
+                        ka.ctypes.data if ka is not None else None, ma.ctypes.data, int(max_sweeps), float(tol))
+        return self._submit(req)  # inputs are copied by the call
+
+    def out_shape(self, task: int, grid: int, ticks: int):
+        c = self.forward_models[grid].config
+        return ((ticks + 1, 3, c.ny, c.nx) if task == TASK_RECONSTRUCT else (3, c.ny, c.nx))
+
+    def wait(self, rid: int, task: int, grid: int, ticks: int, timeout: float = -1.0):
+        out = np.empty(self.out_shape(task, grid, ticks), dtype=np.float32)
+        info = JcResult()
+        _check(self._L.jc_server_wait(self._h, int(rid), out.ctypes.data, out.size, C.byref(info), float(timeout)))
+        return out, {f: getattr(info, f) for f, _ in JcResult._fields_}
+
+    def stats(self) -> dict:
+        st = JcServerStats()
+        _check(self._L.jc_server_get_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in JcServerStats._fields_}

@@ -1,0 +1,171 @@
+"""The serving loop: continuous batching of forward, rewind and reconstruct
+requests of several grid sizes. Results must not depend on what else runs in
+the same launches, and must match the single-request paths and the oracle."""
+
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from helpers import field_errors
+from jacobi2000_gb300 import engine
+from jacobi2000_gb300.checkpoint import parse_config, synthetic_family, write_safetensors_bytes, meta_of
+from jacobi2000_gb300.ic import random_drops
+from oracle.oracle import OracleModel
+
+pytestmark = pytest.mark.gpu
+
+SIDES = [32, 48, 64]
+ME = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+
+
+def _family(seed, precision):
+    fam = synthetic_family(128, 4, seed, SIDES)
+    models, oracles, cfgs = [], [], []
+    for s in SIDES:
+        t, cj = fam[(s, s)]
+        models.append(engine.Model.from_bytes(write_safetensors_bytes(t), cj, precision))
+        cfg = parse_config(cj, t)
+        oracles.append(OracleModel(cfg, t))
+        cfgs.append(cfg)
+    return models, oracles, cfgs
+
+
+@pytest.fixture(scope="module", params=[engine.FP32, engine.BF16], ids=["fp32", "bf16"])
+def families(request):
+    fwd = _family(0, request.param)
+    rev = _family(1, request.param)  # the reverse checkpoints: a second seeded family
+    yield fwd, rev
+    for m in fwd[0] + rev[0]:
+        m.close()
+
+
+def test_mixed_requests_match_single_runs(families):
+    (fm, _, cfgs), (rm, _, _) = families
+    rng = np.random.default_rng(7)
+    reqs = []
+    for k in range(12):
+        task = engine.TASK_FORWARD if k % 2 == 0 else engine.TASK_REWIND
+        g = int(rng.integers(0, len(SIDES)))
+        ticks = int(rng.integers(2, 9))
+        x = random_drops(cfgs[g], seed=200 + k)
+        reqs.append((task, g, ticks, x, meta_of(cfgs[g])))
+    with engine.Server(fm, rm, max_active_cells=6 * 64 * 64) as srv:
+        ids = []
+        for k, (task, g, ticks, x, meta) in enumerate(reqs):
+            ids.append(srv.submit(task, g, x, meta, ticks, ME))
+            if k % 3 == 2:
+                time.sleep(0.002)  # later requests arrive while earlier ones run
+        outs = [srv.wait(i, task, g, ticks, timeout=60) for i, (task, g, ticks, _, _) in zip(ids, reqs)]
+        st = srv.stats()
+    assert st["completed"] == len(reqs)
+    for (task, g, ticks, x, meta), (out, info) in zip(reqs, outs):
+        model = fm[g] if task == engine.TASK_FORWARD else rm[g]
+        alone, energies = model.rollout(x, meta, ticks, ME)
+        assert np.array_equal(out, alone), (task, g, ticks)
+        assert info["energy"] == energies[-1]
+        assert info["latency_s"] >= info["queue_s"] >= 0
+
+
+def _reconstruct_oracle(fo, ro, vals, known, meta, H, sweeps):
+    """The reconstruct rule restated with the f32 oracle's steps."""
+    X = np.where(known[:, None], vals, 0.0).astype(np.float32)
+    for _ in range(sweeps):
+        F = [fo.step(X[t - 1], meta) for t in range(1, H + 1)]
+        R = [ro.step(X[t + 1], meta) for t in range(0, H)]
+        new = np.empty_like(X)
+        for t in range(H + 1):
+            if t == 0:
+                v = R[0]
+            elif t == H:
+                v = F[H - 1]
+            else:
+                v = np.float32(0.5) * (F[t - 1] + R[t])
+            new[t] = np.where(known[t][None], vals[t], v)
+        X = new
+    return X
+
+
+def test_reconstruct_matches_oracle(families):
+    (fm, fo, cfgs), (rm, ro, _) = families
+    g, H, sweeps = 0, 3, 3
+    cfg = cfgs[g]
+    rng = np.random.default_rng(3)
+    truth = np.stack([random_drops(cfg, seed=t) for t in range(H + 1)])
+    known = rng.random((H + 1, cfg.ny, cfg.nx)) < 0.02
+    known[0] = True  # a fully known first slice plus sparse readings
+    vals = np.where(known[:, None], truth, 0).astype(np.float32)
+    meta = meta_of(cfg)
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        rid = srv.submit(engine.TASK_RECONSTRUCT, g, vals, meta, H, known=known, max_sweeps=sweeps, tol=0.0)
+        out, info = srv.wait(rid, engine.TASK_RECONSTRUCT, g, H, timeout=60)
+    assert info["sweeps"] == sweeps
+    want = _reconstruct_oracle(fo[g], ro[g], vals, known, meta, H, sweeps)
+    tol = 1e-4 if fm[g].precision == engine.FP32 else 2e-2
+    for t in range(H + 1):
+        assert max(field_errors(out[t], want[t])) <= tol, t
+    assert np.array_equal(out[0], vals[0])  # the fully known first slice is kept
+
+
+def test_reconstruct_in_the_mix_equals_alone(families):
+    (fm, _, cfgs), (rm, _, _) = families
+    g, H = 1, 2
+    cfg = cfgs[g]
+    rng = np.random.default_rng(5)
+    known = rng.random((H + 1, cfg.ny, cfg.nx)) < 0.05
+    vals = np.stack([random_drops(cfg, seed=40 + t) for t in range(H + 1)]).astype(np.float32)
+    meta = meta_of(cfg)
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        rid = srv.submit(engine.TASK_RECONSTRUCT, g, vals, meta, H, known=known, max_sweeps=2, tol=0.0)
+        alone, _ = srv.wait(rid, engine.TASK_RECONSTRUCT, g, H, timeout=60)
+        others = [srv.submit(engine.TASK_FORWARD, k % 3, random_drops(cfgs[k % 3], seed=k), meta_of(cfgs[k % 3]), 5)
+                  for k in range(5)]
+        rid = srv.submit(engine.TASK_RECONSTRUCT, g, vals, meta, H, known=known, max_sweeps=2, tol=0.0)
+        mixed, _ = srv.wait(rid, engine.TASK_RECONSTRUCT, g, H, timeout=60)
+        for i, k in zip(others, range(5)):
+            srv.wait(i, engine.TASK_FORWARD, k % 3, 5, timeout=60)
+    assert np.array_equal(alone, mixed)
+
+
+def test_admission_limits(families):
+    (fm, _, cfgs), (rm, _, _) = families
+    cfg = cfgs[2]
+    with engine.Server(fm, rm, max_active_cells=64 * 64) as srv:
+        # one request per tick fits; a reconstruct of 2 x 4 instances does not
+        with pytest.raises(engine.JcError) as e:
+            srv.submit(engine.TASK_RECONSTRUCT, 2, np.zeros((5, 3, 64, 64), np.float32), meta_of(cfg), 4,
+                       known=np.zeros((5, 64, 64), np.uint8))
+        assert e.value.name == "OVER_BUDGET"
+        # several requests queue behind the one that runs and all complete
+        ids = [srv.submit(engine.TASK_FORWARD, 2, random_drops(cfg, seed=k), meta_of(cfg), 3) for k in range(4)]
+        for i in ids:
+            out, info = srv.wait(i, engine.TASK_FORWARD, 2, 3, timeout=60)
+            assert np.all(np.isfinite(out))
+        with pytest.raises(engine.JcError) as e:
+            srv.wait(12345, engine.TASK_FORWARD, 2, 3, timeout=1)
+        assert e.value.name == "NOT_FOUND"
+
+
+def test_submissions_from_many_threads(families):
+    (fm, _, cfgs), (rm, _, _) = families
+    results = {}
+
+    def client(k):
+        g = k % 3
+        x = random_drops(cfgs[g], seed=500 + k)
+        with lock:
+            pass
+        rid = srv.submit(engine.TASK_FORWARD, g, x, meta_of(cfgs[g]), 4)
+        results[k] = (g, x, srv.wait(rid, engine.TASK_FORWARD, g, 4, timeout=60)[0])
+
+    lock = threading.Lock()
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        th = [threading.Thread(target=client, args=(k,)) for k in range(8)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    for k, (g, x, out) in results.items():
+        alone, _ = fm[g].rollout(x, meta_of(cfgs[g]), 4, ME)
+        assert np.array_equal(out, alone)
