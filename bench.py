@@ -55,6 +55,10 @@ def parse_args():
     ap.add_argument("--dim", type=int, default=128)
     ap.add_argument("--layers", type=int, default=4)
     ap.add_argument("--cpu-sample-ticks", type=int, default=1)
+    ap.add_argument("--served-rates", default="100,400,1600",
+                    help="request arrival rates (req/s) of the served-form run; empty to skip")
+    ap.add_argument("--served-requests", type=int, default=240)
+    ap.add_argument("--served-fp32-requests", type=int, default=24)
     return ap.parse_args()
 
 
@@ -163,6 +167,123 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
     if name in byte:
         return "byte", byte[name]
     return None, None
+
+
+SERVED_SIDES = [32, 64, 96, 128, 160, 192, 224, 256]
+
+
+def served_requests(rng, n, rate, cfgs, volumes, masks):
+    """Poisson arrivals at `rate`; grid side log-uniform in [32, 256] rounded
+    to a multiple of 32; horizon U[10, 50]; tasks 1/3 forward (initial state
+    known), 1/3 rewind (final state known), 1/3 reconstruct (2% of the
+    space-time cells known). Returns (arrival_s, task, grid, ticks, x, known)."""
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.ic import random_drops
+
+    out, t = [], 0.0
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        side = float(np.exp(rng.uniform(np.log(32), np.log(256))))
+        g = int(np.argmin([abs(side - s) for s in SERVED_SIDES]))
+        ticks = int(rng.integers(10, 51))
+        task = int(rng.integers(0, 3))
+        if task == engine.TASK_RECONSTRUCT:
+            x, known = volumes[g][: ticks + 1], masks[g][: ticks + 1]
+        else:
+            x, known = random_drops(cfgs[g], seed=int(rng.integers(1 << 30))), None
+        out.append((t, task, g, ticks, x, known))
+    return out
+
+
+def run_served(srv, reqs, metas, sweeps, concurrent=True):
+    """Submits at the arrival times (concurrent) or one request at a time
+    after the previous result (sequential). Returns throughput and latency
+    percentiles, latency measured from the scheduled arrival."""
+    import threading
+
+    from jacobi2000_gb300 import engine
+
+    lat = [None] * len(reqs)
+    cell_ticks = sum(SERVED_SIDES[g] ** 2 * ticks for _, _, g, ticks, _, _ in reqs)
+    t0 = time.perf_counter()
+    ids = [None] * len(reqs)
+
+    def collect():
+        for k, (arr, task, g, ticks, _, _) in enumerate(reqs):
+            while ids[k] is None:
+                time.sleep(0.0002)
+            srv.wait(ids[k], task, g, ticks, timeout=600)
+            lat[k] = time.perf_counter() - (t0 + arr)
+
+    if concurrent:
+        th = threading.Thread(target=collect)
+        th.start()
+        for k, (arr, task, g, ticks, x, known) in enumerate(reqs):
+            delay = t0 + arr - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids[k] = srv.submit(task, g, x, metas[g], ticks, known=known, max_sweeps=sweeps, tol=0.0)
+        th.join()
+    else:
+        for k, (arr, task, g, ticks, x, known) in enumerate(reqs):
+            delay = t0 + arr - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            rid = srv.submit(task, g, x, metas[g], ticks, known=known, max_sweeps=sweeps, tol=0.0)
+            srv.wait(rid, task, g, ticks, timeout=600)
+            lat[k] = time.perf_counter() - (t0 + arr)
+    span = time.perf_counter() - t0
+    lat_ms = np.array(lat) * 1e3
+    return {"requests": len(reqs), "cell_ticks_per_s": cell_ticks / span, "span_s": span,
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99))}
+
+
+def served_bench(args):
+    """Config: Poisson arrivals, three task types, sides 32-256, BF16 served
+    form with continuous batching vs the FP32 one-request-at-a-time path."""
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.checkpoint import parse_config, synthetic_family, write_safetensors_bytes, meta_of
+
+    rates = [float(r) for r in args.served_rates.split(",") if r.strip()]
+    if not rates:
+        return None
+    fam_f = synthetic_family(args.dim, args.layers, 0, SERVED_SIDES)
+    fam_r = synthetic_family(args.dim, args.layers, 1, SERVED_SIDES)
+    cfgs = [parse_config(fam_f[(s, s)][1], fam_f[(s, s)][0]) for s in SERVED_SIDES]
+    metas = [meta_of(c) for c in cfgs]
+    rng = np.random.default_rng(1234)
+    volumes, masks = [], []
+    for s in SERVED_SIDES:
+        volumes.append((0.3 * rng.standard_normal((51, 3, s, s))).astype(np.float32))
+        masks.append((rng.random((51, s, s)) < 0.02).astype(np.uint8))
+    sweeps = 4
+    out = {"task_mix": "1/3 forward, 1/3 rewind, 1/3 reconstruct (2% known, 4 Jacobi sweeps)",
+           "sides": "log-uniform 32-256, rounded to a multiple of 32", "horizon": "U[10,50] ticks",
+           "admission": "0.8 x HBM, 8M cells per tick", "bf16": []}
+    for prec, key in ((engine.BF16, "bf16"), (engine.FP32, "fp32_one_at_a_time")):
+        fm = [engine.Model.from_bytes(write_safetensors_bytes(fam_f[(s, s)][0]), fam_f[(s, s)][1], prec)
+              for s in SERVED_SIDES]
+        rm = [engine.Model.from_bytes(write_safetensors_bytes(fam_r[(s, s)][0]), fam_r[(s, s)][1], prec)
+              for s in SERVED_SIDES]
+        with engine.Server(fm, rm, max_active_cells=8 << 20, hbm_fraction=0.8) as srv:
+            warm = served_requests(np.random.default_rng(99), 12, 1000.0, cfgs, volumes, masks)
+            run_served(srv, warm, metas, sweeps)
+            if prec == engine.BF16:
+                for rate in rates:
+                    reqs = served_requests(np.random.default_rng(int(rate)), args.served_requests, rate, cfgs,
+                                           volumes, masks)
+                    r = run_served(srv, reqs, metas, sweeps)
+                    r["rate_req_s"] = rate
+                    out["bf16"].append(r)
+            else:
+                reqs = served_requests(np.random.default_rng(int(rates[0])), args.served_fp32_requests, rates[0],
+                                       cfgs, volumes, masks)
+                r = run_served(srv, reqs, metas, sweeps, concurrent=False)
+                r["rate_req_s"] = rates[0]
+                out[key] = r
+        for m in fm + rm:
+            m.close()
+    return out
 
 
 def cpu_sample(cfg, t, x0, meta, ticks: int):
@@ -324,6 +445,8 @@ def main():
                 "bytes_per_launch": amount}
     roof.update({"avg_launch_ms": avg_s * 1e3, "share": tot_ms / total_ms})
 
+    served = served_bench(args) if rank == 0 else None
+
     cpu = None
     if rank == 0:
         v, cores, dt = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks)
@@ -338,7 +461,7 @@ def main():
                 "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
                                "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local),
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,
                 "gpu_launches": launches_per_step * args.steps,
                 "kernels": table, "peaks": pk_kind}
         print(json.dumps(line), flush=True)
