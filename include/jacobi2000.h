@@ -122,14 +122,20 @@ jc_status jc_rollout_device(jc_model* m, const float* d_x0, const float* d_meta,
 typedef struct jc_batch jc_batch;
 
 typedef struct {
-    int32_t model;        /* index into the batch's model list */
-    int32_t ticks;        /* rollout length, >= 0 */
-    uint32_t flags;       /* JC_PROJECT_* for this instance */
-    int32_t reserved;     /* must be 0 */
-    const float* x0;      /* initial state [channels, ny, nx] of that model's grid */
+    int32_t model;        /* index into the batch's model list (reconstruct: the forward checkpoint) */
+    int32_t ticks;        /* rollout length / reconstruct horizon H, >= 0 */
+    uint32_t flags;       /* JC_PROJECT_* for this instance (rollouts) */
+    int32_t task;         /* 0 = rollout (forward, or rewind on a reverse checkpoint), 2 = reconstruct */
+    const float* x0;      /* rollout: initial state [channels, ny, nx]; reconstruct: values [H+1, 3, ny, nx] */
     const float* meta;    /* [meta_dim] */
-    float* final_state;   /* receives the state after `ticks` ticks */
-    double* energy;       /* optional [2]: final energy, max relative energy violation */
+    float* final_state;   /* rollout: state after `ticks` ticks; reconstruct: volume [H+1, 3, ny, nx] */
+    double* energy;       /* optional [2]: rollout: final energy, max relative energy violation;
+                             reconstruct: sweeps run, last max |change| */
+    const uint8_t* known; /* reconstruct: [H+1, ny, nx], 1 = known cell */
+    int32_t reverse_model;/* reconstruct: index of the reverse checkpoint (same grid) */
+    int32_t max_sweeps;   /* reconstruct: sweep limit, >= 1 */
+    float tol;            /* reconstruct: stop when the largest change is below tol */
+    int32_t reserved;     /* must be 0 */
 } jc_instance;
 
 /* max_instances / max_cells bound one jc_batch_rollout call; the workspace is
@@ -139,9 +145,14 @@ jc_status jc_batch_create(jc_model* const* models, int32_t n_models, int32_t max
 void jc_batch_destroy(jc_batch* b);
 
 /* Runs every instance to its own horizon; blocks until the results are
- * written. device_pointers = 0: x0/meta/final_state are host memory (copied
- * in and out inside the call); 1: they are device memory. `stream` is a
- * cudaStream_t (null = the batch's own stream). */
+ * written. Rollouts run their ticks; reconstruct instances then run Jacobi
+ * sweeps (the rule of JC_TASK_RECONSTRUCT below) inside one CUDA-graph
+ * conditional while loop that ends on the device when every reconstruct
+ * instance has converged or reached its sweep limit; the whole call is one
+ * graph launch, cached by the batch's shape. device_pointers = 0:
+ * x0/meta/final_state/known are host memory (copied in and out inside the
+ * call); 1: they are device memory. `stream` is a cudaStream_t (null = the
+ * batch's own stream). */
 jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
                            int32_t device_pointers, void* stream);
 

@@ -80,6 +80,32 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
 // flags), f64 sums. init = 1 records mass0 and the energy of the state.
 void projection(const Dims& d, const Pack& p, int init, cudaStream_t s);
 
+// One reconstruct instance of a batch: its space-time volume X[0..H], the
+// step results F_t = step_F(X_{t-1}) (t = 1..H) and R_t = step_R(X_{t+1})
+// (t = 0..H-1), the known values and mask, and its sweep bookkeeping.
+struct ReconDev {
+    float* vol;            // [H+1][3][cells]
+    const float* F;        // [H][3][cells]
+    const float* R;        // [H][3][cells]
+    const float* vals;     // [H+1][3][cells]
+    const uint8_t* known;  // [H+1][cells]
+    long long cells;
+    int H, max_sweeps;
+    float tol;
+    int sweeps, frozen;
+    unsigned resid_bits;   // max |change| of this sweep, as float bits
+    float last_resid;
+};
+
+// X <- known ? value : 0 and bookkeeping reset, for n reconstruct instances.
+void recon_init(ReconDev* d, int n, cudaStream_t s);
+// X_t <- known_t ? value : mean of the available step results, for every
+// instance not yet frozen; records each instance's largest change.
+void recon_update(ReconDev* d, int n, cudaStream_t s);
+// Counts the sweep, freezes converged or exhausted instances and, when
+// use_handle, sets the graph's while condition to "some instance still runs".
+void recon_finalize(ReconDev* d, int n, unsigned long long handle, int use_handle, cudaStream_t s);
+
 // Optional per-launch timing with CUDA events (profiling only; never active
 // during graph capture). Kernels are timed by name on the launching stream.
 struct KernelTimer {

@@ -680,6 +680,7 @@ Batch::Batch(jc_model* const* models, int n_models, int max_inst, long long max_
     }
     const int pp = dims_.P * dims_.P;
     cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking), "cudaStreamCreate");
     ws_.alloc(arena_, dims_, (int)(max_cells / pp) + 1, max_cells, max_inst, m0.w.bf16.get());
     cuda_check(cudaMallocHost(&h_states_, 3 * (size_t)max_cells * 4), "cudaMallocHost", JC_OVER_BUDGET);
     cuda_check(cudaMallocHost(&h_metas_, (size_t)max_inst * 64 * 4), "cudaMallocHost", JC_OVER_BUDGET);
@@ -692,6 +693,7 @@ Batch::~Batch() {
         cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
     }
+    if (stream2_) cudaStreamDestroy(stream2_);
     if (h_states_) cudaFreeHost(h_states_);
     if (h_metas_) cudaFreeHost(h_metas_);
     if (h_slots_) cudaFreeHost(h_slots_);
@@ -709,6 +711,18 @@ Batch::Plan Batch::plan(const jc_instance* in, int n) const {
         if (x.ticks < 0) throw Error(JC_BAD_ARGUMENT, "instance ticks must be >= 0");
         if (x.flags & ~3u) throw Error(JC_BAD_ARGUMENT, "unknown instance flag");
         if (!x.x0 || !x.meta || !x.final_state) throw Error(JC_BAD_ARGUMENT, "null instance buffer");
+        if (x.reserved != 0) throw Error(JC_BAD_ARGUMENT, "jc_instance.reserved must be 0");
+        if (x.task == JC_TASK_RECONSTRUCT) {
+            if (x.reverse_model < 0 || x.reverse_model >= (int)models_.size())
+                throw Error(JC_BAD_ARGUMENT, "reconstruct: reverse model index out of range");
+            const Model &mf = *models_[x.model], &mr = *models_[x.reverse_model];
+            if (mf.cfg.nx != mr.cfg.nx || mf.cfg.ny != mr.cfg.ny)
+                throw Error(JC_BAD_ARGUMENT, "reconstruct: forward and reverse checkpoints differ in grid");
+            if (!x.known || x.ticks < 1 || x.max_sweeps < 1)
+                throw Error(JC_BAD_ARGUMENT, "reconstruct needs a known mask, ticks >= 1 and max_sweeps >= 1");
+            continue;  // sweep phase, planned below
+        }
+        if (x.task != 0) throw Error(JC_BAD_ARGUMENT, "unknown instance task");
         int g = group_of_[x.model];
         if (std::find(gorder.begin(), gorder.end(), g) == gorder.end()) gorder.push_back(g);
     }
@@ -717,7 +731,7 @@ Batch::Plan Batch::plan(const jc_instance* in, int n) const {
     for (int g : gorder) {
         std::vector<int> idx;
         for (int i = 0; i < n; i++)
-            if (group_of_[in[i].model] == g) idx.push_back(i);
+            if (in[i].task == 0 && group_of_[in[i].model] == g) idx.push_back(i);
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return in[a].ticks > in[b].ticks; });
         Plan::Group G;
         G.model = g;
@@ -773,10 +787,146 @@ Batch::Plan Batch::plan(const jc_instance* in, int n) const {
     }
     // meta slots follow the packed order
     for (size_t k = 0; k < p.inst.size(); k++) p.inst[k].meta = ws_.metas + k * 64;
+    p.n_tick_inst = (int)p.inst.size();
+
+    // reconstruct: one F sub-instance per t = 1..H (forward weights) and one
+    // R sub-instance per t = 0..H-1 (reverse weights), grouped by weights
+    struct Sub {
+        const Model* m;
+        size_t state_off, out_off;
+        int recon;
+    };
+    std::map<int, std::vector<Sub>> subs;  // weight group -> sub-instances
+    std::vector<int> sg_order;
+    for (int i = 0; i < n; i++) {
+        const jc_instance& x = in[i];
+        if (x.task != JC_TASK_RECONSTRUCT) continue;
+        const Model& mf = *models_[x.model];
+        Plan::Recon r{};
+        r.order = i;
+        r.H = x.ticks;
+        r.nx = mf.cfg.nx;
+        r.ny = mf.cfg.ny;
+        r.cells = (long long)r.nx * r.ny;
+        r.max_sweeps = x.max_sweeps;
+        r.tol = x.tol;
+        const size_t len = 3 * (size_t)r.cells, H = (size_t)r.H;
+        r.off_vol = p.recon_floats;
+        p.recon_floats += (H + 1) * len;
+        r.off_F = p.recon_floats;
+        p.recon_floats += H * len;
+        r.off_R = p.recon_floats;
+        p.recon_floats += H * len;
+        r.off_vals = p.recon_floats;
+        p.recon_floats += (H + 1) * len;
+        r.off_known = p.recon_bytes;
+        p.recon_bytes += (H + 1) * (size_t)r.cells;
+        const int gf = group_of_[x.model], gr = group_of_[x.reverse_model];
+        for (int gg : {gf, gr})
+            if (std::find(sg_order.begin(), sg_order.end(), gg) == sg_order.end()) sg_order.push_back(gg);
+        const int ri = (int)p.recons.size();
+        for (int t = 1; t <= r.H; t++)
+            subs[gf].push_back({&mf, r.off_vol + (size_t)(t - 1) * len, r.off_F + (size_t)(t - 1) * len, ri});
+        for (int t = 0; t < r.H; t++)
+            subs[gr].push_back({models_[x.reverse_model], r.off_vol + (size_t)(t + 1) * len, r.off_R + (size_t)t * len, ri});
+        p.recons.push_back(r);
+    }
+    int base = p.n_tick_inst;
+    for (int g : sg_order) {
+        Plan::Group G;
+        G.model = g;
+        G.inst_base = base;
+        G.n = (int)subs[g].size();
+        G.row_base = 0;
+        G.cell_base = 0;
+        G.cell_base_i = 0;
+        G.max_cells = 0;
+        int rows = 0, tiles = 0, ttiles = 0, ctiles = 0;
+        long long cells = 0;
+        for (auto& sb : subs[g]) {
+            const Model& m = *sb.m;
+            InstDev d{};
+            d.row0 = rows;
+            d.tx = m.cfg.nx / m.cfg.patch;
+            d.ty = m.cfg.ny / m.cfg.patch;
+            d.nx = m.cfg.nx;
+            d.ny = m.cfg.ny;
+            d.cell0 = cells;
+            d.pos = m.w.pos;
+            d.meta = ws_.metas + (size_t)(p.n_tick_inst + sb.recon) * 64;
+            d.flags = 4u;
+            d.tile0 = tiles;
+            d.tt0 = ttiles;
+            d.ct0 = ctiles;
+            p.inst.push_back(d);
+            p.sub_off.push_back({sb.state_off, sb.out_off});
+            rows += d.tx * d.ty;
+            cells += (long long)d.nx * d.ny;
+            tiles += cell_tiles(d.nx, d.ny);
+            ttiles += conv_tiles(d.tx, d.ty);
+            ctiles += conv_tiles(d.nx, d.ny);
+            G.rows.push_back(rows);
+            G.cells.push_back(cells);
+            G.tiles.push_back(tiles);
+            G.ttiles.push_back(ttiles);
+            G.ctiles.push_back(ctiles);
+            G.ticks.push_back(0);
+            G.max_cells = std::max(G.max_cells, (long long)d.nx * d.ny);
+        }
+        if (rows > ws_.max_rows || cells > ws_.max_cells)
+            throw Error(JC_OVER_BUDGET, "a reconstruct sweep needs more cells than the batch was created for");
+        base += G.n;
+        p.sgroups.push_back(std::move(G));
+    }
+    if ((int)p.inst.size() > ws_.max_inst || p.n_tick_inst + (int)p.recons.size() > ws_.max_inst)
+        throw Error(JC_OVER_BUDGET, "reconstruct sub-instances exceed the batch's instance capacity");
     return p;
 }
 
-void Batch::enqueue(const Plan& p, cudaStream_t s) const {
+void Batch::bind_recon(Plan& p) {
+    if (p.recons.empty()) return;
+    bool grew = false;
+    if (p.recon_floats > recon_f_cap_) {
+        if (recon_f_) arena_.release(recon_f_);
+        recon_f_cap_ = p.recon_floats;
+        recon_f_ = arena_.alloc_n<float>(recon_f_cap_);
+        grew = true;
+    }
+    if (p.recon_bytes > recon_u8_cap_) {
+        if (recon_u8_) arena_.release(recon_u8_);
+        recon_u8_cap_ = p.recon_bytes;
+        recon_u8_ = arena_.alloc_n<uint8_t>(recon_u8_cap_);
+        grew = true;
+    }
+    if ((int)p.recons.size() > recon_cap_) {
+        if (d_recon_) arena_.release(d_recon_);
+        recon_cap_ = (int)p.recons.size();
+        d_recon_ = arena_.alloc_n<ReconDev>(recon_cap_);
+        grew = true;
+    }
+    if (grew) {  // cached graphs hold the old buffers
+        for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+        graphs_.clear();
+    }
+    for (size_t k = 0; k < p.sub_off.size(); k++) {
+        InstDev& d = p.inst[p.n_tick_inst + k];
+        d.state = recon_f_ + p.sub_off[k].first;
+        d.out = recon_f_ + p.sub_off[k].second;
+    }
+}
+
+void Batch::enqueue_sweep(const Plan& p, cudaStream_t s) const {
+    for (const auto& G : p.sgroups) {
+        if (G.n == 0) continue;
+        Pack v = ws_.view(dims_, G.inst_base, G.n, 0, G.rows.back(), 0, G.cells.back(), G.tiles.back(),
+                          G.ttiles.back(), G.ctiles.back());
+        v.max_inst_cells = G.max_cells;
+        models_[G.model]->forward_pack(v, kWriteNextState, s);
+    }
+    recon_update(d_recon_, (int)p.recons.size(), s);
+}
+
+void Batch::enqueue(const Plan& p, cudaStream_t s, bool capture) const {
     for (const auto& G : p.groups) {
         if (G.n == 0) continue;
         Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
@@ -796,12 +946,91 @@ void Batch::enqueue(const Plan& p, cudaStream_t s) const {
             projection(dims_, v, 0, s);
         }
     }
+    if (p.recons.empty()) return;
+    const int nrec = (int)p.recons.size();
+    recon_init(d_recon_, nrec, s);
+    if (!capture) {
+        // outside a graph (profiling): sweeps up to the largest limit; frozen
+        // instances are left unchanged by the update
+        int most = 0;
+        for (const auto& r : p.recons) most = std::max(most, r.max_sweeps);
+        for (int k = 0; k < most; k++) {
+            enqueue_sweep(p, s);
+            recon_finalize(d_recon_, nrec, 0ull, 0, s);
+        }
+        return;
+    }
+    // a conditional while node: its body is one sweep plus the kernel that
+    // decides on the device whether another sweep runs
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cuda_check(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps), "cudaStreamGetCaptureInfo");
+    if (st != cudaStreamCaptureStatusActive) throw Error(JC_CUDA_ERROR, "reconstruct loop outside a capture");
+    cudaGraphConditionalHandle h;
+    cuda_check(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault), "conditional handle");
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    std::vector<cudaGraphNode_t> dv(deps, deps + ndeps);
+    cuda_check(cudaGraphAddNode(&cn, g, dv.data(), nullptr, dv.size(), &cp), "conditional node");
+    cuda_check(cudaStreamUpdateCaptureDependencies(s, &cn, nullptr, 1, cudaStreamSetCaptureDependencies),
+               "capture dependencies");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cuda_check(cudaStreamBeginCaptureToGraph(stream2_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+               "capture the loop body");
+    try {
+        enqueue_sweep(p, stream2_);
+        recon_finalize(d_recon_, nrec, (unsigned long long)h, 1, stream2_);
+    } catch (...) {
+        cudaGraph_t tmp;
+        cudaStreamEndCapture(stream2_, &tmp);
+        throw;
+    }
+    cuda_check(cudaStreamEndCapture(stream2_, &body), "end body capture");
+}
+
+void Batch::upload_recon(const Plan& p, const jc_instance* in, bool device_ptrs, cudaStream_t s) {
+    if (p.recons.empty()) return;
+    const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    std::vector<ReconDev> rd;
+    for (const auto& r : p.recons) {
+        const jc_instance& x = in[r.order];
+        const size_t len = 3 * (size_t)r.cells, H = (size_t)r.H;
+        cuda_check(cudaMemcpyAsync(recon_f_ + r.off_vals, x.x0, (H + 1) * len * 4, kind, s), "reconstruct values",
+                   JC_MAP);
+        cuda_check(cudaMemcpyAsync(recon_u8_ + r.off_known, x.known, (H + 1) * (size_t)r.cells, kind, s),
+                   "reconstruct mask", JC_MAP);
+        ReconDev d{};
+        d.vol = recon_f_ + r.off_vol;
+        d.F = recon_f_ + r.off_F;
+        d.R = recon_f_ + r.off_R;
+        d.vals = recon_f_ + r.off_vals;
+        d.known = recon_u8_ + r.off_known;
+        d.cells = r.cells;
+        d.H = r.H;
+        d.max_sweeps = r.max_sweeps;
+        d.tol = r.tol;
+        rd.push_back(d);
+    }
+    cuda_check(cudaMemcpyAsync(d_recon_, rd.data(), rd.size() * sizeof(ReconDev), cudaMemcpyHostToDevice, s),
+               "reconstruct descriptors", JC_MAP);
+    // each reconstruct instance's meta, read by its sweep sub-instances
+    for (size_t ri = 0; ri < p.recons.size(); ri++)
+        cuda_check(cudaMemcpyAsync(ws_.metas + (size_t)(p.n_tick_inst + ri) * 64, in[p.recons[ri].order].meta,
+                                   dims_.meta_dim * 4, kind, s),
+                   "reconstruct meta", JC_MAP);
 }
 
 void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t s) {
     if (!s) s = stream_;
     Plan p = plan(in, n);
     if (n == 0) return;
+    bind_recon(p);
     const int md = dims_.meta_dim;
     long long total = 0;
     for (size_t k = 0; k < p.order.size(); k++) {
@@ -826,9 +1055,15 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
     cuda_check(cudaMemcpyAsync(ws_.base.inst, p.inst.data(), p.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
                                s),
                "instance descriptors", JC_MAP);
+    upload_recon(p, in, device_ptrs, s);
     prepare_maps(p, s);
     std::vector<long long> key;
     key.push_back((long long)(uintptr_t)s);
+    for (const auto& r : p.recons) {
+        key.push_back(-1000000 - r.H);
+        key.push_back(((long long)r.nx << 20) | r.ny);
+        key.push_back((long long)in[r.order].model * 4096 + in[r.order].reverse_model);
+    }
     for (const auto& G : p.groups) {
         key.push_back(-1 - G.model);
         for (size_t k = 0; k < G.ticks.size(); k++) {
@@ -842,7 +1077,7 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
         cudaGraph_t g;
         cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
         try {
-            enqueue(p, s);
+            enqueue(p, s, true);
         } catch (...) {
             cudaStreamEndCapture(s, &g);
             if (g) cudaGraphDestroy(g);
@@ -856,6 +1091,18 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
         it = graphs_.emplace(key, ge).first;
     }
     cuda_check(cudaGraphLaunch(it->second, s), "graph launch");
+    std::vector<ReconDev> rres(p.recons.size());
+    for (size_t ri = 0; ri < p.recons.size(); ri++) {
+        const auto& r = p.recons[ri];
+        const jc_instance& x = in[r.order];
+        const size_t bytes = (size_t)(r.H + 1) * 3 * (size_t)r.cells * 4;
+        cuda_check(cudaMemcpyAsync(x.final_state, recon_f_ + r.off_vol, bytes,
+                                   device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s),
+                   "reconstruct volume", JC_MAP);
+    }
+    if (!p.recons.empty())
+        cuda_check(cudaMemcpyAsync(rres.data(), d_recon_, rres.size() * sizeof(ReconDev), cudaMemcpyDeviceToHost, s),
+                   "reconstruct results", JC_MAP);
     if (device_ptrs) {
         for (size_t k = 0; k < p.order.size(); k++) {
             const InstDev& d = p.inst[k];
@@ -880,11 +1127,18 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
             x.energy[1] = h_slots_[k].max_viol;
         }
     }
+    for (size_t ri = 0; ri < p.recons.size(); ri++) {
+        const jc_instance& x = in[p.recons[ri].order];
+        if (x.energy) {
+            x.energy[0] = rres[ri].sweeps;
+            x.energy[1] = rres[ri].last_resid;
+        }
+    }
 }
 
 std::map<std::string, std::pair<int, double>> Batch::profile(const jc_instance* in, int n, bool device_ptrs) {
-    (void)device_ptrs;
     Plan p = plan(in, n);
+    bind_recon(p);
     cudaStream_t s = stream_;
     for (size_t k = 0; k < p.order.size(); k++) {
         const jc_instance& x = in[p.order[k]];
@@ -900,11 +1154,12 @@ std::map<std::string, std::pair<int, double>> Batch::profile(const jc_instance* 
     cuda_check(cudaMemcpyAsync(ws_.base.inst, p.inst.data(), p.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
                                s),
                "instance descriptors", JC_MAP);
+    upload_recon(p, in, device_ptrs, s);
     prepare_maps(p, s);
     KernelTimer kt;
     g_ktimer = &kt;
     try {
-        enqueue(p, s);
+        enqueue(p, s, false);
     } catch (...) {
         g_ktimer = nullptr;
         throw;
@@ -922,6 +1177,12 @@ void Batch::prepare_maps(const Plan& p, cudaStream_t s) const {
         if (G.n == 0) continue;
         Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
                           G.tiles.back(), G.ttiles.back(), G.ctiles.back());
+        m0.w.bf16->prepare(dims_, v, p.inst.data() + G.inst_base, s);
+    }
+    for (const auto& G : p.sgroups) {
+        if (G.n == 0) continue;
+        Pack v = ws_.view(dims_, G.inst_base, G.n, 0, G.rows.back(), 0, G.cells.back(), G.tiles.back(),
+                          G.ttiles.back(), G.ctiles.back());
         m0.w.bf16->prepare(dims_, v, p.inst.data() + G.inst_base, s);
     }
 }

@@ -150,6 +150,12 @@ class Batch {
     DeviceArena arena_;
     Workspace ws_;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t stream2_ = nullptr;  // captures the body of the reconstruct while loop
+    float* recon_f_ = nullptr;        // reconstruct volumes, step results and values
+    uint8_t* recon_u8_ = nullptr;     // reconstruct masks
+    size_t recon_f_cap_ = 0, recon_u8_cap_ = 0;
+    ReconDev* d_recon_ = nullptr;
+    int recon_cap_ = 0;
     float* h_states_ = nullptr;  // pinned [3 * max_cells]
     float* h_metas_ = nullptr;   // pinned [max_inst * 64]
     ProjSlot* h_slots_ = nullptr;
@@ -166,9 +172,25 @@ class Batch {
         std::vector<Group> groups;
         std::vector<long long> state_off;  // per packed instance, floats
         int max_ticks = 0;
+        // reconstruct instances and their sweep-phase groups
+        struct Recon {
+            int order;  // caller index
+            int H, nx, ny, max_sweeps;
+            float tol;
+            long long cells;
+            size_t off_vol, off_F, off_R, off_vals, off_known;
+        };
+        std::vector<Recon> recons;
+        std::vector<Group> sgroups;
+        int n_tick_inst = 0;
+        std::vector<std::pair<size_t, size_t>> sub_off;  // sweep sub-instances: (state, out) slab offsets
+        size_t recon_floats = 0, recon_bytes = 0;
     };
     Plan plan(const jc_instance* inst, int n) const;
-    void enqueue(const Plan& p, cudaStream_t s) const;
+    void bind_recon(Plan& p);
+    void enqueue(const Plan& p, cudaStream_t s, bool capture) const;
+    void enqueue_sweep(const Plan& p, cudaStream_t s) const;
+    void upload_recon(const Plan& p, const jc_instance* in, bool device_ptrs, cudaStream_t s);
     void prepare_maps(const Plan& p, cudaStream_t s) const;
     std::map<std::vector<long long>, cudaGraphExec_t> graphs_;
 };

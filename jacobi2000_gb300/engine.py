@@ -197,8 +197,10 @@ def project_energy(x, prev_energy: float, config: JcConfig, cells: int) -> np.nd
 
 
 class JcInstance(C.Structure):
-    _fields_ = [("model", C.c_int32), ("ticks", C.c_int32), ("flags", C.c_uint32), ("reserved", C.c_int32),
-                ("x0", C.c_void_p), ("meta", C.c_void_p), ("final_state", C.c_void_p), ("energy", C.c_void_p)]
+    _fields_ = [("model", C.c_int32), ("ticks", C.c_int32), ("flags", C.c_uint32), ("task", C.c_int32),
+                ("x0", C.c_void_p), ("meta", C.c_void_p), ("final_state", C.c_void_p), ("energy", C.c_void_p),
+                ("known", C.c_void_p), ("reverse_model", C.c_int32), ("max_sweeps", C.c_int32), ("tol", C.c_float),
+                ("reserved", C.c_int32)]
 
 
 def _declare_batch(L):
@@ -252,15 +254,34 @@ class Batch:
         self.close()
 
     def _instances(self, items, device: bool):
+        """Items are tuples (model, x0, meta, ticks[, flags[, final_device_ptr]])
+        for rollouts, or dicts with task=2 (reconstruct): model,
+        reverse_model, x (values [H+1,3,ny,nx]), known ([H+1,ny,nx]), meta,
+        ticks, max_sweeps, tol."""
         n = len(items)
         arr = (JcInstance * n)()
         keep = []
         outs = []
         for k, it in enumerate(items):
+            e = np.zeros(2, dtype=np.float64)
+            keep.append(e)
+            if isinstance(it, dict):
+                m = self.models[it["model"]]
+                c = m.config
+                H = int(it["ticks"])
+                xa = np.ascontiguousarray(it["x"], dtype=np.float32).reshape(H + 1, 3, c.ny, c.nx)
+                ka = np.ascontiguousarray(it["known"], dtype=np.uint8).reshape(H + 1, c.ny, c.nx)
+                ma = m._meta(it["meta"])
+                out = np.empty_like(xa)
+                keep += [xa, ka, ma]
+                arr[k] = JcInstance(int(it["model"]), H, 0, TASK_RECONSTRUCT, xa.ctypes.data, ma.ctypes.data,
+                                    out.ctypes.data, e.ctypes.data, ka.ctypes.data, int(it["reverse_model"]),
+                                    int(it.get("max_sweeps", 4)), float(it.get("tol", 1e-3)), 0)
+                outs.append((out, e))
+                continue
             mi, x0, meta, ticks = it[0], it[1], it[2], it[3]
             flags = it[4] if len(it) > 4 else PROJECT_MASS | PROJECT_ENERGY
             m = self.models[mi]
-            e = np.zeros(2, dtype=np.float64)
             if device:
                 # (x0, meta, final) are device pointers (ints)
                 x0p, metap, outp = int(x0), int(meta), int(it[5])
@@ -271,14 +292,14 @@ class Batch:
                 out = np.empty(m.shape, dtype=np.float32)
                 keep += [xa, ma]
                 x0p, metap, outp = xa.ctypes.data, ma.ctypes.data, out.ctypes.data
-            arr[k] = JcInstance(int(mi), int(ticks), int(flags), 0, x0p, metap, outp, e.ctypes.data)
-            keep.append(e)
+            arr[k] = JcInstance(int(mi), int(ticks), int(flags), 0, x0p, metap, outp, e.ctypes.data, None, 0, 0, 0.0, 0)
             outs.append((out, e))
         return arr, keep, outs
 
     def rollout(self, items, device: bool = False, stream: int | None = None):
         """Returns [(final_state, final_energy, max_violation)] in input order
-        (final_state is None with device pointers)."""
+        (final_state is None with device pointers); for reconstruct items
+        [(volume, sweeps, last_residual)]."""
         arr, keep, outs = self._instances(items, device)
         _check(self._L.jc_batch_rollout(self._h, arr, len(items), int(device), stream))
         return [(o, float(e[0]), float(e[1])) for o, e in outs]
