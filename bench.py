@@ -59,6 +59,7 @@ def parse_args():
                     help="request arrival rates (req/s) of the served-form run; empty to skip")
     ap.add_argument("--served-requests", type=int, default=240)
     ap.add_argument("--served-fp32-requests", type=int, default=24)
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-task batch measurement")
     return ap.parse_args()
 
 
@@ -286,6 +287,68 @@ def served_bench(args):
     return out
 
 
+MIXED_SIDES = [32, 64, 96, 128, 192]
+
+
+def mixed_batch_bench(args, steps=3):
+    """Config: 64 instances in one batch call, sides uniform in {32, 64, 96,
+    128, 192}, horizons U[10, 50]; 1/3 forward, 1/3 rewind (the reverse
+    family), 1/3 reconstruct (2% of space-time cells known, 4 Jacobi sweeps).
+    Timed end to end with host buffers, with the autotuned schedules and with
+    the fixed default schedule."""
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.checkpoint import parse_config, synthetic_family, write_safetensors_bytes, meta_of
+    from jacobi2000_gb300.ic import random_drops
+
+    fam_f = synthetic_family(args.dim, args.layers, 0, MIXED_SIDES)
+    fam_r = synthetic_family(args.dim, args.layers, 1, MIXED_SIDES)
+    cfgs = [parse_config(fam_f[(s, s)][1], fam_f[(s, s)][0]) for s in MIXED_SIDES]
+    models = [engine.Model.from_bytes(write_safetensors_bytes(f[(s, s)][0]), f[(s, s)][1], engine.BF16)
+              for f in (fam_f, fam_r) for s in MIXED_SIDES]
+    nf = len(MIXED_SIDES)
+    rng = np.random.default_rng(4)
+    me = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+    items, useful, n_inst, recon_cells, tick_cells = [], 0, 0, 0, 0
+    for k in range(64):
+        g = int(rng.integers(nf))
+        cfg, H = cfgs[g], int(rng.integers(10, 51))
+        cells = cfg.nx * cfg.ny
+        useful += cells * H
+        task = k % 3
+        if task < 2:
+            items.append((g + nf * task, random_drops(cfg, seed=int(rng.integers(1 << 30))), meta_of(cfg), H, me))
+            n_inst += 1
+            tick_cells += cells
+        else:
+            known = rng.random((H + 1, cfg.ny, cfg.nx)) < 0.02
+            vals = np.where(known[:, None], (0.3 * rng.standard_normal((H + 1, 3, cfg.ny, cfg.nx))), 0)
+            items.append({"task": engine.TASK_RECONSTRUCT, "model": g, "reverse_model": g + nf,
+                          "x": vals.astype(np.float32), "known": known.astype(np.uint8), "meta": meta_of(cfg),
+                          "ticks": H, "max_sweeps": 4, "tol": 0.0})
+            n_inst += 2 * H + 2
+            recon_cells += cells * (2 * H + 2)
+    out = {"instances": 64, "sides": MIXED_SIDES, "horizon": "U[10,50] ticks",
+           "task_mix": "1/3 forward, 1/3 rewind, 1/3 reconstruct (2% known, 4 Jacobi sweeps)",
+           "useful_cell_ticks": useful, "timing": "wall clock per batch call, host buffers in and out"}
+    prev = engine.autotune(None)
+    try:
+        with engine.Batch(models, max_instances=n_inst, max_cells=max(tick_cells, recon_cells)) as b:
+            for key, on in (("default_schedule", False), ("autotuned", True)):
+                engine.autotune(on)
+                b.rollout(items)  # capture (and, when on, tune) outside the timed calls
+                t0 = time.perf_counter()
+                for _ in range(steps):
+                    b.rollout(items)
+                dt = (time.perf_counter() - t0) / steps
+                out[key] = {"s_per_batch": dt, "cell_ticks_per_s": useful / dt}
+    finally:
+        engine.autotune(prev)
+        for m in models:
+            m.close()
+    out["autotune_speedup"] = out["default_schedule"]["s_per_batch"] / out["autotuned"]["s_per_batch"]
+    return out
+
+
 def cpu_sample(cfg, t, x0, meta, ticks: int):
     """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
     masked scan) on all host cores, over `ticks` ticks of one instance."""
@@ -446,6 +509,7 @@ def main():
     roof.update({"avg_launch_ms": avg_s * 1e3, "share": tot_ms / total_ms})
 
     served = served_bench(args) if rank == 0 else None
+    mixed = mixed_batch_bench(args) if rank == 0 and not args.no_mixed else None
 
     cpu = None
     if rank == 0:
@@ -462,6 +526,7 @@ def main():
                 "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
                                "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,
+                "mixed_batch": mixed,
                 "gpu_launches": launches_per_step * args.steps,
                 "kernels": table, "peaks": pk_kind}
         print(json.dumps(line), flush=True)

@@ -257,6 +257,20 @@ double jc_energy(const float* x, const jc_config* cfg, int64_t n);
 void   jc_project_mass(float* x, double target, int64_t n);
 void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int64_t n);
 
+/* Autotuning of the BF16 schedules (no counterpart in the reference, whose
+ * GPU backend has one fixed workgroup shape per kernel). With enable = 1 (the
+ * default; environment JC_AUTOTUNE=0 starts with it off) the first BF16
+ * launch outside a stream capture for each row-count bucket (powers of two of
+ * token rows) times the candidate schedules of the fused MLP (64 or 128 hidden
+ * columns per step) and of the attention (64, 128 or 256 threads per CTA) with
+ * CUDA events, once, and later launches and graph captures use the fastest.
+ * enable = 0 selects the fixed schedule (64 columns, 256 threads); enable < 0
+ * only queries. Returns the setting before the call. If JC_AUTOTUNE_CACHE
+ * names a file, tuned schedules are appended to it and read back by models
+ * created later. Results are identical under every schedule: the candidates
+ * differ in tiling, not in arithmetic order of any sum. */
+int32_t jc_autotune(int32_t enable);
+
 /* Thread-local description of the last failure on this thread ("" if none). */
 const char* jc_last_error(void);
 

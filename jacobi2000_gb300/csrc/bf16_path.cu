@@ -19,6 +19,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <stdexcept>
@@ -961,6 +963,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
                     "the BF16 path needs dim a multiple of 32 and <= 256, heads dividing 32, a cell-head width of 32, "
                     "3 channels and patch 4");
     nc_mlp = 64;
+    n_nc = (D <= 128 && F % 128 == 0) ? 2 : 1;  // nc 128 needs 128 KB of shared memory at dim 128
     bn_qkv = (3 * D) % 128 == 0 ? 128 : 3 * D;
     bn_tm = D <= 128 ? D : 64;
     if (F % nc_mlp) throw Error(JC_LIMIT, "the MLP width must be a multiple of the MLP chunk");
@@ -975,16 +978,19 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
         const auto& wpr = tget(t, p + "proj.weight").data;
         wp[l] = upload_bf16(arena, blocked(D, D, D, [&](int n, int kk) { return wpr[(size_t)kk * D + n]; }));
         const auto& w1h = tget(t, p + "ff1.weight").data;  // [D, F]
-        w1[l] = upload_bf16(arena, blocked(F, D, nc_mlp, [&](int n, int kk) { return w1h[(size_t)kk * F + n]; }));
-        // W2 chunk j: B2_j[n][k] = W2[j*NC + k][n] -> [j][NC/8][D][8]
         const auto& w2h = tget(t, p + "ff2.weight").data;  // [F, D]
-        std::vector<uint16_t> w2b((size_t)F * D);
-        size_t i = 0;
-        for (int j = 0; j < F / nc_mlp; j++)
-            for (int kc = 0; kc < nc_mlp / 8; kc++)
-                for (int n = 0; n < D; n++)
-                    for (int e = 0; e < 8; e++) w2b[i++] = f2bf(w2h[(size_t)(j * nc_mlp + kc * 8 + e) * D + n]);
-        w2[l] = upload_bf16(arena, w2b);
+        for (int v = 0; v < n_nc; v++) {
+            const int nc = v == 0 ? 64 : 128;
+            w1v[v][l] = upload_bf16(arena, blocked(F, D, nc, [&](int n, int kk) { return w1h[(size_t)kk * F + n]; }));
+            // W2 chunk j: B2_j[n][k] = W2[j*nc + k][n] -> [j][nc/8][D][8]
+            std::vector<uint16_t> w2b((size_t)F * D);
+            size_t i = 0;
+            for (int j = 0; j < F / nc; j++)
+                for (int kc = 0; kc < nc / 8; kc++)
+                    for (int n = 0; n < D; n++)
+                        for (int e = 0; e < 8; e++) w2b[i++] = f2bf(w2h[(size_t)(j * nc + kc * 8 + e) * D + n]);
+            w2v[v][l] = upload_bf16(arena, w2b);
+        }
     }
     {
         // token_mix: per N block of 128 (or D) and tap: [C/8][BN][8] of W[co][ci][ky][kx]
@@ -1035,6 +1041,9 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
                     }
         wc1 = upload_bf16(arena, o);
     }
+    cache_key_ = "d" + std::to_string(D) + "_l" + std::to_string(d.L) + "_f" + std::to_string(F) + "_r" +
+                 std::to_string(d.radius) + "_k" + std::to_string(d.mask_kind) + "_g" + std::to_string(d.dilation);
+    load_cache();
     set_smem(tc_gemm_kernel<EPI_BF16>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_F32>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
@@ -1044,6 +1053,148 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(bf_embed_kernel<1>, 100 * 1024);
     set_smem(bf_embed_kernel<4>, 100 * 1024);
     set_smem(bf_embed_kernel<8>, 100 * 1024);
+}
+
+static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
+                             int threads, cudaStream_t s) {
+    const int wpb = threads / 32;
+    const unsigned blocks = (unsigned)((R + wpb - 1) / wpb);
+    const int fpl = d.D / 32;
+    const bool r1 = d.mask_kind == 1 && d.radius == 1;
+    if (fpl == 1) {
+        if (r1) bf_attention_r1_kernel<1><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+        else bf_attention_kernel<1><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+    } else if (fpl == 4) {
+        if (r1) bf_attention_r1_kernel<4><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+        else bf_attention_kernel<4><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+    } else if (fpl == 8) {
+        if (r1) bf_attention_r1_kernel<8><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+        else bf_attention_kernel<8><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
+    } else {
+        throw Error(JC_LIMIT, "the BF16 attention supports dim 32, 128 or 256");
+    }
+}
+
+static int initial_autotune() {
+    const char* e = std::getenv("JC_AUTOTUNE");
+    return e && std::atoi(e) == 0 ? 0 : 1;
+}
+std::atomic<int> g_autotune{initial_autotune()};
+
+static int row_bucket(int R) {
+    int b = 128;
+    while (b < R && b < (1 << 30)) b <<= 1;
+    return b;
+}
+
+Tuning BF16Path::tuning_for(int rows) const {
+    std::lock_guard<std::mutex> lk(tune_mu_);
+    if (g_autotune.load()) {
+        auto it = tuned_.find(row_bucket(rows));
+        if (it != tuned_.end()) return it->second;
+    }
+    return Tuning{nc_mlp, 256};
+}
+
+// Times `launch` with CUDA events: one warm-up, then `reps` launches.
+template <class F>
+static float time_launches(F&& launch, int reps, cudaStream_t s) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    launch();
+    cudaEventRecord(a, s);
+    for (int i = 0; i < reps; i++) launch();
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+}
+
+void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStream_t s) const {
+    if (!g_autotune.load() || p.R == 0) return;
+    const int bucket = row_bucket(p.R);
+    {
+        std::lock_guard<std::mutex> lk(tune_mu_);
+        if (tuned_.count(bucket)) return;
+    }
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    const int R = p.R, D = d.D;
+    bf16* ln = reinterpret_cast<bf16*>(p.bt[0]);
+    bf16* qkv = reinterpret_cast<bf16*>(p.bt[1]);
+    bf16* attn = reinterpret_cast<bf16*>(p.bt[2]);
+    const CUtensorMap m_ln = rows_map(ln, D, R);
+    const unsigned gm = (unsigned)((R + 127) / 128);
+    Tuning best{nc_mlp, 256};
+    // the workspace holds transient values; the timed launches may leave
+    // anything in it (every forward rewrites it from the state)
+    float best_ms = 1e30f;
+    for (int v = 0; v < n_nc; v++) {
+        const int NC = v == 0 ? 64 : 128;
+        const size_t smem = std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
+        const float ms = time_launches(
+            [&] {
+                tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1v[v][0], w2v[v][0], w.blk[0].b1, w.blk[0].b2, D,
+                                                            d.F, NC, R, p.x, w.norm_g, w.norm_b, ln, p.err);
+            },
+            3, s);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.nc = NC;
+        }
+    }
+    best_ms = 1e30f;
+    for (int threads : {64, 128, 256}) {
+        const float ms = time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s); }, 3, s);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.attn_threads = threads;
+        }
+    }
+    cuda_check(cudaGetLastError(), "autotune");
+    {
+        std::lock_guard<std::mutex> lk(tune_mu_);
+        tuned_[bucket] = best;
+    }
+    save_cache(bucket, best);
+}
+
+// Tuned schedules persist in the JSON-lines file named by JC_AUTOTUNE_CACHE,
+// one object per tuned row bucket:
+//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "nc": 64, "attn_threads": 128}
+// keyed by the model shape (dim, layers, MLP width, mask radius, kind and
+// dilation). Lines that do not parse or name another shape are skipped;
+// later lines override earlier ones.
+void BF16Path::load_cache() {
+    const char* path = std::getenv("JC_AUTOTUNE_CACHE");
+    if (!path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char line[512], key[128];
+    while (std::fgets(line, sizeof line, f)) {
+        int bucket, nc, th;
+        if (std::sscanf(line, " {\"model\": \"%127[^\"]\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d", key,
+                        &bucket, &nc, &th) != 4)
+            continue;
+        if (cache_key_ == key && (nc == 64 || (nc == 128 && n_nc == 2)) && (th == 64 || th == 128 || th == 256))
+            tuned_[bucket] = Tuning{nc, th};
+    }
+    std::fclose(f);
+}
+
+void BF16Path::save_cache(int bucket, const Tuning& t) const {
+    const char* path = std::getenv("JC_AUTOTUNE_CACHE");
+    if (!path) return;
+    std::lock_guard<std::mutex> lk(tune_mu_);
+    FILE* f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "{\"model\": \"%s\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d}\n", cache_key_.c_str(), bucket,
+                 t.nc, t.attn_threads);
+    std::fclose(f);
 }
 
 void BF16Path::alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows, long long cells, int max_inst) const {
@@ -1084,6 +1235,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     float* c1 = reinterpret_cast<float*>(p.bc[1]);
     const CUtensorMap m_ln = rows_map(ln, D, R), m_attn = rows_map(attn, D, R), m_t1 = rows_map(t1, D, R);
     const unsigned gm = (unsigned)((R + 127) / 128);
+    const Tuning tu = tuning_for(R);
     {
         KScope k("bf_embed", s);
         const unsigned blocks = (unsigned)((R + kEmbedRows - 1) / kEmbedRows);
@@ -1105,21 +1257,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         }
         {
             KScope k("bf_attention", s);
-            const unsigned blocks = (unsigned)((R + 7) / 8);
-            const int fpl = D / 32;
-            const bool r1 = d.mask_kind == 1 && d.radius == 1;
-            if (fpl == 1) {
-                if (r1) bf_attention_r1_kernel<1><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-                else bf_attention_kernel<1><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            } else if (fpl == 4) {
-                if (r1) bf_attention_r1_kernel<4><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-                else bf_attention_kernel<4><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            } else if (fpl == 8) {
-                if (r1) bf_attention_r1_kernel<8><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-                else bf_attention_kernel<8><<<blocks, 256, 0, s>>>(d, qkv, p.inst, n, R, attn);
-            } else {
-                throw Error(JC_LIMIT, "the BF16 attention supports dim 32, 128 or 256");
-            }
+            launch_attention(d, qkv, p.inst, n, R, attn, tu.attn_threads, s);
             check_launch("bf_attention");
         }
         {
@@ -1132,12 +1270,12 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         }
         {
             KScope k("tc_mlp", s);
-            const int NC = nc_mlp;
+            const int NC = tu.nc, v = NC == 128 ? 1 : 0;
             const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
             const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
             const size_t smem = std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
-            tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1[l], w2[l], B.b1, B.b2, D, d.F, NC, R, p.x, ng, nbeta, ln,
-                                                p.err);
+            tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, NC, R, p.x, ng,
+                                                        nbeta, ln, p.err);
             check_launch("tc_mlp");
         }
     }

@@ -5,9 +5,25 @@
 
 #include <cuda_bf16.h>
 
+#include <atomic>
+#include <map>
+#include <mutex>
+
 #include "runtime.hpp"
 
 namespace jc {
+
+// A schedule the autotuner picks per (row-count bucket): the MLP's hidden
+// chunk width and the attention kernel's CTA size.
+struct Tuning {
+    int nc;            // 64 or 128 hidden columns per MLP step
+    int attn_threads;  // 64, 128 or 256
+};
+
+// 1 (default; environment JC_AUTOTUNE=0 turns it off): BF16 launches time the
+// candidate schedules once per row-count bucket and keep the fastest; 0: the
+// fixed default schedule {nc 64, 256 threads}.
+extern std::atomic<int> g_autotune;
 
 class BF16Path {
    public:
@@ -19,13 +35,28 @@ class BF16Path {
     // host-side descriptors are `hinst` (same order as the device array).
     void prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s) const;
     void forward(const Dims& d, const WeightsF32& w32, const Pack& p, int mode, cudaStream_t s) const;
+    // Picks the schedule for p's row count (timing the candidates on p's own
+    // workspace) unless it is known or autotuning is off. Never call while
+    // `s` is capturing a graph.
+    void tune(const Dims& d, const WeightsF32& w32, const Pack& p, cudaStream_t s) const;
+    Tuning tuning_for(int rows) const;
 
     // Weights in the tensor-core operand layout ([block][K/8][rows][8] bf16).
-    const __nv_bfloat16 *wqkv[kMaxLayers], *wp[kMaxLayers], *w1[kMaxLayers], *w2[kMaxLayers];
+    const __nv_bfloat16 *wqkv[kMaxLayers], *wp[kMaxLayers];
+    // the MLP weights arranged for each chunk width: [0] nc 64, [1] nc 128
+    const __nv_bfloat16 *w1v[2][kMaxLayers], *w2v[2][kMaxLayers];
+    int n_nc = 1;
     const __nv_bfloat16 *wtm, *wtc, *wc1;
-    int nc_mlp;  // MLP chunk width (columns of ff1 per step)
+    int nc_mlp;  // default MLP chunk width (columns of ff1 per step)
     int bn_qkv;  // N block of the q/k/v GEMM
     int bn_tm;   // N block of the token_mix convolution
+
+   private:
+    mutable std::mutex tune_mu_;
+    mutable std::map<int, Tuning> tuned_;  // row-count bucket -> schedule
+    std::string cache_key_;
+    void load_cache();
+    void save_cache(int bucket, const Tuning& t) const;
 };
 
 }  // namespace jc

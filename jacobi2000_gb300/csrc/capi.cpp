@@ -5,6 +5,7 @@
 #include <string>
 
 #include "../../include/jacobi2000.h"
+#include "bf16_path.hpp"
 #include "runtime.hpp"
 
 namespace {
@@ -234,6 +235,12 @@ void jc_project_energy(float* x, double prev_energy, const jc_config* c, int64_t
 }
 
 const char* jc_last_error(void) { return g_last_error.c_str(); }
+
+int32_t jc_autotune(int32_t enable) {
+    const int prev = jc::g_autotune.load();
+    if (enable >= 0) jc::g_autotune.store(enable ? 1 : 0);
+    return prev;
+}
 
 const char* jc_version(void) { return "jacobi2000-gb300 0.1 (sm_103a)"; }
 

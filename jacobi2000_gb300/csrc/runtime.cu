@@ -504,6 +504,7 @@ void Model::forward_host(const float* state, const float* meta, float* inc) {
     cuda_check(cudaMemcpyAsync(d_state, hs, state_len * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
     cuda_check(cudaMemcpyAsync(d_meta, hm, cfg.meta_dim * 4, cudaMemcpyHostToDevice, stream), "H2D", JC_MAP);
     put_instance(d_state, d_inc, d_meta, 0, stream);
+    if (w.bf16) w.bf16->tune(dims, w.f32, pack_, stream);
     forward_pack(pack_, kWriteIncrement, stream);
     cuda_check(cudaMemcpyAsync(ho, d_inc, state_len * 4, cudaMemcpyDeviceToHost, stream), "D2H", JC_MAP);
     cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize", JC_POLL);
@@ -536,6 +537,7 @@ void Model::enqueue_rollout(int ticks, double* e, float* traj, cudaStream_t s) {
 cudaGraphExec_t Model::graph_for(const GraphKey& key, double* e, float* traj) {
     auto it = graphs_.find(key);
     if (it != graphs_.end()) return it->second;
+    if (w.bf16) w.bf16->tune(dims, w.f32, pack_, key.s);
     cudaGraph_t g;
     cuda_check(cudaStreamBeginCapture(key.s, cudaStreamCaptureModeThreadLocal), "begin capture");
     try {
@@ -562,7 +564,7 @@ void Model::rollout_device(const float* d_x0, const float* d_meta_in, int ticks,
     cuda_check(cudaMemcpyAsync(ws_.states, d_x0, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy x0");
     cuda_check(cudaMemcpyAsync(ws_.metas, d_meta_in, cfg.meta_dim * 4, cudaMemcpyDeviceToDevice, s), "copy meta");
     put_instance(ws_.states, ws_.states, ws_.metas, flags, s);
-    cuda_check(cudaGraphLaunch(graph_for(GraphKey{ticks, d_energies_out, nullptr, s}, d_energies_out, nullptr), s),
+    cuda_check(cudaGraphLaunch(graph_for(GraphKey{ticks, d_energies_out, nullptr, s, g_autotune.load()}, d_energies_out, nullptr), s),
                "graph launch");
     if (d_final)
         cuda_check(cudaMemcpyAsync(d_final, ws_.states, state_len * 4, cudaMemcpyDeviceToDevice, s), "copy final");
@@ -588,7 +590,7 @@ void Model::rollout_host(const float* x0, const float* meta, int ticks, uint32_t
     put_instance(ws_.states, ws_.states, ws_.metas, flags, stream);
     float* d_traj = traj ? arena.alloc_n<float>((size_t)(ticks + 1) * state_len) : nullptr;
     double* e = energies ? d_energies_ : nullptr;
-    GraphKey key{ticks, e, d_traj, stream};
+    GraphKey key{ticks, e, d_traj, stream, g_autotune.load()};
     try {
         cuda_check(cudaGraphLaunch(graph_for(key, e, d_traj), stream), "graph launch");
         cuda_check(cudaMemcpyAsync(ho, ws_.states, state_len * 4, cudaMemcpyDeviceToHost, stream), "D2H", JC_MAP);
@@ -626,6 +628,7 @@ void Model::forward_device(const float* d_state_in, const float* d_meta_in, floa
     if (!d_state_in || !d_meta_in || !d_inc_out) throw Error(JC_BAD_ARGUMENT, "null buffer");
     if (!s) s = stream;
     put_instance(const_cast<float*>(d_state_in), d_inc_out, d_meta_in, 0, s);
+    if (w.bf16) w.bf16->tune(dims, w.f32, pack_, s);
     forward_pack(pack_, kWriteIncrement, s);
 }
 
@@ -1059,6 +1062,7 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
     prepare_maps(p, s);
     std::vector<long long> key;
     key.push_back((long long)(uintptr_t)s);
+    key.push_back(g_autotune.load());
     for (const auto& r : p.recons) {
         key.push_back(-1000000 - r.H);
         key.push_back(((long long)r.nx << 20) | r.ny);
@@ -1178,12 +1182,14 @@ void Batch::prepare_maps(const Plan& p, cudaStream_t s) const {
         Pack v = ws_.view(dims_, G.inst_base, G.n, G.row_base, G.rows.back(), G.cell_base, G.cells.back(),
                           G.tiles.back(), G.ttiles.back(), G.ctiles.back());
         m0.w.bf16->prepare(dims_, v, p.inst.data() + G.inst_base, s);
+        m0.w.bf16->tune(dims_, m0.w.f32, v, s);
     }
     for (const auto& G : p.sgroups) {
         if (G.n == 0) continue;
         Pack v = ws_.view(dims_, G.inst_base, G.n, 0, G.rows.back(), 0, G.cells.back(), G.tiles.back(),
                           G.ttiles.back(), G.ctiles.back());
         m0.w.bf16->prepare(dims_, v, p.inst.data() + G.inst_base, s);
+        m0.w.bf16->tune(dims_, m0.w.f32, v, s);
     }
 }
 

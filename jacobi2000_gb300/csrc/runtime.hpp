@@ -122,7 +122,9 @@ class Model {
         const void* e;
         const void* t;
         cudaStream_t s;
+        int tune;  // autotuning switch at capture time
         bool operator<(const GraphKey& o) const {
+            if (tune != o.tune) return tune < o.tune;
             if (ticks != o.ticks) return ticks < o.ticks;
             if (e != o.e) return e < o.e;
             if (t != o.t) return t < o.t;

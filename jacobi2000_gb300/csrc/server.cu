@@ -522,8 +522,14 @@ void Server::iteration(std::vector<Request*>& act) {
     pr.max_inst_cells = rmax;
     const BF16Path* bf = fwd_[0]->w.bf16.get();
     if (bf) {
-        if (!fg.empty()) bf->prepare(dims_, pf, h_inst_ + fi, s);
-        if (!rg.empty()) bf->prepare(dims_, pr, h_inst_ + ri, s);
+        if (!fg.empty()) {
+            bf->prepare(dims_, pf, h_inst_ + fi, s);
+            bf->tune(dims_, fwd_[0]->w.f32, pf, s);
+        }
+        if (!rg.empty()) {
+            bf->prepare(dims_, pr, h_inst_ + ri, s);
+            rev_[0]->w.bf16->tune(dims_, rev_[0]->w.f32, pr, s);
+        }
     }
     if (!init.empty()) {
         Pack pi = ws_.view(dims_, 0, (int)init.size(), 0, ir, 0, ic, it_, itt, ict);

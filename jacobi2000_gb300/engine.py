@@ -44,7 +44,7 @@ class JcConfig(C.Structure):
 # Every symbol include/jacobi2000.h declares.
 EXPORTED = ["jc_model_create", "jc_model_destroy", "jc_model_config", "jc_meta_of", "jc_forward", "jc_step",
             "jc_rollout", "jc_forward_device", "jc_rollout_device", "jc_mass", "jc_energy", "jc_project_mass",
-            "jc_project_energy", "jc_last_error", "jc_version"]
+            "jc_project_energy", "jc_last_error", "jc_version", "jc_autotune"]
 
 _lib = None
 
@@ -194,6 +194,14 @@ def project_energy(x, prev_energy: float, config: JcConfig, cells: int) -> np.nd
     y = np.array(x, dtype=np.float32, copy=True)
     load_library().jc_project_energy(y.reshape(-1), float(prev_energy), C.byref(config), int(cells))
     return y
+
+
+def autotune(enable: bool | None = None) -> bool:
+    """Turns the BF16 schedule autotuner on or off (None: query only);
+    returns the previous setting."""
+    L = load_library()
+    L.jc_autotune.argtypes = [C.c_int32]
+    return bool(L.jc_autotune(-1 if enable is None else int(bool(enable))))
 
 
 class JcInstance(C.Structure):
