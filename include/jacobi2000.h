@@ -268,7 +268,8 @@ void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int
  * only queries. Returns the setting before the call. If JC_AUTOTUNE_CACHE
  * names a file, tuned schedules are appended to it and read back by models
  * created later. Results are identical under every schedule: the candidates
- * differ in tiling, not in arithmetic order of any sum. */
+ * differ in tiling, not in the order of any sum, so an instance's result does
+ * not depend on the batch it runs in. */
 int32_t jc_autotune(int32_t enable);
 
 /* Thread-local description of the last failure on this thread ("" if none). */

@@ -119,93 +119,117 @@ constexpr int kHaloPlane = (kHaloW * kHaloH * 16 + 127) / 128 * 128;
 __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 
 // Token embedding and the first LayerNorm (cpu.rs:253-280, 289). One CTA per
-// 64 token rows: the embed weights and the 64 patches are staged in shared
-// memory (patches gathered x-contiguously from the state), then one warp per
-// token computes its D outputs (lane handles o = lane + 32 j), adds pos and
-// the meta linear, writes x (f32) and LayerNorm(x) (bf16).
+// 64 token rows: the embed weights [pd][D] and the 64 patches (transposed,
+// [pd][64], gathered from the state) are staged in shared memory by
+// asynchronous copies, all in flight at once. Warp w
+// owns rows 8w..8w+7 and lane l owns the CPL = D/32 consecutive outputs
+// [CPL l, CPL l + CPL): per patch element it reads 8 patch values and CPL
+// weights once and does 8 x CPL FMAs. Each output is summed in the
+// reference's order (bias, then the patch elements in order, then + pos,
+// + the meta linear); x is written f32 and LayerNorm(x) bf16.
 constexpr int kEmbedRows = 64;
 
-template <int DPL>
+template <int CPL>
 __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __restrict__ We,
                                                        const float* __restrict__ be, const float* __restrict__ Wm,
                                                        const float* __restrict__ bm, const float* __restrict__ g,
                                                        const float* __restrict__ b, const InstDev* inst, int n_inst,
                                                        int R, float* __restrict__ x, bf16* __restrict__ ln) {
-    extern __shared__ float esm[];
-    const int D = d.D, P = d.P, pd = d.C * P * P;
-    float* sW = esm;                 // [pd][D]
-    float* sP = esm + (size_t)pd * D;  // [kEmbedRows][pd]
+    extern __shared__ __align__(16) float esm[];
+    constexpr int D = 32 * CPL;
+    const int P = d.P, pd = d.C * P * P;
+    float* sW = esm;                   // [pd][D]
+    float* sP = esm + (size_t)pd * D;  // [pd][kEmbedRows]
     __shared__ int rinst[kEmbedRows];
+    __shared__ const float* rbase[kEmbedRows];  // the row's patch origin in its state (channel 0)
+    __shared__ int rpitch[kEmbedRows];          // the state's row pitch (nx)
+    __shared__ long long rplane[kEmbedRows];    // the state's channel plane (nx * ny)
     const int r0 = blockIdx.x * kEmbedRows;
-    for (int i = threadIdx.x; i < pd * D; i += blockDim.x) sW[i] = We[i];
-    if (threadIdx.x < kEmbedRows)
-        rinst[threadIdx.x] = r0 + (int)threadIdx.x < R ? inst_of_row(inst, n_inst, r0 + threadIdx.x) : -1;
-    __syncthreads();
-    for (int e = threadIdx.x; e < kEmbedRows * pd; e += blockDim.x) {
-        const int px = e % P, i = (e / P) % kEmbedRows, cpy = e / (P * kEmbedRows);
-        const int c = cpy / P, py = cpy % P;
-        float v = 0.f;
-        if (rinst[i] >= 0) {
-            const InstDev& I = inst[rinst[i]];
-            const int t = r0 + i - I.row0;
-            const int y = (t / I.tx) * P + py, xx = (t % I.tx) * P + px;
-            v = I.state[((size_t)c * I.ny + y) * I.nx + xx];
+    for (int i = threadIdx.x; i < pd * D / 4; i += blockDim.x)
+        cp_async16(reinterpret_cast<float4*>(sW) + i, reinterpret_cast<const float4*>(We) + i, true);
+    if (threadIdx.x < kEmbedRows) {
+        const int r = r0 + (int)threadIdx.x;
+        const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
+        rinst[threadIdx.x] = ii;
+        if (ii >= 0) {
+            const InstDev& I = inst[ii];
+            const int t = r - I.row0;
+            rbase[threadIdx.x] = I.state + (size_t)(t / I.tx) * P * I.nx + (size_t)(t % I.tx) * P;
+            rpitch[threadIdx.x] = I.nx;
+            rplane[threadIdx.x] = (long long)I.nx * I.ny;
         }
-        sP[i * pd + c * P * P + py * P + px] = v;
     }
     __syncthreads();
+    for (int e = threadIdx.x; e < kEmbedRows * pd; e += blockDim.x) {
+        const int i = e % kEmbedRows, f = e / kEmbedRows;
+        const int c = f / (P * P), py = (f / P) % P, px = f % P;
+        const bool in = rinst[i] >= 0;
+        const float* src = in ? rbase[i] + c * rplane[i] + (size_t)py * rpitch[i] + px : We;
+        cp_async4(sP + f * kEmbedRows + i, src, in);
+    }
+    cp_async_wait_all();
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = warp; i < kEmbedRows; i += (int)(blockDim.x >> 5)) {
-        const int r = r0 + i;
-        if (r >= R) break;
-        const InstDev& I = inst[rinst[i]];
-        const int t = r - I.row0;
-        float v[DPL];
+    const int i0 = warp * 8;  // this warp's 8 rows
+    if (r0 + i0 >= R) return;
+    const int o0 = CPL * lane;
+    float v[8][CPL];
 #pragma unroll
-        for (int j = 0; j < DPL; j++) {
-            const int o = lane + 32 * j;
-            v[j] = o < D ? be[o] : 0.f;
-        }
-        const float* pp = sP + i * pd;
-        for (int f = 0; f < pd; f++) {
-            const float pv = pp[f];
+    for (int k = 0; k < 8; k++)
 #pragma unroll
-            for (int j = 0; j < DPL; j++) {
-                const int o = lane + 32 * j;
-                if (o < D) v[j] = fmaf(pv, sW[f * D + o], v[j]);
+        for (int c = 0; c < CPL; c++) v[k][c] = be[o0 + c];
+    for (int f = 0; f < pd; f++) {
+        const float4 p0 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0);
+        const float4 p1 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0 + 4);
+        const float pv[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+        float wv[CPL];
+        if (CPL % 4 == 0) {
+#pragma unroll
+            for (int c = 0; c < CPL; c += 4) {
+                const float4 w4 = *reinterpret_cast<const float4*>(sW + f * D + o0 + c);
+                wv[c] = w4.x; wv[c + 1] = w4.y; wv[c + 2] = w4.z; wv[c + 3] = w4.w;
             }
+        } else {
+#pragma unroll
+            for (int c = 0; c < CPL; c++) wv[c] = sW[f * D + o0 + c];
         }
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+#pragma unroll
+            for (int c = 0; c < CPL; c++) v[k][c] = fmaf(pv[k], wv[c], v[k][c]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int r = r0 + i0 + k;
+        if (r >= R) continue;  // warp-uniform
+        const InstDev& I = inst[rinst[i0 + k]];
+        const int t = r - I.row0;
         float sum = 0.f;
 #pragma unroll
-        for (int j = 0; j < DPL; j++) {
-            const int o = lane + 32 * j;
-            if (o < D) {
-                float m = bm[o];
-                for (int f = 0; f < d.meta_dim; f++) m = fmaf(I.meta[f], Wm[(size_t)f * D + o], m);
-                v[j] = (v[j] + I.pos[(size_t)t * D + o]) + m;
-                x[(size_t)r * D + o] = v[j];
-                sum += v[j];
-            }
+        for (int c = 0; c < CPL; c++) {
+            const int o = o0 + c;
+            float m = bm[o];
+            for (int f = 0; f < d.meta_dim; f++) m = fmaf(I.meta[f], Wm[(size_t)f * D + o], m);
+            v[k][c] = (v[k][c] + I.pos[(size_t)t * D + o]) + m;
+            sum += v[k][c];
         }
         const float mean = warp_sum(sum) / (float)D;
         float q = 0.f;
 #pragma unroll
-        for (int j = 0; j < DPL; j++)
-            if (lane + 32 * j < D) q += (v[j] - mean) * (v[j] - mean);
+        for (int c = 0; c < CPL; c++) q += (v[k][c] - mean) * (v[k][c] - mean);
         const float rstd = 1.0f / sqrtf(warp_sum(q) / (float)D + 1e-5f);
+        float o[CPL];
 #pragma unroll
-        for (int j = 0; j < DPL; j++) {
-            const int o = lane + 32 * j;
-            if (o < D) ln[(size_t)r * D + o] = __float2bfloat16((v[j] - mean) * rstd * g[o] + b[o]);
+        for (int c = 0; c < CPL; c++) {
+            x[(size_t)r * D + o0 + c] = v[k][c];
+            o[c] = (v[k][c] - mean) * rstd * g[o0 + c] + b[o0 + c];
         }
+#pragma unroll
+        for (int c = 0; c < CPL; c++) ln[(size_t)r * D + o0 + c] = __float2bfloat16(o[c]);
     }
 }
 
-// Stencil-masked attention on bf16 q/k/v (cpu.rs:97-164, mask.rs:18-30).
-// One warp per query token, all heads at once: lane l holds features
-// [FPL l, FPL l + FPL) and heads occupy 32/heads consecutive lanes. Scores are
-// reduced within a head's lanes; softmax is the online (running max) form in
-// f32 over the candidates in increasing key index.
+// Packed bf16 vectors of 1, 4 or 8 elements <-> f32.
 template <int FPL>
 struct BfVec;
 template <>
@@ -253,145 +277,152 @@ struct BfVec<8> {
     }
 };
 
-template <int FPL>
-__global__ void __launch_bounds__(256) bf_attention_kernel(Dims d, const bf16* __restrict__ qkv, const InstDev* inst,
-                                                           int n_inst, int R, bf16* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// One thread per (token row, head): the head's query stays in registers and
+// every dot product and weighted sum runs serially in the thread, so no
+// shuffles are needed; the threads of one row read the key and value rows of
+// a candidate as consecutive 16-byte pieces. Radius-1 stencil (any dilation):
+// scores, max, exp, denominator and the (e / denom)-weighted sum in the
+// reference's order (cpu.rs:121-158); a general stencil or the full mask uses
+// the online (running max) form.
+template <int HD>
+__device__ __forceinline__ void load_head(const bf16* p, float* f) {
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const uint4 u = reinterpret_cast<const uint4*>(p)[w];
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            f[8 * w + 2 * i] = __uint_as_float(a[i] << 16);
+            f[8 * w + 2 * i + 1] = __uint_as_float(a[i] & 0xffff0000u);
+        }
+    }
+}
+
+template <int HD>
+__device__ __forceinline__ float dot_head(const float* q, const bf16* kp) {
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const uint4 u = reinterpret_cast<const uint4*>(kp)[w];
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            p0 = fmaf(q[8 * w + 2 * i], __uint_as_float(a[i] << 16), p0);
+            p1 = fmaf(q[8 * w + 2 * i + 1], __uint_as_float(a[i] & 0xffff0000u), p1);
+        }
+    }
+    return p0 + p1;
+}
+
+template <int HD>
+__device__ __forceinline__ void axpy_head(float wgt, const bf16* vp, float* acc) {
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const uint4 u = reinterpret_cast<const uint4*>(vp)[w];
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            acc[8 * w + 2 * i] = fmaf(wgt, __uint_as_float(a[i] << 16), acc[8 * w + 2 * i]);
+            acc[8 * w + 2 * i + 1] = fmaf(wgt, __uint_as_float(a[i] & 0xffff0000u), acc[8 * w + 2 * i + 1]);
+        }
+    }
+}
+
+template <int HD>
+__device__ __forceinline__ void store_head(bf16* p, const float* acc) {
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) BfVec<8>::store(p + 8 * w, acc + 8 * w);
+}
+
+template <int HD>
+__global__ void __launch_bounds__(256) bf_attn_head_r1_kernel(Dims d, const bf16* __restrict__ qkv,
+                                                              const InstDev* inst, int n_inst, int R,
+                                                              bf16* __restrict__ out) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = gid / d.heads, h = gid - r * d.heads;
     if (r >= R) return;
-    const int D = d.D, D3 = 3 * D;
-    const int lph = 32 / d.heads;  // lanes per head
+    const int D = d.D;
+    const size_t D3 = 3 * (size_t)D;
     const InstDev& I = inst[inst_of_row(inst, n_inst, r)];
-    const int t = r - I.row0, qy = t / I.tx, qx = t % I.tx;
-    const float scale = 1.0f / sqrtf((float)(D / d.heads));
-    float q[FPL];
-    BfVec<FPL>::load(qkv + (size_t)r * D3 + lane * FPL, q);
+    const int t = r - I.row0, qy = t / I.tx, qx = t - qy * I.tx, dil = d.dilation;
+    const float scale = 1.0f / sqrtf((float)HD);
+    float q[HD];
+    load_head<HD>(qkv + (size_t)r * D3 + h * HD, q);
+    float sc[9];
+    int kr[9];
+    float smax = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int ky = qy + (j / 3 - 1) * dil, kx = qx + (j % 3 - 1) * dil;
+        const bool in = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
+        kr[j] = in ? I.row0 + ky * I.tx + kx : -1;
+        sc[j] = in ? dot_head<HD>(q, qkv + (size_t)kr[j] * D3 + D + h * HD) * scale : -INFINITY;
+        smax = fmaxf(smax, sc[j]);
+    }
+    float denom = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        sc[j] = kr[j] >= 0 ? __expf(sc[j] - smax) : 0.f;
+        denom += sc[j];
+    }
+    const float inv = 1.0f / denom;
+    float acc[HD];
+#pragma unroll
+    for (int i = 0; i < HD; i++) acc[i] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++)
+        if (kr[j] >= 0) axpy_head<HD>(sc[j] * inv, qkv + (size_t)kr[j] * D3 + 2 * D + h * HD, acc);
+    store_head<HD>(out + (size_t)r * D + h * HD, acc);
+}
+
+template <int HD>
+__global__ void __launch_bounds__(256) bf_attn_head_kernel(Dims d, const bf16* __restrict__ qkv, const InstDev* inst,
+                                                           int n_inst, int R, bf16* __restrict__ out) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = gid / d.heads, h = gid - r * d.heads;
+    if (r >= R) return;
+    const int D = d.D;
+    const size_t D3 = 3 * (size_t)D;
+    const InstDev& I = inst[inst_of_row(inst, n_inst, r)];
+    const int t = r - I.row0, qy = t / I.tx, qx = t - qy * I.tx;
+    const float scale = 1.0f / sqrtf((float)HD);
+    float q[HD], acc[HD];
+    load_head<HD>(qkv + (size_t)r * D3 + h * HD, q);
+#pragma unroll
+    for (int i = 0; i < HD; i++) acc[i] = 0.f;
     const int side = 2 * d.radius + 1;
     const int nc = d.mask_kind == 0 ? I.tx * I.ty : side * side;
-    float m = -INFINITY, l = 0.f, acc[FPL];
-#pragma unroll
-    for (int i = 0; i < FPL; i++) acc[i] = 0.f;
+    float m = -INFINITY, l = 0.f;
     for (int j = 0; j < nc; j++) {
         int kr;
         if (d.mask_kind == 0) {
             kr = I.row0 + j;
         } else {
-            int ky = qy + (j / side - d.radius) * d.dilation, kx = qx + (j % side - d.radius) * d.dilation;
+            const int ky = qy + (j / side - d.radius) * d.dilation, kx = qx + (j % side - d.radius) * d.dilation;
             if (ky < 0 || kx < 0 || ky >= I.ty || kx >= I.tx) continue;
             kr = I.row0 + ky * I.tx + kx;
         }
-        float k[FPL], v[FPL];
-        BfVec<FPL>::load(qkv + (size_t)kr * D3 + D + lane * FPL, k);
-        BfVec<FPL>::load(qkv + (size_t)kr * D3 + 2 * D + lane * FPL, v);
-        float p = 0.f;
-#pragma unroll
-        for (int i = 0; i < FPL; i++) p = fmaf(q[i], k[i], p);
-        for (int o = 1; o < lph; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        const float s = p * scale;
+        const float s = dot_head<HD>(q, qkv + (size_t)kr * D3 + D + h * HD) * scale;
         const float mn = fmaxf(m, s);
         const float c = __expf(m - mn), e = __expf(s - mn);
         l = l * c + e;
 #pragma unroll
-        for (int i = 0; i < FPL; i++) acc[i] = acc[i] * c + e * v[i];
+        for (int i = 0; i < HD; i++) acc[i] *= c;
+        axpy_head<HD>(e, qkv + (size_t)kr * D3 + 2 * D + h * HD, acc);
         m = mn;
     }
     const float inv = 1.0f / l;
 #pragma unroll
-    for (int i = 0; i < FPL; i++) acc[i] *= inv;
-    BfVec<FPL>::store(out + (size_t)r * D + lane * FPL, acc);
-}
-
-// Radius-1 stencil (3 x 3 candidates, any dilation), unrolled: the nine key
-// and value vectors are loaded up front as packed bf16 words, then scores,
-// max, exp, denominator and the (e / denom)-weighted sum follow the
-// reference's order (cpu.rs:121-158).
-template <int FPL>
-__global__ void __launch_bounds__(256) bf_attention_r1_kernel(Dims d, const bf16* __restrict__ qkv,
-                                                              const InstDev* inst, int n_inst, int R,
-                                                              bf16* __restrict__ out) {
-    constexpr int W = FPL / 2 > 0 ? FPL / 2 : 1;  // 32-bit words per lane per vector
-    const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (r >= R) return;
-    const int D = d.D, D3 = 3 * D;
-    const int lph = 32 / d.heads;
-    const InstDev& I = inst[inst_of_row(inst, n_inst, r)];
-    const int t = r - I.row0, qy = t / I.tx, qx = t % I.tx, dil = d.dilation;
-    const float scale = 1.0f / sqrtf((float)(D / d.heads));
-    float q[FPL];
-    BfVec<FPL>::load(qkv + (size_t)r * D3 + lane * FPL, q);
-    uint32_t kw[9][W], vw[9][W];
-    bool in[9];
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        const int ky = qy + (j / 3 - 1) * dil, kx = qx + (j % 3 - 1) * dil;
-        in[j] = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
-        const size_t kr = in[j] ? (size_t)(I.row0 + ky * I.tx + kx) : (size_t)r;
-        const bf16* kp = qkv + kr * D3 + D + lane * FPL;
-        const bf16* vp = kp + D;
-        if (FPL == 1) {
-            kw[j][0] = *reinterpret_cast<const uint16_t*>(kp);
-            vw[j][0] = *reinterpret_cast<const uint16_t*>(vp);
-        } else if (FPL == 4) {
-            const uint2 a = *reinterpret_cast<const uint2*>(kp), b = *reinterpret_cast<const uint2*>(vp);
-            kw[j][0] = a.x; kw[j][W > 1 ? 1 : 0] = a.y;
-            vw[j][0] = b.x; vw[j][W > 1 ? 1 : 0] = b.y;
-        } else {
-            const uint4 a = *reinterpret_cast<const uint4*>(kp), b = *reinterpret_cast<const uint4*>(vp);
-            const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-            for (int i = 0; i < W; i++) { kw[j][i] = aw[i]; vw[j][i] = bw[i]; }
-        }
-    }
-    auto unpack = [&](const uint32_t* w, float* f) {
-        if (FPL == 1) {
-            f[0] = __uint_as_float(w[0] << 16);
-        } else {
-#pragma unroll
-            for (int i = 0; i < W; i++) {
-                f[2 * i] = __uint_as_float(w[i] << 16);
-                f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-            }
-        }
-    };
-    float sc[9];
-    float smax = -INFINITY;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        float k[FPL];
-        unpack(kw[j], k);
-        float p = 0.f;
-#pragma unroll
-        for (int i = 0; i < FPL; i++) p = fmaf(q[i], k[i], p);
-        for (int o = 1; o < lph; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        sc[j] = p * scale;
-        if (in[j]) smax = fmaxf(smax, sc[j]);
-    }
-    float denom = 0.f;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        sc[j] = in[j] ? __expf(sc[j] - smax) : 0.f;
-        denom += sc[j];
-    }
-    const float inv = 1.0f / denom;
-    float acc[FPL];
-#pragma unroll
-    for (int i = 0; i < FPL; i++) acc[i] = 0.f;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        float v[FPL];
-        unpack(vw[j], v);
-        const float wn = sc[j] * inv;
-#pragma unroll
-        for (int i = 0; i < FPL; i++) acc[i] = fmaf(wn, v[i], acc[i]);
-    }
-    BfVec<FPL>::store(out + (size_t)r * D + lane * FPL, acc);
+    for (int i = 0; i < HD; i++) acc[i] *= inv;
+    store_head<HD>(out + (size_t)r * D + h * HD, acc);
 }
 
 // z0 (f32 [rows, HD]) -> zc (bf16 [cells, 48]): upsample along y then x
 // (cpu.rs:211-245), state channels appended (cpu.rs:339-342), zero padding.
+template <int HD, int C>
 __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst, int n_inst,
                                    long long NC, bf16* __restrict__ zc) {
+    static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh, "zc layout");
     long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= NC) return;
     const InstDev& I = inst[inst_of_cell(inst, n_inst, cell)];
@@ -400,15 +431,16 @@ __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const I
     int yt = y / d.P, iy = y % d.P, xt = x / d.P, ix = x % d.P;
     int yt2 = min(yt + 1, I.ty - 1), xt2 = min(xt + 1, I.tx - 1);
     float wy = ((float)iy + 0.5f) / (float)d.P, wx = ((float)ix + 0.5f) / (float)d.P;
-    const float4* a = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt) * d.HD);
-    const float4* b = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt2) * d.HD);
-    const float4* c = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt) * d.HD);
-    const float4* e = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt2) * d.HD);
+    const float4* a = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt) * HD);
+    const float4* b = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt2) * HD);
+    const float4* c = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt) * HD);
+    const float4* e = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt2) * HD);
     const float uy = 1.0f - wy, ux = 1.0f - wx;
     float vals[kZcCh];
 #pragma unroll
     for (int i = 0; i < kZcCh; i++) vals[i] = 0.f;
-    for (int q = 0; q < d.HD / 4; q++) {
+#pragma unroll
+    for (int q = 0; q < HD / 4; q++) {
         float4 A = a[q], B = b[q], Cc = c[q], E = e[q];
         vals[4 * q + 0] = (A.x * uy + Cc.x * wy) * ux + (B.x * uy + E.x * wy) * wx;
         vals[4 * q + 1] = (A.y * uy + Cc.y * wy) * ux + (B.y * uy + E.y * wy) * wx;
@@ -416,7 +448,8 @@ __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const I
         vals[4 * q + 3] = (A.w * uy + Cc.w * wy) * ux + (B.w * uy + E.w * wy) * wx;
     }
     const size_t plane = (size_t)I.nx * I.ny;
-    for (int ch = 0; ch < d.C; ch++) {
+#pragma unroll
+    for (int ch = 0; ch < C; ch++) {
         const float sv = I.state[ch * plane + cl];
         const float hi = bf2f(__float2bfloat16(sv));
         vals[kZcState + ch] = hi;
@@ -678,15 +711,215 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
 }
 
 // Fused MLP: x += gelu(LN2(x) @ W1 + b1) @ W2 + b2, then LayerNorm of the new
-// x (the next block's norm1, or the final norm) into `ln`. Per chunk of NC
-// hidden columns: S = A @ W1_chunk (TMEM), h = gelu(S + b1) written to
+// x (the next block's norm1, or the final norm) into `ln`. The hidden layer
+// is walked in chunks of NC columns: S_j = A @ W1_j (TMEM), h_j = gelu(S_j +
+// b1_j) as bf16 in shared memory, O += h_j @ W2_j (TMEM); the hidden
+// activations never leave the SM.
+//
+// Warp-specialised and pipelined: warp 8 (one elected lane) streams the
+// weight chunks through an NS-stage shared-memory ring and issues every MMA;
+// warps 0-7 (two per TMEM lane quarter, one half of the chunk's columns each)
+// turn S_j into h_j. S and h are double-buffered, so S_{j+1} / S_{j+2} and
+// O += h_{j-1} W2_{j-1} run on the tensor core while the GELU warps work on
+// chunk j. All nine warps run the residual + LayerNorm epilogue from a
+// shared-memory copy of O. Every summation order is fixed by NC-independent
+// K slices of 16, so every chunk width gives the same bits.
+constexpr int kMlpWarps = 8;                       // GELU / epilogue warps
+constexpr int kMlpThreads = (kMlpWarps + 1) * 32;  // + the producer / MMA warp
+
+struct MlpSmem {
+    int D, NC, NS;
+    size_t a, w, h, b1, total, tile;
+    __host__ __device__ MlpSmem(int D_, int F, int NC_, int NS_) : D(D_), NC(NC_), NS(NS_) {
+        a = 0;                                           // [D/8][128][8]
+        w = a + (size_t)D * 256;                         // NS x ([D/8][NC][8] W1 | [NC/8][D][8] W2)
+        h = w + (size_t)NS * 4 * D * NC;                 // 2 x [NC/8][128][8]
+        b1 = h + (size_t)2 * NC * 256;                   // [F] f32
+        total = b1 + (size_t)F * 4;
+        tile = (size_t)128 * D * 4;                      // epilogue: f32 [128][D]
+        if (tile > total) total = tile;
+    }
+};
+
+__global__ void __launch_bounds__(kMlpThreads, 2) tc_mlp_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                             const bf16* __restrict__ W1, const bf16* __restrict__ W2,
+                                                             const float* __restrict__ b1,
+                                                             const float* __restrict__ b2, int D, int F, int NC, int NS,
+                                                             int R, float* __restrict__ x, const float* __restrict__ g,
+                                                             const float* __restrict__ b, bf16* __restrict__ ln,
+                                                             int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const MlpSmem L(D, F, NC, NS);
+    uint8_t* sA = smem + L.a;
+    uint8_t* sW = smem + L.w;
+    uint8_t* sH = smem + L.h;
+    float* sb1 = reinterpret_cast<float*>(smem + L.b1);
+    constexpr int kMaxStages = 4;
+    __shared__ uint64_t bar_a, bar_o, bar_w[kMaxStages], bar_wfree[kMaxStages], bar_s[2], bar_h[2], bar_hfree[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * 128;
+    const int nch = F / NC;
+    const uint32_t s_col = (uint32_t)(D < 64 ? 64 : D);
+    uint32_t ncols = 32;
+    while (ncols < s_col + 2u * NC) ncols <<= 1;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar_a, 1);
+        tc::mbar_init(&bar_o, 1);
+        for (int i = 0; i < NS; i++) {
+            tc::mbar_init(&bar_w[i], 1);
+            tc::mbar_init(&bar_wfree[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(&bar_s[i], 1);
+            tc::mbar_init(&bar_h[i], kMlpWarps * 32);
+            tc::mbar_init(&bar_hfree[i], 1);
+        }
+        tc::fence_barrier_init();
+        failed = 0;
+        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
+    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tO = tmem_base;
+    const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
+    bool ok = !failed;
+    if (warp == kMlpWarps) {
+        if (lane == 0 && ok) {
+            // producer + MMA issuer
+            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH), w0 = tc::smem_u32(sW);
+            auto load_w = [&](int j) {
+                uint64_t* bar = &bar_w[j % NS];
+                uint8_t* dst = sW + (size_t)(j % NS) * 2 * wbytes;
+                tc::mbar_expect_tx(bar, 2 * wbytes);
+                tc::bulk_load(dst, W1 + (size_t)j * D * NC, wbytes, bar);
+                tc::bulk_load(dst + wbytes, W2 + (size_t)j * D * NC, wbytes, bar);
+            };
+            auto issue_s = [&](int j) -> bool {
+                if (!tc::mbar_wait(&bar_w[j % NS], (uint32_t)(j / NS) & 1u, err, &failed)) return false;
+                tc::tc_fence_after();
+                const uint32_t ws = w0 + (uint32_t)(j % NS) * 2 * wbytes;
+                const uint32_t idesc = tc::idesc_bf16(128, NC);
+                const uint32_t tS = tO + s_col + (uint32_t)(j & 1) * NC;
+                for (int k = 0; k < D / 16; k++)
+                    tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(ws + k * 2 * NC * 16, NC * 16, 128),
+                                 idesc, k > 0 ? 1u : 0u);
+                tc::mma_commit(&bar_s[j & 1]);
+                return true;
+            };
+            tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
+            for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &bar_a);
+            for (int j = 0; j < NS && j < nch; j++) load_w(j);
+            bool good = tc::mbar_wait(&bar_a, 0, err, &failed);
+            for (int j = 0; j < 2 && j < nch && good; j++) good = issue_s(j);
+            for (int j = 0; j < nch && good; j++) {
+                if (!tc::mbar_wait(&bar_h[j & 1], (uint32_t)(j >> 1) & 1u, err, &failed)) {
+                    good = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t ws2 = w0 + (uint32_t)(j % NS) * 2 * wbytes + wbytes;
+                const uint32_t hs = h0 + (uint32_t)(j & 1) * NC * 256;
+                const uint32_t idesc = tc::idesc_bf16(128, D);
+                for (int k = 0; k < NC / 16; k++)
+                    tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(ws2 + k * 2 * D * 16, D * 16, 128),
+                                 idesc, (j > 0 || k > 0) ? 1u : 0u);
+                tc::mma_commit(&bar_wfree[j % NS]);
+                tc::mma_commit(&bar_hfree[j & 1]);
+                // refill the stage O_j used with chunk j + NS once O_j is done;
+                // with two stages that chunk is the one S_{j+2} needs, so the
+                // refill comes first, otherwise S_{j+2} (loaded earlier) does
+                auto refill = [&]() -> bool {
+                    if (j + NS >= nch) return true;
+                    if (!tc::mbar_wait(&bar_wfree[j % NS], (uint32_t)(j / NS) & 1u, err, &failed)) return false;
+                    load_w(j + NS);
+                    return true;
+                };
+                if (NS == 2 && !refill()) {
+                    good = false;
+                    break;
+                }
+                if (j + 2 < nch && !issue_s(j + 2)) {
+                    good = false;
+                    break;
+                }
+                if (NS > 2 && !refill()) {
+                    good = false;
+                    break;
+                }
+            }
+            if (good) tc::mma_commit(&bar_o);
+        }
+        __syncwarp();
+    } else if (ok) {
+        // GELU warps: chunk j's S (TMEM) -> h_j (bf16, core-matrix layout)
+        const int quarter = warp & 3, half = warp >> 2;
+        const int r = quarter * 32 + lane;
+        const int cw = NC / 2;  // columns per warp half: 16 or 32
+        for (int j = 0; j < nch; j++) {
+            const bool s_ready = tc::mbar_wait(&bar_s[j & 1], (uint32_t)(j >> 1) & 1u, err, &failed);
+            const bool h_free = j < 2 || tc::mbar_wait(&bar_hfree[j & 1], (uint32_t)((j - 2) >> 1) & 1u, err, &failed);
+            // the TMEM load below is warp-collective: every lane runs it, and a
+            // failed wait anywhere ends the loop for the whole warp
+            if (!__all_sync(0xffffffffu, s_ready && h_free)) break;
+            tc::tc_fence_after();
+            const uint32_t ta = lane_addr(tO + s_col + (uint32_t)(j & 1) * NC);
+            uint8_t* hb = sH + (size_t)(j & 1) * NC * 256;
+            for (int c = half * cw; c < (half + 1) * cw; c += 16) {
+                float a[16];
+                tc::tmem_ld16(ta + c, a);
+                const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float4 bv = bb[i];
+                    a[4 * i] = gelu_fast(a[4 * i] + bv.x);
+                    a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
+                    a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
+                    a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
+                }
+                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
+                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
+            }
+            tc::fence_async_shared();
+            tc::tc_fence_before();
+            tc::mbar_arrive(&bar_h[j & 1]);
+        }
+    }
+    // all MMAs done (or a wait gave up)
+    bool done = true;
+    if (warp < kMlpWarps) done = tc::mbar_wait(&bar_o, 0, err, &failed);
+    ok = __syncthreads_and(ok && done && !failed) != 0;
+    tc::tc_fence_after();
+    if (ok) {
+        float* tile = reinterpret_cast<float*>(smem);
+        if (warp < kMlpWarps) {
+            const int quarter = warp & 3, half = warp >> 2;
+            stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
+        }
+        __syncthreads();
+        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpWarps + 1);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
+}
+
+// The same MLP as tc_mlp_kernel without warp specialisation: per chunk of NC
+// hidden columns, one after the other, S = A @ W1_chunk (TMEM), h = gelu(S + b1) written to
 // shared memory as bf16 by all 8 warps (two per TMEM lane quarter, one
 // column half each), O += h @ W2_chunk (TMEM). The hidden activations never
 // leave the SM. The residual + LayerNorm epilogue stages O through shared
 // memory and runs one warp per row.
-constexpr int kMlpThreads = 256;
+constexpr int kMlpSerialThreads = 256;
 
-__global__ void __launch_bounds__(kMlpThreads) tc_mlp_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const __grid_constant__ CUtensorMap tmA,
                                                              const bf16* __restrict__ W1, const bf16* __restrict__ W2,
                                                              const float* __restrict__ b1,
                                                              const float* __restrict__ b2, int D, int F, int NC, int R,
@@ -786,7 +1019,7 @@ __global__ void __launch_bounds__(kMlpThreads) tc_mlp_kernel(const __grid_consta
         float* tile = reinterpret_cast<float*>(smem);
         stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
         __syncthreads();
-        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpThreads / 32);
+        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpSerialThreads / 32);
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -958,15 +1191,20 @@ static void set_smem(K kernel, size_t bytes) {
 
 BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     const int D = d.D, F = d.F, HD = d.HD;
+    dims_D_ = D;
+    dims_F_ = F;
     if (D % 32 || D > 256 || 32 % d.heads || F % 64 || HD != 32 || d.C != 3 || d.P != 4 || d.C * d.P * d.P > 64)
         throw Error(JC_LIMIT,
                     "the BF16 path needs dim a multiple of 32 and <= 256, heads dividing 32, a cell-head width of 32, "
                     "3 channels and patch 4");
-    nc_mlp = 64;
-    n_nc = (D <= 128 && F % 128 == 0) ? 2 : 1;  // nc 128 needs 128 KB of shared memory at dim 128
+    n_nc = 2;  // MLP weights arranged for chunk widths 32 and 64
     bn_qkv = (3 * D) % 128 == 0 ? 128 : 3 * D;
     bn_tm = D <= 128 ? D : 64;
-    if (F % nc_mlp) throw Error(JC_LIMIT, "the MLP width must be a multiple of the MLP chunk");
+    if (F > 1024) throw Error(JC_LIMIT, "the BF16 MLP supports a hidden width of at most 1024");
+    def_tuning_ = Tuning{32, 3, 256};
+    if (!mlp_fits(32, 3)) def_tuning_.ns = 2;
+    if (!mlp_fits(def_tuning_.nc, def_tuning_.ns))
+        throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
     for (int l = 0; l < d.L; l++) {
         const std::string p = "blocks." + std::to_string(l) + ".";
         const auto &q = tget(t, p + "q.weight").data, &k = tget(t, p + "k.weight").data, &v = tget(t, p + "v.weight").data;
@@ -980,7 +1218,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
         const auto& w1h = tget(t, p + "ff1.weight").data;  // [D, F]
         const auto& w2h = tget(t, p + "ff2.weight").data;  // [F, D]
         for (int v = 0; v < n_nc; v++) {
-            const int nc = v == 0 ? 64 : 128;
+            const int nc = v == 0 ? 32 : 64;
             w1v[v][l] = upload_bf16(arena, blocked(F, D, nc, [&](int n, int kk) { return w1h[(size_t)kk * F + n]; }));
             // W2 chunk j: B2_j[n][k] = W2[j*nc + k][n] -> [j][nc/8][D][8]
             std::vector<uint16_t> w2b((size_t)F * D);
@@ -1047,32 +1285,39 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_gemm_kernel<EPI_BF16>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_F32>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
-    set_smem(tc_mlp_kernel, 200 * 1024);
+    set_smem(tc_mlp_kernel, kMlpSmemMax);
+    set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
     set_smem(bf_embed_kernel<1>, 100 * 1024);
+    set_smem(bf_embed_kernel<2>, 100 * 1024);
+    set_smem(bf_embed_kernel<3>, 100 * 1024);
     set_smem(bf_embed_kernel<4>, 100 * 1024);
+    set_smem(bf_embed_kernel<5>, 100 * 1024);
+    set_smem(bf_embed_kernel<6>, 100 * 1024);
+    set_smem(bf_embed_kernel<7>, 100 * 1024);
     set_smem(bf_embed_kernel<8>, 100 * 1024);
 }
 
+// One thread per (token row, head) in CTAs of `threads` threads (64, 128 or
+// 256; the arithmetic of a thread does not depend on it).
 static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
                              int threads, cudaStream_t s) {
-    const int wpb = threads / 32;
-    const unsigned blocks = (unsigned)((R + wpb - 1) / wpb);
-    const int fpl = d.D / 32;
     const bool r1 = d.mask_kind == 1 && d.radius == 1;
-    if (fpl == 1) {
-        if (r1) bf_attention_r1_kernel<1><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-        else bf_attention_kernel<1><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-    } else if (fpl == 4) {
-        if (r1) bf_attention_r1_kernel<4><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-        else bf_attention_kernel<4><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-    } else if (fpl == 8) {
-        if (r1) bf_attention_r1_kernel<8><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-        else bf_attention_kernel<8><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);
-    } else {
-        throw Error(JC_LIMIT, "the BF16 attention supports dim 32, 128 or 256");
+    const int hd = d.D / d.heads;
+    const unsigned blocks = (unsigned)(((long long)R * d.heads + threads - 1) / threads);
+#define JC_ATTN_HEAD(H)                                                                          \
+    if (hd == H) {                                                                               \
+        if (r1) bf_attn_head_r1_kernel<H><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn); \
+        else bf_attn_head_kernel<H><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);       \
+        return;                                                                                  \
     }
+    JC_ATTN_HEAD(8)
+    JC_ATTN_HEAD(16)
+    JC_ATTN_HEAD(32)
+    JC_ATTN_HEAD(64)
+#undef JC_ATTN_HEAD
+    throw Error(JC_LIMIT, "the BF16 attention supports head widths 8, 16, 32 and 64");
 }
 
 static int initial_autotune() {
@@ -1093,7 +1338,36 @@ Tuning BF16Path::tuning_for(int rows) const {
         auto it = tuned_.find(row_bucket(rows));
         if (it != tuned_.end()) return it->second;
     }
-    return Tuning{nc_mlp, 256};
+    return def_tuning_;
+}
+
+// Shared memory of the serial MLP kernel (one stage, one h buffer).
+static size_t mlp_serial_smem(int D, int NC) {
+    return std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
+}
+
+bool BF16Path::mlp_fits(int nc, int ns) const {
+    if (!(nc == 32 || nc == 64) || dims_F_ % nc) return false;
+    if (ns == 1) return mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
+    return ns >= 2 && ns <= 4 && MlpSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
+}
+
+void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln,
+                          const Pack& p, cudaStream_t s) const {
+    const int D = d.D, R = p.R;
+    const int v = tu.nc == 64 ? 1 : 0;
+    const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
+    const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
+    if (tu.ns == 1) {
+        tc_mlp_serial_kernel<<<(unsigned)((R + 127) / 128), kMlpSerialThreads, mlp_serial_smem(D, tu.nc), s>>>(
+            m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, R, p.x, ng, nbeta,
+            reinterpret_cast<bf16*>(p.bt[0]), p.err);
+        return;
+    }
+    const size_t smem = MlpSmem(D, d.F, tu.nc, tu.ns).total;
+    tc_mlp_kernel<<<(unsigned)((R + 127) / 128), kMlpThreads, smem, s>>>(
+        m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
+        reinterpret_cast<bf16*>(p.bt[0]), p.err);
 }
 
 // Times `launch` with CUDA events: one warm-up, then `reps` launches.
@@ -1128,28 +1402,30 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     bf16* qkv = reinterpret_cast<bf16*>(p.bt[1]);
     bf16* attn = reinterpret_cast<bf16*>(p.bt[2]);
     const CUtensorMap m_ln = rows_map(ln, D, R);
-    const unsigned gm = (unsigned)((R + 127) / 128);
-    Tuning best{nc_mlp, 256};
+    Tuning best = def_tuning_;
     // the workspace holds transient values; the timed launches may leave
     // anything in it (every forward rewrites it from the state)
+    std::string log;
     float best_ms = 1e30f;
-    for (int v = 0; v < n_nc; v++) {
-        const int NC = v == 0 ? 64 : 128;
-        const size_t smem = std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
-        const float ms = time_launches(
-            [&] {
-                tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1v[v][0], w2v[v][0], w.blk[0].b1, w.blk[0].b2, D,
-                                                            d.F, NC, R, p.x, w.norm_g, w.norm_b, ln, p.err);
-            },
-            3, s);
+    const int cand[][2] = {{32, 1}, {64, 1}, {32, 2}, {32, 3}, {32, 4}, {64, 2}, {64, 3}};
+    for (const auto& c : cand) {
+        if (!mlp_fits(c[0], c[1])) continue;
+        Tuning t = best;
+        t.nc = c[0];
+        t.ns = c[1];
+        const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, 3, s);
+        log += (log.empty() ? "" : ", ") + std::string("\"mlp_") + std::to_string(c[0]) + "x" + std::to_string(c[1]) +
+               "_ms\": " + std::to_string(ms);
         if (ms < best_ms) {
             best_ms = ms;
-            best.nc = NC;
+            best.nc = t.nc;
+            best.ns = t.ns;
         }
     }
     best_ms = 1e30f;
     for (int threads : {64, 128, 256}) {
         const float ms = time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s); }, 3, s);
+        log += ", \"attn_" + std::to_string(threads) + "_ms\": " + std::to_string(ms);
         if (ms < best_ms) {
             best_ms = ms;
             best.attn_threads = threads;
@@ -1160,15 +1436,15 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
         std::lock_guard<std::mutex> lk(tune_mu_);
         tuned_[bucket] = best;
     }
-    save_cache(bucket, best);
+    save_cache(bucket, best, log);
 }
 
 // Tuned schedules persist in the JSON-lines file named by JC_AUTOTUNE_CACHE,
 // one object per tuned row bucket:
-//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "nc": 64, "attn_threads": 128}
+//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "nc": 32, "stages": 3, "attn_threads": 256}
 // keyed by the model shape (dim, layers, MLP width, mask radius, kind and
-// dilation). Lines that do not parse or name another shape are skipped;
-// later lines override earlier ones.
+// dilation), followed by the candidates' measured times. Lines that do not
+// parse or name another shape are skipped; later lines override earlier ones.
 void BF16Path::load_cache() {
     const char* path = std::getenv("JC_AUTOTUNE_CACHE");
     if (!path) return;
@@ -1176,24 +1452,24 @@ void BF16Path::load_cache() {
     if (!f) return;
     char line[512], key[128];
     while (std::fgets(line, sizeof line, f)) {
-        int bucket, nc, th;
-        if (std::sscanf(line, " {\"model\": \"%127[^\"]\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d", key,
-                        &bucket, &nc, &th) != 4)
+        int bucket, nc, ns, th;
+        if (std::sscanf(line, " {\"model\": \"%127[^\"]\", \"rows\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": %d",
+                        key, &bucket, &nc, &ns, &th) != 5)
             continue;
-        if (cache_key_ == key && (nc == 64 || (nc == 128 && n_nc == 2)) && (th == 64 || th == 128 || th == 256))
-            tuned_[bucket] = Tuning{nc, th};
+        if (cache_key_ == key && mlp_fits(nc, ns) && (th == 64 || th == 128 || th == 256))
+            tuned_[bucket] = Tuning{nc, ns, th};
     }
     std::fclose(f);
 }
 
-void BF16Path::save_cache(int bucket, const Tuning& t) const {
+void BF16Path::save_cache(int bucket, const Tuning& t, const std::string& timings) const {
     const char* path = std::getenv("JC_AUTOTUNE_CACHE");
     if (!path) return;
     std::lock_guard<std::mutex> lk(tune_mu_);
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "{\"model\": \"%s\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d}\n", cache_key_.c_str(), bucket,
-                 t.nc, t.attn_threads);
+    std::fprintf(f, "{\"model\": \"%s\", \"rows\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": %d%s%s}\n",
+                 cache_key_.c_str(), bucket, t.nc, t.ns, t.attn_threads, timings.empty() ? "" : ", ", timings.c_str());
     std::fclose(f);
 }
 
@@ -1240,9 +1516,16 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         KScope k("bf_embed", s);
         const unsigned blocks = (unsigned)((R + kEmbedRows - 1) / kEmbedRows);
         const size_t smem = ((size_t)d.C * d.P * d.P * D + (size_t)kEmbedRows * d.C * d.P * d.P) * sizeof(float);
-        if (D <= 32) bf_embed_kernel<1><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
-        else if (D <= 128) bf_embed_kernel<4><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
-        else bf_embed_kernel<8><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);
+#define JC_EMBED(CPL)                                                                                           \
+    case CPL:                                                                                                   \
+        bf_embed_kernel<CPL><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, \
+                                                       w.blk[0].n1b, p.inst, n, R, p.x, ln);                     \
+        break;
+        switch (D / 32) {
+            JC_EMBED(1) JC_EMBED(2) JC_EMBED(3) JC_EMBED(4) JC_EMBED(5) JC_EMBED(6) JC_EMBED(7) JC_EMBED(8)
+            default: throw Error(JC_LIMIT, "the BF16 embed supports dim 32..256 in steps of 32");
+        }
+#undef JC_EMBED
         check_launch("bf_embed");
     }
     for (int l = 0; l < d.L; l++) {
@@ -1270,12 +1553,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         }
         {
             KScope k("tc_mlp", s);
-            const int NC = tu.nc, v = NC == 128 ? 1 : 0;
-            const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
-            const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
-            const size_t smem = std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
-            tc_mlp_kernel<<<gm, kMlpThreads, smem, s>>>(m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, NC, R, p.x, ng,
-                                                        nbeta, ln, p.err);
+            launch_mlp(d, w, l, tu, m_ln, p, s);
             check_launch("tc_mlp");
         }
     }
@@ -1297,7 +1575,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     const long long NC = p.NC;
     {
         KScope k("bf_upsample", s);
-        bf_upsample_kernel<<<(unsigned)((NC + 255) / 256), 256, 0, s>>>(d, p.z0, p.inst, n, NC, zc);
+        bf_upsample_kernel<32, 3><<<(unsigned)((NC + 255) / 256), 256, 0, s>>>(d, p.z0, p.inst, n, NC, zc);
         check_launch("bf_upsample");
     }
     {

@@ -3,6 +3,7 @@
 // statistics, softmax, the residual stream and the projection stay f32/f64.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <atomic>
@@ -14,15 +15,18 @@
 namespace jc {
 
 // A schedule the autotuner picks per (row-count bucket): the MLP's hidden
-// chunk width and the attention kernel's CTA size.
+// chunk width and the attention kernel's CTA size. Every schedule gives the
+// same bits: the candidates change tiling, never the order of a sum, so an
+// instance's result does not depend on the batch it runs in.
 struct Tuning {
-    int nc;            // 64 or 128 hidden columns per MLP step
-    int attn_threads;  // 64, 128 or 256
+    int nc;            // 32 or 64 hidden columns per MLP step
+    int ns;            // MLP weight-ring stages (2-4); 1 = the serial (unpipelined) MLP kernel
+    int attn_threads;  // 64, 128 or 256 threads per attention CTA
 };
 
 // 1 (default; environment JC_AUTOTUNE=0 turns it off): BF16 launches time the
 // candidate schedules once per row-count bucket and keep the fastest; 0: the
-// fixed default schedule {nc 64, 256 threads}.
+// fixed default schedule {nc 32, 3 stages, 256 threads}.
 extern std::atomic<int> g_autotune;
 
 class BF16Path {
@@ -44,19 +48,24 @@ class BF16Path {
     // Weights in the tensor-core operand layout ([block][K/8][rows][8] bf16).
     const __nv_bfloat16 *wqkv[kMaxLayers], *wp[kMaxLayers];
     // the MLP weights arranged for each chunk width: [0] nc 64, [1] nc 128
-    const __nv_bfloat16 *w1v[2][kMaxLayers], *w2v[2][kMaxLayers];
+    const __nv_bfloat16 *w1v[2][kMaxLayers], *w2v[2][kMaxLayers];  // chunk widths 32 | 64
     int n_nc = 1;
     const __nv_bfloat16 *wtm, *wtc, *wc1;
-    int nc_mlp;  // default MLP chunk width (columns of ff1 per step)
     int bn_qkv;  // N block of the q/k/v GEMM
     int bn_tm;   // N block of the token_mix convolution
 
    private:
+    static constexpr size_t kMlpSmemMax = 200 * 1024;
+    int dims_D_ = 0, dims_F_ = 0;
+    Tuning def_tuning_{32, 3, 256};
+    bool mlp_fits(int nc, int ns) const;
+    void launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln, const Pack& p,
+                    cudaStream_t s) const;
     mutable std::mutex tune_mu_;
     mutable std::map<int, Tuning> tuned_;  // row-count bucket -> schedule
     std::string cache_key_;
     void load_cache();
-    void save_cache(int bucket, const Tuning& t) const;
+    void save_cache(int bucket, const Tuning& t, const std::string& timings) const;
 };
 
 }  // namespace jc

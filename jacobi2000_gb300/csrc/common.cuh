@@ -82,6 +82,24 @@ __device__ __forceinline__ float gelu_erf(float x) {
     return 0.5f * x * (1.0f + erff(x * 0.70710678118654752440f));
 }
 
+// Asynchronous global -> shared copies (no register staging, many in flight
+// per thread). `bytes` of the source are copied and the rest of the 4- or
+// 16-byte destination is zero-filled, so bytes = 0 writes zeros (the source
+// address must still be a valid one).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+// Waits for every copy this thread issued (a __syncthreads() must follow
+// before other threads read the data).
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Neumaier compensated accumulator in f64.
 struct Neu {
     double s, c;

@@ -247,14 +247,29 @@ __global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, con
 // tile's c1 values plus a one-cell halo are staged channel-major in shared
 // memory (consecutive threads read consecutive cells: no bank conflicts), the
 // weights as [ci][tap] float4 (3 outputs + 0). One thread per cell.
+// head.conv2 (3x3, HD -> C, zero padding; cpu.rs:171-205, 347-348) and the
+// step's residual (cpu.rs:84-88) over one 16 x 16 cell tile per CTA. The
+// halo tile of c1 is staged channel-last in shared memory by asynchronous
+// copies (all in flight at once) with a position pitch of HD + 4 floats, so the 16-byte reads of eight neighbouring
+// positions fall in distinct banks. Each of the 64 threads owns a vertical
+// strip of 4 cells: per input channel it reads the 6 x 3 halo values once
+// and the channel's 9 taps x C weights once, and reuses both across the
+// strip (432 FMAs per 54 shared-memory reads per channel group). Per cell,
+// the sum runs in the reference's order: bias, then channel, ky, kx.
+constexpr int kConv2Threads = 64;
+constexpr int kConv2Pitch = 36;  // floats per halo position (HD = 32 + 4 pad)
+constexpr int kConv2Smem = ((kCellTile + 2) * (kCellTile + 2) * kConv2Pitch + 32 * 9 * 4) * 4;
+
 template <int C, int HD>
-__global__ void __launch_bounds__(256) conv2_step_kernel(const float* __restrict__ c1, const float* __restrict__ w2,
-                                                         const float* __restrict__ b2, const InstDev* inst,
-                                                         int n_inst, int mode) {
-    static_assert(C <= 4, "conv2 keeps its outputs in one float4 weight row");
-    constexpr int S = kCellTile + 2;
-    __shared__ float tile[HD][S * S];
-    __shared__ float4 ws[HD][9];
+__global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* __restrict__ c1,
+                                                                   const float* __restrict__ w2,
+                                                                   const float* __restrict__ b2, const InstDev* inst,
+                                                                   int n_inst, int mode) {
+    static_assert(C == 3 && HD == 32, "conv2 is built for 3 channels and a cell-head width of 32");
+    constexpr int S = kCellTile + 2, Q = HD / 4, P = kConv2Pitch;
+    extern __shared__ __align__(16) float c2smem[];
+    float* tile = c2smem;                                   // [S*S][P]
+    float4* ws = reinterpret_cast<float4*>(c2smem + S * S * P);  // [HD][9] (C outputs + pad)
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -269,47 +284,63 @@ __global__ void __launch_bounds__(256) conv2_step_kernel(const float* __restrict
         float w[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int co = 0; co < C; co++) w[co] = w2[(co * HD + ci) * 9 + tap];
-        ws[ci][tap] = make_float4(w[0], w[1], w[2], w[3]);
+        ws[i] = make_float4(w[0], w[1], w[2], w[3]);
     }
-    constexpr int Q = HD / 4;
     for (int e = threadIdx.x; e < S * S * Q; e += blockDim.x) {
         const int q = e % Q, p = e / Q, sy = p / S, sx = p % S;
         const int y = y0 + sy - 1, x = x0 + sx - 1;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (y >= 0 && x >= 0 && y < I.ny && x < I.nx)
-            v = reinterpret_cast<const float4*>(c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD)[q];
-        tile[4 * q + 0][p] = v.x;
-        tile[4 * q + 1][p] = v.y;
-        tile[4 * q + 2][p] = v.z;
-        tile[4 * q + 3][p] = v.w;
+        const bool in = y >= 0 && x >= 0 && y < I.ny && x < I.nx;
+        const float* src = in ? c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 4 * q : c1;
+        cp_async16(tile + p * P + 4 * q, src, in);  // zero outside the grid
     }
+    cp_async_wait_all();
     __syncthreads();
-    const int ty = threadIdx.x / kCellTile, tx = threadIdx.x % kCellTile;
-    const int y = y0 + ty, x = x0 + tx;
-    if (y >= I.ny || x >= I.nx) return;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const int tx = threadIdx.x % kCellTile, sy = (threadIdx.x / kCellTile) * 4;  // cells (tx, sy..sy+3)
+    float acc[4][C];
 #pragma unroll
-    for (int co = 0; co < C; co++) acc[co] = b2[co];
-#pragma unroll 4
-    for (int ci = 0; ci < HD; ci++) {
+    for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int ky = 0; ky < 3; ky++)
+        for (int co = 0; co < C; co++) acc[i][co] = b2[co];
+#pragma unroll 1
+    for (int q = 0; q < Q; q++) {
+        float4 a[6][3];  // halo rows sy..sy+5, columns tx..tx+2, channels 4q..4q+3
 #pragma unroll
-            for (int kx = 0; kx < 3; kx++) {
-                const float a = tile[ci][(ty + ky) * S + tx + kx];  // zero outside the grid
-                const float4 w = ws[ci][ky * 3 + kx];
-                acc[0] = fmaf(a, w.x, acc[0]);
-                acc[1] = fmaf(a, w.y, acc[1]);
-                acc[2] = fmaf(a, w.z, acc[2]);
-                acc[3] = fmaf(a, w.w, acc[3]);
-            }
+        for (int r = 0; r < 6; r++)
+#pragma unroll
+            for (int kx = 0; kx < 3; kx++) a[r][kx] = reinterpret_cast<const float4*>(tile + ((sy + r) * S + tx + kx) * P)[q];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int ci = 4 * q + c;
+#pragma unroll
+            for (int ky = 0; ky < 3; ky++)
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) {
+                    const float4 w = ws[ci * 9 + ky * 3 + kx];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const float4 av = a[i + ky][kx];
+                        const float v = c == 0 ? av.x : c == 1 ? av.y : c == 2 ? av.z : av.w;
+                        acc[i][0] = fmaf(v, w.x, acc[i][0]);
+                        acc[i][1] = fmaf(v, w.y, acc[i][1]);
+                        acc[i][2] = fmaf(v, w.z, acc[i][2]);
+                    }
+                }
+        }
     }
-    const size_t plane = (size_t)I.nx * I.ny, cl = (size_t)y * I.nx + x;
+    const size_t plane = (size_t)I.nx * I.ny;
+    const int x = x0 + tx;
+    if (x >= I.nx) return;
 #pragma unroll
-    for (int co = 0; co < C; co++) {
-        float v = acc[co];
-        if (mode == kWriteNextState) v = v + I.state[co * plane + cl];
-        I.out[co * plane + cl] = v;
+    for (int i = 0; i < 4; i++) {
+        const int y = y0 + sy + i;
+        if (y >= I.ny) break;
+        const size_t cl = (size_t)y * I.nx + x;
+#pragma unroll
+        for (int co = 0; co < C; co++) {
+            float v = acc[i][co];
+            if (mode == kWriteNextState) v = v + I.state[co * plane + cl];
+            I.out[co * plane + cl] = v;
+        }
     }
 }
 
@@ -575,8 +606,14 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
                 cudaStream_t s) {
     KScope k(name, s);
     if (d.C != 3 || d.HD != 32) throw std::runtime_error("conv2 is built for 3 channels and a cell-head width of 32");
-    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, kCellTile * kCellTile, 0, s>>>(c1, w.c2_w, w.c2_b, p.inst, p.n_inst,
-                                                                              mode);
+    static bool attr = false;
+    if (!attr) {
+        cuda_check_attr(cudaFuncSetAttribute(f32k::conv2_step_kernel<3, 32>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, f32k::kConv2Smem));
+        attr = true;
+    }
+    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, f32k::kConv2Threads, f32k::kConv2Smem, s>>>(c1, w.c2_w, w.c2_b, p.inst,
+                                                                                          p.n_inst, mode);
     check_launch(name);
 }
 
