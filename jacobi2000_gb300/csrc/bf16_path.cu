@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
                                                        int R, float* __restrict__ x, bf16* __restrict__ ln) {
     extern __shared__ __align__(16) float esm[];
     constexpr int D = 32 * CPL;
-    const int P = d.P, pd = d.C * P * P;
+    constexpr int P = 4, pd = 3 * P * P;  // 3 channels, patch 4 (checked when the path is built)
     float* sW = esm;                   // [pd][D]
     float* sP = esm + (size_t)pd * D;  // [pd][kEmbedRows]
     __shared__ int rinst[kEmbedRows];
@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
     for (int k = 0; k < 8; k++)
 #pragma unroll
         for (int c = 0; c < CPL; c++) v[k][c] = be[o0 + c];
+#pragma unroll 8
     for (int f = 0; f < pd; f++) {
         const float4 p0 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0);
         const float4 p1 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0 + 4);
@@ -198,19 +199,29 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
 #pragma unroll
             for (int c = 0; c < CPL; c++) v[k][c] = fmaf(pv[k], wv[c], v[k][c]);
     }
+    // the meta linear depends only on the instance: computed once for the
+    // warp's first row and again only where the instance changes
+    int m_inst = -1;
+    float m[CPL];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const int r = r0 + i0 + k;
         if (r >= R) continue;  // warp-uniform
-        const InstDev& I = inst[rinst[i0 + k]];
+        const int ii = rinst[i0 + k];
+        const InstDev& I = inst[ii];
+        if (ii != m_inst) {
+            m_inst = ii;
+#pragma unroll
+            for (int c = 0; c < CPL; c++) {
+                m[c] = bm[o0 + c];
+                for (int f = 0; f < d.meta_dim; f++) m[c] = fmaf(I.meta[f], Wm[(size_t)f * D + o0 + c], m[c]);
+            }
+        }
         const int t = r - I.row0;
         float sum = 0.f;
 #pragma unroll
         for (int c = 0; c < CPL; c++) {
-            const int o = o0 + c;
-            float m = bm[o];
-            for (int f = 0; f < d.meta_dim; f++) m = fmaf(I.meta[f], Wm[(size_t)f * D + o], m);
-            v[k][c] = (v[k][c] + I.pos[(size_t)t * D + o]) + m;
+            v[k][c] = (v[k][c] + I.pos[(size_t)t * D + o0 + c]) + m[c];
             sum += v[k][c];
         }
         const float mean = warp_sum(sum) / (float)D;

@@ -249,15 +249,17 @@ __global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, con
 // weights as [ci][tap] float4 (3 outputs + 0). One thread per cell.
 // head.conv2 (3x3, HD -> C, zero padding; cpu.rs:171-205, 347-348) and the
 // step's residual (cpu.rs:84-88) over one 16 x 16 cell tile per CTA. The
-// halo tile of c1 is staged channel-last in shared memory by asynchronous
-// copies (all in flight at once) with a position pitch of HD + 4 floats, so the 16-byte reads of eight neighbouring
-// positions fall in distinct banks. Each of the 64 threads owns a vertical
-// strip of 4 cells: per input channel it reads the 6 x 3 halo values once
-// and the channel's 9 taps x C weights once, and reuses both across the
-// strip (432 FMAs per 54 shared-memory reads per channel group). Per cell,
-// the sum runs in the reference's order: bias, then channel, ky, kx.
+// halo tile of c1 is staged channel-last in shared memory, half of the
+// channels at a time, by asynchronous copies (all in flight at once), with a
+// position pitch of HD/2 + 4 floats so the 16-byte reads of eight
+// neighbouring positions fall in distinct banks; the small footprint keeps
+// seven CTAs per SM, whose loads and arithmetic overlap. Each of the 64
+// threads owns a vertical strip of 4 cells: per group of 4 input channels it
+// reads the 6 x 3 halo values once and the channels' 9 taps x C weights once,
+// and reuses both across the strip (432 FMAs per 54 shared-memory reads).
+// Per cell, the sum runs in the reference's order: bias, then channel, ky, kx.
 constexpr int kConv2Threads = 64;
-constexpr int kConv2Pitch = 36;  // floats per halo position (HD = 32 + 4 pad)
+constexpr int kConv2Pitch = 20;  // floats per halo position (HD / 2 = 16 + 4 pad)
 constexpr int kConv2Smem = ((kCellTile + 2) * (kCellTile + 2) * kConv2Pitch + 32 * 9 * 4) * 4;
 
 template <int C, int HD>
@@ -266,9 +268,9 @@ __global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* 
                                                                    const float* __restrict__ b2, const InstDev* inst,
                                                                    int n_inst, int mode) {
     static_assert(C == 3 && HD == 32, "conv2 is built for 3 channels and a cell-head width of 32");
-    constexpr int S = kCellTile + 2, Q = HD / 4, P = kConv2Pitch;
+    constexpr int S = kCellTile + 2, QH = HD / 8, P = kConv2Pitch;  // QH float4 groups per channel half
     extern __shared__ __align__(16) float c2smem[];
-    float* tile = c2smem;                                   // [S*S][P]
+    float* tile = c2smem;                                        // [S*S][P], one channel half
     float4* ws = reinterpret_cast<float4*>(c2smem + S * S * P);  // [HD][9] (C outputs + pad)
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
@@ -279,6 +281,16 @@ __global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* 
     const int tiles_x = (I.nx + kCellTile - 1) / kCellTile;
     const int tl = blockIdx.x - I.tile0;
     const int y0 = (tl / tiles_x) * kCellTile, x0 = (tl % tiles_x) * kCellTile;
+    auto load_half = [&](int h) {
+        for (int e = threadIdx.x; e < S * S * QH; e += blockDim.x) {
+            const int q = e % QH, p = e / QH, sy = p / S, sx = p % S;
+            const int y = y0 + sy - 1, x = x0 + sx - 1;
+            const bool in = y >= 0 && x >= 0 && y < I.ny && x < I.nx;
+            const float* src = in ? c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 4 * (QH * h + q) : c1;
+            cp_async16(tile + p * P + 4 * q, src, in);  // zero outside the grid
+        }
+    };
+    load_half(0);
     for (int i = threadIdx.x; i < HD * 9; i += blockDim.x) {
         const int ci = i / 9, tap = i % 9;
         float w[4] = {0.f, 0.f, 0.f, 0.f};
@@ -286,15 +298,6 @@ __global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* 
         for (int co = 0; co < C; co++) w[co] = w2[(co * HD + ci) * 9 + tap];
         ws[i] = make_float4(w[0], w[1], w[2], w[3]);
     }
-    for (int e = threadIdx.x; e < S * S * Q; e += blockDim.x) {
-        const int q = e % Q, p = e / Q, sy = p / S, sx = p % S;
-        const int y = y0 + sy - 1, x = x0 + sx - 1;
-        const bool in = y >= 0 && x >= 0 && y < I.ny && x < I.nx;
-        const float* src = in ? c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 4 * q : c1;
-        cp_async16(tile + p * P + 4 * q, src, in);  // zero outside the grid
-    }
-    cp_async_wait_all();
-    __syncthreads();
     const int tx = threadIdx.x % kCellTile, sy = (threadIdx.x / kCellTile) * 4;  // cells (tx, sy..sy+3)
     float acc[4][C];
 #pragma unroll
@@ -302,29 +305,39 @@ __global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* 
 #pragma unroll
         for (int co = 0; co < C; co++) acc[i][co] = b2[co];
 #pragma unroll 1
-    for (int q = 0; q < Q; q++) {
-        float4 a[6][3];  // halo rows sy..sy+5, columns tx..tx+2, channels 4q..4q+3
+    for (int h = 0; h < 2; h++) {
+        if (h == 1) {
+            __syncthreads();  // every thread is done with the first half
+            load_half(1);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll 1
+        for (int q = 0; q < QH; q++) {
+            float4 a[6][3];  // halo rows sy..sy+5, columns tx..tx+2, channels 4 (QH h + q) ..
 #pragma unroll
-        for (int r = 0; r < 6; r++)
+            for (int r = 0; r < 6; r++)
 #pragma unroll
-            for (int kx = 0; kx < 3; kx++) a[r][kx] = reinterpret_cast<const float4*>(tile + ((sy + r) * S + tx + kx) * P)[q];
+                for (int kx = 0; kx < 3; kx++)
+                    a[r][kx] = reinterpret_cast<const float4*>(tile + ((sy + r) * S + tx + kx) * P)[q];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const int ci = 4 * q + c;
+            for (int c = 0; c < 4; c++) {
+                const int ci = 4 * (QH * h + q) + c;
 #pragma unroll
-            for (int ky = 0; ky < 3; ky++)
+                for (int ky = 0; ky < 3; ky++)
 #pragma unroll
-                for (int kx = 0; kx < 3; kx++) {
-                    const float4 w = ws[ci * 9 + ky * 3 + kx];
+                    for (int kx = 0; kx < 3; kx++) {
+                        const float4 w = ws[ci * 9 + ky * 3 + kx];
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const float4 av = a[i + ky][kx];
-                        const float v = c == 0 ? av.x : c == 1 ? av.y : c == 2 ? av.z : av.w;
-                        acc[i][0] = fmaf(v, w.x, acc[i][0]);
-                        acc[i][1] = fmaf(v, w.y, acc[i][1]);
-                        acc[i][2] = fmaf(v, w.z, acc[i][2]);
+                        for (int i = 0; i < 4; i++) {
+                            const float4 av = a[i + ky][kx];
+                            const float v = c == 0 ? av.x : c == 1 ? av.y : c == 2 ? av.z : av.w;
+                            acc[i][0] = fmaf(v, w.x, acc[i][0]);
+                            acc[i][1] = fmaf(v, w.y, acc[i][1]);
+                            acc[i][2] = fmaf(v, w.z, acc[i][2]);
+                        }
                     }
-                }
+            }
         }
     }
     const size_t plane = (size_t)I.nx * I.ny;
