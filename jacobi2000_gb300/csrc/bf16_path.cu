@@ -66,10 +66,12 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// bf16 tensor of `rank` dims (innermost first), strides in bytes of dims
-// 1..rank-1, box dims; no swizzle, zero fill out of bounds.
+// Tensor of `rank` dims (innermost first), strides in bytes of dims
+// 1..rank-1, box dims; bf16 and no swizzle unless given; zero fill out of
+// bounds.
 static CUtensorMap make_map(const void* base, int rank, const uint64_t* dims, const uint64_t* strides,
-                            const uint32_t* box) {
+                            const uint32_t* box, CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                            CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE) {
     CUtensorMap m;
     cuuint64_t gd[5], gs[4];
     cuuint32_t bx[5], es[5];
@@ -79,8 +81,8 @@ static CUtensorMap make_map(const void* base, int rank, const uint64_t* dims, co
         es[i] = 1;
     }
     for (int i = 0; i < rank - 1; i++) gs[i] = strides[i];
-    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), gd, gs, bx, es,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    CUresult r = encode_fn()(&m, type, rank, const_cast<void*>(base), gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             swz,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(JC_CUDA_ERROR, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return m;
@@ -92,6 +94,19 @@ static CUtensorMap rows_map(const void* base, int cols, int rows) {
     uint64_t strides[1] = {(uint64_t)cols * 2};
     uint32_t box[2] = {8, 128};
     return make_map(base, 2, dims, strides, box);
+}
+
+// Output tiles of a [rows, cols] matrix with row pitch `ld` elements (bf16,
+// or f32 when f32): boxes of 128 bytes x 128 rows, stored from shared memory
+// in the 128-byte swizzled layout (16-byte chunk j of tile row r at chunk
+// j ^ (r % 8)).
+static CUtensorMap store_map(const void* base, int cols, int rows, int ld, bool f32) {
+    const int es = f32 ? 4 : 2;
+    uint64_t dims[2] = {(uint64_t)cols, (uint64_t)(rows > 0 ? rows : 1)};
+    uint64_t strides[1] = {(uint64_t)ld * es};
+    uint32_t box[2] = {(uint32_t)(128 / es), 128};
+    return make_map(base, 2, dims, strides, box, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                    CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 // One instance's [ny, nx, C] channel-last grid, loaded as 8-channel x 10 x 18 halo boxes.
@@ -641,11 +656,13 @@ struct GemmEpi {
 // the epilogue from TMEM.
 template <int EPI>
 __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                      const __grid_constant__ CUtensorMap tmO,
                                                       const bf16* __restrict__ Bblk, int K, int BN, int R,
                                                       GemmEpi ep, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;                       // [K/8][128][8]
     uint8_t* sB = smem + (size_t)K * 256;     // [K/8][BN][8]
+    __shared__ float sbias[256];
     __shared__ uint64_t bar_load, bar_mma;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
@@ -663,6 +680,8 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
         }
     }
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    if (EPI != EPI_RESID_LN)
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) sbias[i] = ep.bias[nb * BN + i];
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
@@ -688,7 +707,6 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
     const bool ok = __syncthreads_and(tc::mbar_wait(&bar_mma, 0, err, &failed) ? 1 : 0) != 0;
     tc::tc_fence_after();
     if (ok) {
-        const int row = m0 + threadIdx.x;
         const uint32_t ta = lane_addr(tmem);
         const int n0 = nb * BN;
         if (EPI == EPI_RESID_LN) {
@@ -699,20 +717,40 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
             __syncthreads();
             rows_resid_ln_any(tile, BN, m0, R, ep.bias, ep.x, ep.g, ep.b, ep.out_bf, warp, 4);
         } else {
+            // stage the tile (bias added) in 128-byte swizzled boxes of 128
+            // rows in the operand shared memory, then store it with TMA
+            constexpr int EB = EPI == EPI_BF16 ? 2 : 4;  // bytes per element
+            constexpr int PB = 128 / EB;                 // elements per box row
+            const int r = threadIdx.x;
             for (int c = 0; c < BN; c += 16) {
                 float a[16];
                 tc::tmem_ld16(ta + c, a);  // collective: every lane of the warp loads
-                if (row < R) {
 #pragma unroll
-                    for (int i = 0; i < 16; i++) a[i] += ep.bias[n0 + c + i];
-                    if (EPI == EPI_BF16) {
-                        store_bf16x16(ep.out_bf + (size_t)row * ep.ldo + n0 + c, a);
-                    } else {
-                        float4* o = reinterpret_cast<float4*>(ep.out_f + (size_t)row * ep.ldo + n0 + c);
-#pragma unroll
-                        for (int i = 0; i < 4; i++) o[i] = make_float4(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]);
-                    }
+                for (int i = 0; i < 16; i += 4) {
+                    const float4 bv = *reinterpret_cast<const float4*>(sbias + c + i);
+                    a[i] += bv.x;
+                    a[i + 1] += bv.y;
+                    a[i + 2] += bv.z;
+                    a[i + 3] += bv.w;
                 }
+                uint8_t* box = smem + (size_t)(c / PB) * 16384 + (size_t)r * 128;
+                const int j0 = (c % PB) * EB / 16;  // first 16-byte chunk of these 16 columns
+                if (EPI == EPI_BF16) {
+                    BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
+                    BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        *reinterpret_cast<float4*>(box + (((j0 + q) ^ (r & 7)) << 4)) =
+                            make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+                }
+            }
+            tc::fence_async_shared();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int c = 0; c < BN; c += PB) tc::tma_store_2d(&tmO, smem + (size_t)(c / PB) * 16384, n0 + c, m0);
+                tc::bulk_commit();
+                tc::bulk_wait_read();
             }
         }
     }
@@ -1521,6 +1559,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     bf16* zc = reinterpret_cast<bf16*>(p.bc[0]);
     float* c1 = reinterpret_cast<float*>(p.bc[1]);
     const CUtensorMap m_ln = rows_map(ln, D, R), m_attn = rows_map(attn, D, R), m_t1 = rows_map(t1, D, R);
+    const CUtensorMap m_qkv_out = store_map(qkv, 3 * D, R, 3 * D, false), m_z0_out = store_map(p.z0, d.HD, R, d.HD, true);
     const unsigned gm = (unsigned)((R + 127) / 128);
     const Tuning tu = tuning_for(R);
     {
@@ -1545,8 +1584,9 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             KScope k("tc_qkv", s);
             const int BN = bn_qkv;
             GemmEpi ep{B.bqkv, qkv, nullptr, nullptr, nullptr, nullptr, 3 * D};
-            tc_gemm_kernel<EPI_BF16><<<dim3(gm, 3 * D / BN), 128, (size_t)D * 256 + (size_t)D * BN * 2, s>>>(
-                m_ln, wqkv[l], D, BN, R, ep, p.err);
+            const size_t smem = std::max((size_t)D * 256 + (size_t)D * BN * 2, (size_t)((BN + 63) / 64) * 16384);
+            tc_gemm_kernel<EPI_BF16><<<dim3(gm, 3 * D / BN), 128, smem, s>>>(m_ln, m_qkv_out, wqkv[l], D, BN, R, ep,
+                                                                         p.err);
             check_launch("tc_qkv");
         }
         {
@@ -1558,8 +1598,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             KScope k("tc_proj_ln", s);
             GemmEpi ep{B.bp, ln, nullptr, p.x, B.n2g, B.n2b, D};
             const size_t smem = std::max((size_t)D * 256 + (size_t)D * D * 2, (size_t)128 * D * 4);
-            tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(
-                m_attn, wp[l], D, D, R, ep, p.err);
+            tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(m_attn, m_attn, wp[l], D, D, R, ep, p.err);
             check_launch("tc_proj_ln");
         }
         {
@@ -1579,8 +1618,8 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     {
         KScope k("tc_to_cells", s);
         GemmEpi ep{w.tc_b, nullptr, p.z0, nullptr, nullptr, nullptr, d.HD};
-        tc_gemm_kernel<EPI_F32><<<dim3(gm, 1), 128, (size_t)D * 256 + (size_t)D * d.HD * 2, s>>>(
-            m_t1, wtc, D, d.HD, R, ep, p.err);
+        const size_t smem = std::max((size_t)D * 256 + (size_t)D * d.HD * 2, (size_t)((d.HD + 31) / 32) * 16384);
+        tc_gemm_kernel<EPI_F32><<<dim3(gm, 1), 128, smem, s>>>(m_t1, m_z0_out, wtc, D, d.HD, R, ep, p.err);
         check_launch("tc_to_cells");
     }
     const long long NC = p.NC;
