@@ -109,6 +109,19 @@ static CUtensorMap store_map(const void* base, int cols, int rows, int ld, bool 
                     CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+// One instance's [ny, nx, C] channel-last grid (bf16, or f32 when f32),
+// stored as 128-byte x 8 x 16 boxes (one 8 x 16 conv tile, 128 bytes of
+// channels) from 128-byte swizzled shared memory; positions outside the grid
+// are not written.
+static CUtensorMap tile_store_map(const void* base, int C, int nx, int ny, bool f32) {
+    const int es = f32 ? 4 : 2;
+    uint64_t dims[3] = {(uint64_t)C, (uint64_t)nx, (uint64_t)ny};
+    uint64_t strides[2] = {(uint64_t)C * es, (uint64_t)nx * C * es};
+    uint32_t box[3] = {(uint32_t)(128 / es), kConvTX, kConvTY};
+    return make_map(base, 3, dims, strides, box, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                    CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
 // One instance's [ny, nx, C] channel-last grid, loaded as 8-channel x 10 x 18 halo boxes.
 static CUtensorMap halo_map(const void* base, int C, int nx, int ny) {
     uint64_t dims[3] = {(uint64_t)C, (uint64_t)nx, (uint64_t)ny};
@@ -1084,15 +1097,35 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
 //            CONV1:  out = gelu(acc + b)      (cpu.rs:345-346), f32.
 enum { CONV_TOKMIX = 0, CONV_CELL1 = 1 };
 
+// Shared memory of tc_conv3_kernel: the halo planes, then NS tap weight
+// blocks; with NS = 9 every tap is resident and loaded once.
+static __host__ __device__ size_t conv3_smem(int C, int BN, int NS) {
+    return (size_t)(C / 8) * kHaloPlane + (size_t)NS * C * BN * 2;
+}
+// Where the epilogue stages its output boxes: after the halo (1024-aligned,
+// for the 128-byte swizzle) when the halo is still read (token mix), else at
+// the start.
+static __host__ __device__ size_t conv3_stage_offset(int C, bool after_halo) {
+    return after_halo ? ((size_t)(C / 8) * kHaloPlane + 1023) / 1024 * 1024 : 0;
+}
+// Dynamic shared memory of a launch: operands, or the staged output boxes
+// (128 bytes of channels each, eb bytes per element) if those need more.
+static size_t conv3_launch_smem(int C, int BN, int NS, int eb) {
+    const size_t boxes = (size_t)((BN * eb + 127) / 128);
+    return std::max(conv3_smem(C, BN, NS), conv3_stage_offset(C, eb == 2) + boxes * 16384);
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __restrict__ maps, int map_slot,
-                                                       const bf16* __restrict__ Wt, const float* __restrict__ bias,
-                                                       int C, int BN, int N, const InstDev* inst, int n_inst,
-                                                       void* __restrict__ out, int* err) {
+                                                       int store_slot, const bf16* __restrict__ Wt,
+                                                       const float* __restrict__ bias, int C, int BN, int NS,
+                                                       const InstDev* inst, int n_inst, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sHalo = smem;                                   // [C/8][18][10][8]
-    uint8_t* sB = smem + (size_t)(C / 8) * kHaloPlane;       // 2 x [C/8][BN][8]
-    __shared__ uint64_t bar_h, bar_b[2], bar_m[2], bar_done;
+    uint8_t* sB = smem + (size_t)(C / 8) * kHaloPlane;       // NS x [C/8][BN][8]
+    constexpr int kMaxNS = 9;
+    __shared__ uint64_t bar_h, bar_b[kMaxNS], bar_m[kMaxNS], bar_done;
+    __shared__ float sbias[256];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5;
@@ -1105,26 +1138,28 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
         if (t0 <= tile) lo = mid; else hi = mid - 1;
     }
     const InstDev& I = inst[lo];
-    const int gw = KIND == CONV_TOKMIX ? I.tx : I.nx, gh = KIND == CONV_TOKMIX ? I.ty : I.ny;
+    const int gw = KIND == CONV_TOKMIX ? I.tx : I.nx;
     const int tiles_x = (gw + kConvTX - 1) / kConvTX;
     const int tl = tile - (KIND == CONV_TOKMIX ? I.tt0 : I.ct0);
     const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY;
-    const CUtensorMap* map = maps + 2 * lo + map_slot;
+    const CUtensorMap* map = maps + kMapsPerInst * lo + map_slot;
+    const CUtensorMap* omap = maps + kMapsPerInst * lo + store_slot;
     const uint32_t ncols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
     if (threadIdx.x == 0) {
         tc::mbar_init(&bar_h, 1);
         tc::mbar_init(&bar_done, 1);
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < kMaxNS; i++) {
             tc::mbar_init(&bar_b[i], 1);
             tc::mbar_init(&bar_m[i], 1);
         }
         tc::fence_barrier_init();
         failed = 0;
-        if (tc::smem_u32(smem) & 1023u) {  // operand tiles need aligned shared memory
+        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxNS) {  // aligned operand tiles
             failed = 1;
             atomicExch(err, 2);
         }
     }
+    for (int i = threadIdx.x; i < BN; i += blockDim.x) sbias[i] = bias[nb * BN + i];
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
@@ -1134,10 +1169,11 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     const bf16* Wn = Wt + (size_t)nb * 9 * C * BN;
     if (threadIdx.x == 0 && !failed) {
         tc::tensormap_acquire(map);
+        tc::tensormap_acquire(omap);
         tc::mbar_expect_tx(&bar_h, (uint32_t)(C / 8) * (kHaloW * kHaloH * 16));
         for (int kc = 0; kc < C / 8; kc++)
             tc::tma_load_3d(sHalo + kc * kHaloPlane, map, kc * 8, x0 - 1, y0 - 1, &bar_h);
-        for (int t = 0; t < 2; t++) {
+        for (int t = 0; t < NS && t < 9; t++) {
             tc::mbar_expect_tx(&bar_b[t], wtap);
             tc::bulk_load(sB + t * wtap, Wn + (size_t)t * C * BN, wtap, &bar_b[t]);
         }
@@ -1145,8 +1181,8 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
         const uint32_t idesc = tc::idesc_bf16(128, BN);
         const uint32_t h0 = tc::smem_u32(sHalo);
         for (int t = 0; t < 9 && good; t++) {
-            const int buf = t & 1;
-            good = tc::mbar_wait(&bar_b[buf], (t >> 1) & 1, err, &failed);
+            const int buf = t % NS;
+            good = tc::mbar_wait(&bar_b[buf], (uint32_t)(t / NS) & 1u, err, &failed);
             if (!good) break;
             tc::tc_fence_after();
             const int ky = t / 3, kx = t % 3;
@@ -1156,13 +1192,13 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
                 uint64_t bd = tc::sdesc(b0 + 2 * k * BN * 16, BN * 16, 128);
                 tc::mma_bf16(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
             }
-            tc::mma_commit(&bar_m[buf]);
-            if (t + 2 < 9) {
-                // the buffer is refilled once the MMAs reading it are done
-                good = tc::mbar_wait(&bar_m[buf], (t >> 1) & 1, err, &failed);
+            if (t + NS < 9) {
+                // the stage is refilled once the MMAs reading it are done
+                tc::mma_commit(&bar_m[buf]);
+                good = tc::mbar_wait(&bar_m[buf], (uint32_t)(t / NS) & 1u, err, &failed);
                 if (!good) break;
                 tc::mbar_expect_tx(&bar_b[buf], wtap);
-                tc::bulk_load(sB + buf * wtap, Wn + (size_t)(t + 2) * C * BN, wtap, &bar_b[buf]);
+                tc::bulk_load(sB + buf * wtap, Wn + (size_t)(t + NS) * C * BN, wtap, &bar_b[buf]);
             }
         }
         if (good) tc::mma_commit(&bar_done);  // arrives when every MMA above is done
@@ -1171,34 +1207,51 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     const bool ok = __syncthreads_and(tc::mbar_wait(&bar_done, 0, err, &failed) ? 1 : 0) != 0;
     tc::tc_fence_after();
     if (ok) {
+        // epilogue into 128-byte swizzled boxes of the 128 tile positions
+        // (row r = position (y0 + r / 8, x0 + r % 8)), stored with TMA;
+        // positions outside the grid are clipped by the store
         const int r = threadIdx.x;
-        const int y = y0 + r / kConvTX, x = x0 + r % kConvTX;
-        const bool valid = y < gh && x < gw;
         const uint32_t ta = lane_addr(tmem);
-        const int n0 = nb * BN;
-        const long long pos = KIND == CONV_TOKMIX ? (long long)I.row0 + (long long)y * gw + x
-                                                  : I.cell0 + (long long)y * gw + x;
+        constexpr int EB = KIND == CONV_TOKMIX ? 2 : 4;  // bytes per output element
+        constexpr int PB = 128 / EB;                     // elements per box row
+        // TOKMIX still reads the halo centre, so it stages after the halo
+        uint8_t* stage = smem + conv3_stage_offset(C, KIND == CONV_TOKMIX);
         for (int c = 0; c < BN; c += 16) {
             float a[16];
             tc::tmem_ld16(ta + c, a);
-            if (!valid) continue;
             if (KIND == CONV_TOKMIX) {
                 // the centre of the halo tile is xn at this token
                 const uint8_t* centre = sHalo + ((r / kConvTX + 1) * kHaloW + (r % kConvTX + 1)) * 16;
+                const int n0 = nb * BN;
 #pragma unroll
                 for (int i = 0; i < 16; i++) {
                     const int ch = n0 + c + i;
                     const float xn = bf2f(*reinterpret_cast<const bf16*>(centre + (size_t)(ch / 8) * kHaloPlane + (ch % 8) * 2));
-                    a[i] = xn + gelu_fast(a[i] + bias[ch]);
+                    a[i] = xn + gelu_fast(a[i] + sbias[c + i]);
                 }
-                store_bf16x16(static_cast<bf16*>(out) + (size_t)pos * N + n0 + c, a);
             } else {
 #pragma unroll
-                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + bias[n0 + c + i]);
-                float4* o = reinterpret_cast<float4*>(static_cast<float*>(out) + (size_t)pos * N + n0 + c);
-#pragma unroll
-                for (int i = 0; i < 4; i++) o[i] = make_float4(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]);
+                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + sbias[c + i]);
             }
+            uint8_t* box = stage + (size_t)(c / PB) * 16384 + (size_t)r * 128;
+            const int j0 = (c % PB) * EB / 16;
+            if (KIND == CONV_TOKMIX) {
+                BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
+                BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    *reinterpret_cast<float4*>(box + (((j0 + q) ^ (r & 7)) << 4)) =
+                        make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+            }
+        }
+        tc::fence_async_shared();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int c = 0; c < BN; c += PB)
+                tc::tma_store_3d(omap, stage + (size_t)(c / PB) * 16384, nb * BN + c, x0, y0);
+            tc::bulk_commit();
+            tc::bulk_wait_read();
         }
     }
     tc::tc_fence_before();
@@ -1533,15 +1586,18 @@ void BF16Path::alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows,
     p.bc_stride[0] = kZcCh * 2;
     p.bc[1] = static_cast<char*>(a.alloc(NC * d.HD * 4 + 256));  // c1, f32
     p.bc_stride[1] = d.HD * 4;
-    p.tmaps = a.alloc((size_t)max_inst * 2 * sizeof(CUtensorMap));
+    p.tmaps = a.alloc((size_t)max_inst * kMapsPerInst * sizeof(CUtensorMap));
 }
 
 void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s) const {
-    std::vector<CUtensorMap> maps((size_t)p.n_inst * 2);
+    std::vector<CUtensorMap> maps((size_t)p.n_inst * kMapsPerInst);
     for (int i = 0; i < p.n_inst; i++) {
         const InstDev& I = hinst[i];
-        maps[2 * i + 0] = halo_map(p.bt[0] + (size_t)I.row0 * p.bt_stride[0], d.D, I.tx, I.ty);
-        maps[2 * i + 1] = halo_map(p.bc[0] + (size_t)I.cell0 * p.bc_stride[0], kZcCh, I.nx, I.ny);
+        CUtensorMap* m = &maps[(size_t)kMapsPerInst * i];
+        m[0] = halo_map(p.bt[0] + (size_t)I.row0 * p.bt_stride[0], d.D, I.tx, I.ty);
+        m[1] = halo_map(p.bc[0] + (size_t)I.cell0 * p.bc_stride[0], kZcCh, I.nx, I.ny);
+        m[2] = tile_store_map(p.bt[3] + (size_t)I.row0 * p.bt_stride[3], d.D, I.tx, I.ty, false);
+        m[3] = tile_store_map(p.bc[1] + (size_t)I.cell0 * p.bc_stride[1], d.HD, I.nx, I.ny, true);
     }
     // synchronous: the host vector is released on return
     cuda_check(cudaMemcpyAsync(p.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s),
@@ -1610,9 +1666,9 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     {
         KScope k("tc_token_mix", s);
         const int BN = bn_tm;
-        size_t smem = (size_t)(D / 8) * kHaloPlane + 2 * (size_t)D * BN * 2;
-        tc_conv3_kernel<CONV_TOKMIX><<<dim3(p.n_ttiles, D / BN), 128, smem, s>>>(
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), 0, wtm, w.tm_b, D, BN, D, p.inst, n, t1, p.err);
+        const int NS = conv3_smem(D, BN, 9) <= 100 * 1024 ? 9 : 2;
+        tc_conv3_kernel<CONV_TOKMIX><<<dim3(p.n_ttiles, D / BN), 128, conv3_launch_smem(D, BN, NS, 2), s>>>(
+            reinterpret_cast<const CUtensorMap*>(p.tmaps), 0, 2, wtm, w.tm_b, D, BN, NS, p.inst, n, p.err);
         check_launch("tc_token_mix");
     }
     {
@@ -1630,9 +1686,8 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     }
     {
         KScope k("tc_conv1", s);
-        size_t smem = (size_t)(kZcCh / 8) * kHaloPlane + 2 * (size_t)kZcCh * d.HD * 2;
-        tc_conv3_kernel<CONV_CELL1><<<dim3(p.n_ctiles, 1), 128, smem, s>>>(
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), 1, wc1, w.c1_b, kZcCh, d.HD, d.HD, p.inst, n, c1, p.err);
+        tc_conv3_kernel<CONV_CELL1><<<dim3(p.n_ctiles, 1), 128, conv3_launch_smem(kZcCh, d.HD, 9, 4), s>>>(
+            reinterpret_cast<const CUtensorMap*>(p.tmaps), 1, 3, wc1, w.c1_b, kZcCh, d.HD, 9, p.inst, n, p.err);
         check_launch("tc_conv1");
     }
     conv2_step(d, c1, w, p, mode, "bf_conv2_step", s);

@@ -13,6 +13,7 @@
 namespace jc {
 
 constexpr int kMaxLayers = 32;
+constexpr int kMapsPerInst = 4;  // BF16 path: ln halo, zc halo, t1 store, c1 store
 constexpr int kZcStride = 36;  // channel-last stride of the cell-head input: 32 z + 3 state + 1 zero
 
 // Model hyper-parameters shared by every instance of a launch.
@@ -53,7 +54,7 @@ struct Pack {
     long long max_inst_cells;  // cells of the largest instance
     InstDev* inst;    // device array, sorted by row0 / cell0 / tile0
     ProjSlot* proj;   // device array parallel to inst
-    void* tmaps;      // device array: 2 tensor maps per instance (BF16 path)
+    void* tmaps;      // device array: kMapsPerInst tensor maps per instance (BF16 path)
     int* err;         // device flag set when a device-side wait times out
     // FP32 workspace
     float *x, *qkv, *attn, *ff1, *xn, *t1, *z0, *zc, *c1;

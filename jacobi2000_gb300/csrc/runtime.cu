@@ -272,7 +272,7 @@ Pack Workspace::view(const Dims& d, int inst_base, int n, int row_base, int rows
     p.n_tiles = tiles;
     p.n_ttiles = ttiles;
     p.n_ctiles = ctiles;
-    if (base.tmaps) p.tmaps = static_cast<char*>(base.tmaps) + (size_t)inst_base * 2 * 128;
+    if (base.tmaps) p.tmaps = static_cast<char*>(base.tmaps) + (size_t)inst_base * kMapsPerInst * 128;
     p.inst = base.inst + inst_base;
     p.proj = base.proj + inst_base;
     const size_t r = (size_t)row_base, c = (size_t)cell_base;
