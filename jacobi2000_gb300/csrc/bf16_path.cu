@@ -521,18 +521,25 @@ __device__ __forceinline__ void store_bf16x16(bf16* p, const float* v) {
     BfVec<8>::store(p + 8, v + 8);
 }
 
-// Exact-form GELU, 0.5 x (1 + erf(x / sqrt 2)), with erf from Abramowitz &
-// Stegun 7.1.26 (|error| <= 1.5e-7 for the formula; the reciprocal and
-// exponential use the hardware approximations). Used where the result is
-// rounded to bf16 or feeds bf16 arithmetic.
+// GELU, x Phi(x) (cpu.rs:67-74), as x * sigmoid(2 u) with the odd
+// polynomial u = x (c1 + c3 x^2 + c5 x^4): the tanh form of Hendrycks &
+// Gimpel (2016) with its coefficients refitted (minimax of the absolute GELU
+// error on |x| <= 9; |x| is clamped to 9, where Phi is 0 or 1 to f32
+// precision). Maximum absolute error 2.6e-5 against the exact erf form, far
+// below the bf16 rounding of the values it feeds. Two MUFU operations
+// (ex2, rcp) and seven FMA-pipe instructions.
 __device__ __forceinline__ float gelu_fast(float x) {
-    const float z = fabsf(x) * 0.70710678118654752440f;
-    const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
-    const float poly =
-        t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
-    const float erf_abs = 1.0f - poly * __expf(-z * z);
-    const float erf_x = copysignf(erf_abs, x);
-    return 0.5f * x * (1.0f + erf_x);
+    // coefficients of u, times -2 log2(e), so sigmoid(2u) = 1 / (1 + 2^t)
+    constexpr float k1 = -2.0f * 1.4426950408889634f * 7.97506042e-01f;
+    constexpr float k3 = -2.0f * 1.4426950408889634f * 3.70071725e-02f;
+    constexpr float k5 = -2.0f * 1.4426950408889634f * -3.51557324e-04f;
+    const float xc = fminf(fmaxf(x, -9.0f), 9.0f);
+    const float x2 = xc * xc;
+    const float t = xc * fmaf(x2, fmaf(x2, k5, k3), k1);
+    float e, r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(t));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+    return x * r;
 }
 
 __device__ __forceinline__ int slot_swz(int r, int D) { return D >= 128 ? (r & 31) : (r & (D / 4 - 1)); }
@@ -560,7 +567,7 @@ __device__ __forceinline__ void stage_rows(uint32_t ta, int r, int D, int c0, in
 template <int SPL>  // float4 slots per lane: D / 128
 __device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
                               float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
-                              bf16* __restrict__ ln, int warp, int nwarps) {
+                              bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
     const int lane = threadIdx.x & 31;
     float4 bb[SPL], gg[SPL], be[SPL];
 #pragma unroll
@@ -571,7 +578,7 @@ __device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const flo
         be[j] = reinterpret_cast<const float4*>(b)[q];
     }
     constexpr int G = 4;  // rows in flight per warp
-    for (int r0 = warp * G; r0 < 128; r0 += nwarps * G) {
+    for (int r0 = warp * G; r0 < nrows; r0 += nwarps * G) {
         float4 a[G][SPL], xv[G][SPL];
 #pragma unroll
         for (int k = 0; k < G; k++) {
@@ -615,16 +622,17 @@ __device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const flo
     }
 }
 
-// D-dispatch of rows_resid_ln (D = 128 SPL 1, 256 SPL 2; D = 32 uses the
-// first 8 lanes of one slot each).
+// D-dispatch of rows_resid_ln over the first `nrows` rows of the tile (a
+// multiple of 4; D = 128 SPL 1, 256 SPL 2; D = 32 uses the first 8 lanes of
+// one slot each).
 __device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
-                                  const float* g, const float* b, bf16* ln, int warp, int nwarps) {
-    if (D == 256) rows_resid_ln<2>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps);
-    else if (D == 128) rows_resid_ln<1>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps);
+                                  const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128) {
+    if (D == 256) rows_resid_ln<2>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else if (D == 128) rows_resid_ln<1>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
     else {
         // narrow rows (D = 32): lanes 0..7 each own one float4 slot
         const int lane = threadIdx.x & 31;
-        for (int r = warp; r < 128; r += nwarps) {
+        for (int r = warp; r < nrows; r += nwarps) {
             const int row = m0 + r;
             if (row >= R) break;
             const bool on = lane < D / 4;
@@ -1088,6 +1096,214 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
 }
 
+// Persistent form of the fused MLP: one CTA per SM walks row tiles (tile =
+// blockIdx.x + k * gridDim.x) with every stage on its own warps, so the
+// tensor core, the GELU arithmetic and the residual + LayerNorm epilogue of
+// consecutive tiles overlap:
+//   warp 0      (one lane) TMA-loads the A tile (single buffer, refilled once
+//               the tile's last S MMA has read it);
+//   warp 1      (one lane) streams the weight chunks W1_j | W2_j through an
+//               NS-stage ring, continuing across tiles;
+//   warp 2      (one lane) issues every MMA: S_g = A @ W1_j into one of two
+//               TMEM S buffers, O += h_g @ W2_j into one of two TMEM O
+//               buffers (one per tile in flight);
+//   warps 3-10  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers);
+//   warps 11-14 stage a finished O buffer (one TMEM lane quarter each),
+//               release it, and run the residual + LayerNorm rows.
+// g counts chunks over all of this CTA's tiles. The arithmetic and its order
+// are those of the other MLP kernels (the same K slices of 16 in the same
+// order), so the result is bit-identical.
+constexpr int kMlpPWarps = 15;
+constexpr int kMlpPThreads = kMlpPWarps * 32;
+
+struct MlpPSmem {
+    size_t a, w, h, b1, epi, total;
+    __host__ __device__ MlpPSmem(int D, int F, int NC, int NS) {
+        a = 0;                                  // [D/8][128][8]
+        w = a + (size_t)D * 256;                // NS x (W1_j | W2_j)
+        h = w + (size_t)NS * 4 * D * NC;        // 2 x [NC/8][128][8]
+        b1 = h + (size_t)2 * NC * 256;          // [F] f32
+        epi = (b1 + (size_t)F * 4 + 1023) / 1024 * 1024;  // 4 x [32][D] f32
+        total = epi + (size_t)128 * D * 4;
+    }
+};
+
+__global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
+    const __grid_constant__ CUtensorMap tmA, const bf16* __restrict__ W1, const bf16* __restrict__ W2,
+    const float* __restrict__ b1, const float* __restrict__ b2, int D, int F, int NC, int NS, int R,
+    float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b, bf16* __restrict__ ln, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const MlpPSmem L(D, F, NC, NS);
+    uint8_t* sA = smem + L.a;
+    uint8_t* sW = smem + L.w;
+    uint8_t* sH = smem + L.h;
+    float* sb1 = reinterpret_cast<float*>(smem + L.b1);
+    float* sEpi = reinterpret_cast<float*>(smem + L.epi);
+    constexpr int kMaxStages = 4;
+    __shared__ uint64_t a_full, a_empty, w_full[kMaxStages], w_empty[kMaxStages], s_full[2], h_full[2], h_empty[2],
+        o_full[2], o_empty[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_tiles = (R + 127) / 128;
+    const int my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int nch = F / NC;
+    const int total = my_tiles * nch;  // chunks this CTA walks
+    const uint32_t s_col = 2u * D;     // O buffers in [0, 2D), S buffers after
+    uint32_t ncols = 32;
+    while (ncols < s_col + 2u * NC) ncols <<= 1;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&a_full, 1);
+        tc::mbar_init(&a_empty, 1);
+        for (int i = 0; i < NS && i < kMaxStages; i++) {
+            tc::mbar_init(&w_full[i], 1);
+            tc::mbar_init(&w_empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(&s_full[i], 1);
+            tc::mbar_init(&h_full[i], 8 * 32);
+            tc::mbar_init(&h_empty[i], 1);
+            tc::mbar_init(&o_full[i], 1);
+            tc::mbar_init(&o_empty[i], 4 * 32);
+        }
+        tc::fence_barrier_init();
+        failed = 0;
+        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages || ncols > 512) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
+    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
+    if (warp == 0) {
+        if (lane == 0 && !failed) {
+            // A producer
+            for (int it = 0; it < my_tiles; it++) {
+                if (it > 0 && !tc::mbar_wait(&a_empty, (uint32_t)(it - 1) & 1u, err, &failed)) break;
+                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+                tc::mbar_expect_tx(&a_full, (uint32_t)D * 256);
+                for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &a_full);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && !failed) {
+            // weight producer
+            for (int gi = 0; gi < total; gi++) {
+                const int st = gi % NS, j = gi % nch;
+                if (gi >= NS && !tc::mbar_wait(&w_empty[st], (uint32_t)(gi / NS - 1) & 1u, err, &failed)) break;
+                uint8_t* dst = sW + (size_t)st * 2 * wbytes;
+                tc::mbar_expect_tx(&w_full[st], 2 * wbytes);
+                tc::bulk_load(dst, W1 + (size_t)j * D * NC, wbytes, &w_full[st]);
+                tc::bulk_load(dst + wbytes, W2 + (size_t)j * D * NC, wbytes, &w_full[st]);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 2) {
+        if (lane == 0 && !failed) {
+            // MMA issuer
+            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH), w0 = tc::smem_u32(sW);
+            const uint32_t idesc_s = tc::idesc_bf16(128, NC), idesc_o = tc::idesc_bf16(128, D);
+            auto issue_s = [&](int gi) -> bool {
+                const int st = gi % NS, j = gi % nch, it = gi / nch;
+                if (j == 0 && !tc::mbar_wait(&a_full, (uint32_t)it & 1u, err, &failed)) return false;
+                if (!tc::mbar_wait(&w_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) return false;
+                tc::tc_fence_after();
+                const uint32_t ws = w0 + (uint32_t)st * 2 * wbytes;
+                const uint32_t tS = tmem + s_col + (uint32_t)(gi & 1) * NC;
+                for (int k = 0; k < D / 16; k++)
+                    tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(ws + k * 2 * NC * 16, NC * 16, 128),
+                                 idesc_s, k > 0 ? 1u : 0u);
+                tc::mma_commit(&s_full[gi & 1]);
+                if (j == nch - 1) tc::mma_commit(&a_empty);  // the tile's last read of A
+                return true;
+            };
+            bool good = true;
+            for (int gi = 0; gi < 2 && gi < total && good; gi++) good = issue_s(gi);
+            for (int gi = 0; gi < total && good; gi++) {
+                const int st = gi % NS, j = gi % nch, it = gi / nch;
+                if (j == 0 && it >= 2 &&
+                    !tc::mbar_wait(&o_empty[it & 1], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) {
+                    good = false;
+                    break;
+                }
+                if (!tc::mbar_wait(&h_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed)) {
+                    good = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t ws2 = w0 + (uint32_t)st * 2 * wbytes + wbytes;
+                const uint32_t hs = h0 + (uint32_t)(gi & 1) * NC * 256;
+                const uint32_t tO = tmem + (uint32_t)(it & 1) * D;
+                for (int k = 0; k < NC / 16; k++)
+                    tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(ws2 + k * 2 * D * 16, D * 16, 128),
+                                 idesc_o, (j > 0 || k > 0) ? 1u : 0u);
+                tc::mma_commit(&w_empty[st]);
+                tc::mma_commit(&h_empty[gi & 1]);
+                if (j == nch - 1) tc::mma_commit(&o_full[it & 1]);
+                if (gi + 2 < total) good = issue_s(gi + 2);
+            }
+        }
+        __syncwarp();
+    } else if (warp < 11) {
+        // GELU warps
+        const int half = (warp - 3) >> 2;
+        const int r = (warp & 3) * 32 + lane;
+        const int cw = NC / 2;
+        for (int gi = 0; gi < total; gi++) {
+            const int j = gi % nch;
+            const bool s_ready = tc::mbar_wait(&s_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed);
+            const bool h_free = gi < 2 || tc::mbar_wait(&h_empty[gi & 1], (uint32_t)((gi - 2) >> 1) & 1u, err, &failed);
+            if (!__all_sync(0xffffffffu, s_ready && h_free)) break;  // the TMEM load is warp-collective
+            tc::tc_fence_after();
+            const uint32_t ta = lane_addr(tmem + s_col + (uint32_t)(gi & 1) * NC);
+            uint8_t* hb = sH + (size_t)(gi & 1) * NC * 256;
+            for (int c = half * cw; c < (half + 1) * cw; c += 16) {
+                float a[16];
+                tc::tmem_ld16(ta + c, a);
+                const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float4 bv = bb[i];
+                    a[4 * i] = gelu_fast(a[4 * i] + bv.x);
+                    a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
+                    a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
+                    a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
+                }
+                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
+                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
+            }
+            tc::fence_async_shared();
+            tc::tc_fence_before();
+            tc::mbar_arrive(&h_full[gi & 1]);
+        }
+    } else {
+        // epilogue warps: one TMEM lane quarter (32 tile rows) each
+        const int q = warp & 3;
+        float* tile = sEpi + (size_t)q * 32 * D;
+        for (int it = 0; it < my_tiles; it++) {
+            const bool ready = tc::mbar_wait(&o_full[it & 1], (uint32_t)(it >> 1) & 1u, err, &failed);
+            if (!__all_sync(0xffffffffu, ready)) break;
+            tc::tc_fence_after();
+            stage_rows(lane_addr(tmem + (uint32_t)(it & 1) * D), lane, D, 0, D, tile);
+            tc::tc_fence_before();
+            tc::mbar_arrive(&o_empty[it & 1]);
+            __syncwarp();
+            const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + q * 32;
+            rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, 0, 1, 32);
+            __syncwarp();
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
 // 3x3 zero-padded convolution over each instance's grid as an implicit GEMM
 // (cpu.rs:171-205): tile = 8 x 16 positions (M = 128, row r <-> position
 // (y0 + r/8, x0 + r%8)); the halo tile [C/8 planes][18][10][8] is loaded by
@@ -1303,10 +1519,15 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     bn_qkv = (3 * D) % 128 == 0 ? 128 : 3 * D;
     bn_tm = D <= 128 ? D : 64;
     if (F > 1024) throw Error(JC_LIMIT, "the BF16 MLP supports a hidden width of at most 1024");
-    def_tuning_ = Tuning{32, 3, 256};
-    if (!mlp_fits(32, 3)) def_tuning_.ns = 2;
-    if (!mlp_fits(def_tuning_.nc, def_tuning_.ns))
-        throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
+    {
+        int dev = 0;
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&n_sms_, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    }
+    // default: the serial kernel, 64 columns (fits every supported width)
+    def_tuning_ = Tuning{64, 1, 256, 0};
+    if (!mlp_fits(64, 1, 0)) def_tuning_.nc = 32;
+    if (!mlp_fits(def_tuning_.nc, 1, 0)) throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
     for (int l = 0; l < d.L; l++) {
         const std::string p = "blocks." + std::to_string(l) + ".";
         const auto &q = tget(t, p + "q.weight").data, &k = tget(t, p + "k.weight").data, &v = tget(t, p + "v.weight").data;
@@ -1389,6 +1610,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
     set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
+    set_smem(tc_mlp_persistent_kernel, kMlpSmemMax);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
     set_smem(bf_embed_kernel<1>, 100 * 1024);
@@ -1448,10 +1670,12 @@ static size_t mlp_serial_smem(int D, int NC) {
     return std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
 }
 
-bool BF16Path::mlp_fits(int nc, int ns) const {
+bool BF16Path::mlp_fits(int nc, int ns, int form) const {
     if (!(nc == 32 || nc == 64) || dims_F_ % nc) return false;
-    if (ns == 1) return mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
-    return ns >= 2 && ns <= 4 && MlpSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
+    if (form == 0) return ns == 1 && mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
+    if (ns < 2 || ns > 4) return false;
+    if (form == 1) return MlpSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
+    return form == 2 && 2 * dims_D_ + 2 * nc <= 512 && MlpPSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
 }
 
 void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln,
@@ -1460,9 +1684,16 @@ void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tunin
     const int v = tu.nc == 64 ? 1 : 0;
     const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
     const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
-    if (tu.ns == 1) {
+    if (tu.form == 0) {
         tc_mlp_serial_kernel<<<(unsigned)((R + 127) / 128), kMlpSerialThreads, mlp_serial_smem(D, tu.nc), s>>>(
             m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, R, p.x, ng, nbeta,
+            reinterpret_cast<bf16*>(p.bt[0]), p.err);
+        return;
+    }
+    if (tu.form == 2) {
+        const unsigned grid = (unsigned)std::min((R + 127) / 128, n_sms_);
+        tc_mlp_persistent_kernel<<<grid, kMlpPThreads, MlpPSmem(D, d.F, tu.nc, tu.ns).total, s>>>(
+            m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
             reinterpret_cast<bf16*>(p.bt[0]), p.err);
         return;
     }
@@ -1509,19 +1740,23 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     // anything in it (every forward rewrites it from the state)
     std::string log;
     float best_ms = 1e30f;
-    const int cand[][2] = {{32, 1}, {64, 1}, {32, 2}, {32, 3}, {32, 4}, {64, 2}, {64, 3}};
+    // {chunk width, weight stages, form}
+    const int cand[][3] = {{32, 1, 0}, {64, 1, 0}, {32, 2, 1}, {32, 3, 1}, {64, 2, 1}, {64, 3, 1},
+                           {32, 2, 2}, {32, 3, 2}, {32, 4, 2}, {64, 2, 2}};
     for (const auto& c : cand) {
-        if (!mlp_fits(c[0], c[1])) continue;
+        if (!mlp_fits(c[0], c[1], c[2])) continue;
         Tuning t = best;
         t.nc = c[0];
         t.ns = c[1];
+        t.form = c[2];
         const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, 3, s);
-        log += (log.empty() ? "" : ", ") + std::string("\"mlp_") + std::to_string(c[0]) + "x" + std::to_string(c[1]) +
-               "_ms\": " + std::to_string(ms);
+        log += (log.empty() ? "" : ", ") + std::string("\"mlp_f") + std::to_string(c[2]) + "_" + std::to_string(c[0]) +
+               "x" + std::to_string(c[1]) + "_ms\": " + std::to_string(ms);
         if (ms < best_ms) {
             best_ms = ms;
             best.nc = t.nc;
             best.ns = t.ns;
+            best.form = t.form;
         }
     }
     best_ms = 1e30f;
@@ -1543,7 +1778,7 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
 
 // Tuned schedules persist in the JSON-lines file named by JC_AUTOTUNE_CACHE,
 // one object per tuned row bucket:
-//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "nc": 32, "stages": 3, "attn_threads": 256}
+//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "mlp_form": 2, "nc": 32, "stages": 3, "attn_threads": 256}
 // keyed by the model shape (dim, layers, MLP width, mask radius, kind and
 // dilation), followed by the candidates' measured times. Lines that do not
 // parse or name another shape are skipped; later lines override earlier ones.
@@ -1554,12 +1789,14 @@ void BF16Path::load_cache() {
     if (!f) return;
     char line[512], key[128];
     while (std::fgets(line, sizeof line, f)) {
-        int bucket, nc, ns, th;
-        if (std::sscanf(line, " {\"model\": \"%127[^\"]\", \"rows\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": %d",
-                        key, &bucket, &nc, &ns, &th) != 5)
+        int bucket, form, nc, ns, th;
+        if (std::sscanf(line,
+                        " {\"model\": \"%127[^\"]\", \"rows\": %d, \"mlp_form\": %d, \"nc\": %d, \"stages\": %d, "
+                        "\"attn_threads\": %d",
+                        key, &bucket, &form, &nc, &ns, &th) != 6)
             continue;
-        if (cache_key_ == key && mlp_fits(nc, ns) && (th == 64 || th == 128 || th == 256))
-            tuned_[bucket] = Tuning{nc, ns, th};
+        if (cache_key_ == key && mlp_fits(nc, ns, form) && (th == 64 || th == 128 || th == 256))
+            tuned_[bucket] = Tuning{nc, ns, th, form};
     }
     std::fclose(f);
 }
@@ -1570,8 +1807,11 @@ void BF16Path::save_cache(int bucket, const Tuning& t, const std::string& timing
     std::lock_guard<std::mutex> lk(tune_mu_);
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "{\"model\": \"%s\", \"rows\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": %d%s%s}\n",
-                 cache_key_.c_str(), bucket, t.nc, t.ns, t.attn_threads, timings.empty() ? "" : ", ", timings.c_str());
+    std::fprintf(f,
+                 "{\"model\": \"%s\", \"rows\": %d, \"mlp_form\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": "
+                 "%d%s%s}\n",
+                 cache_key_.c_str(), bucket, t.form, t.nc, t.ns, t.attn_threads, timings.empty() ? "" : ", ",
+                 timings.c_str());
     std::fclose(f);
 }
 
