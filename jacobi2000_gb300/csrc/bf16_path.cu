@@ -561,23 +561,57 @@ __device__ __forceinline__ void stage_rows(uint32_t ta, int r, int D, int c0, in
     }
 }
 
-// One warp per tile row: x[row] += acc + bias, then LayerNorm of the new row
-// (two-pass mean and biased variance, eps 1e-5) into `ln` as bf16. Lane l
-// handles float4 slots l + 32 j, so x and ln are read and written coalesced.
-template <int SPL>  // float4 slots per lane: D / 128
-__device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
-                              float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
-                              bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
+// Residual + LayerNorm rows (two-pass mean and biased variance, eps 1e-5),
+// in one fixed arithmetic shared by every kernel that produces them, so the
+// MLP forms give the same bits: every operation is an explicitly rounded
+// one (no compiler contraction), element v = x + (acc + bias); each
+// 4-element slot contributes ((v0 + v1) + (v2 + v3)) and, for the variance,
+// fma(e0, e0, e1 e1) + fma(e2, e2, e3 e3); slot q belongs to lane q % 32, a
+// lane sums its slots in order starting from 0, and the 32 lane partials are
+// added in the xor-butterfly order of warp_sum; out = fma((v - mean) rstd,
+// g, b).
+__device__ __forceinline__ float4 resid4(float4 x, float4 a, float4 bias) {
+    return make_float4(__fadd_rn(x.x, __fadd_rn(a.x, bias.x)), __fadd_rn(x.y, __fadd_rn(a.y, bias.y)),
+                       __fadd_rn(x.z, __fadd_rn(a.z, bias.z)), __fadd_rn(x.w, __fadd_rn(a.w, bias.w)));
+}
+__device__ __forceinline__ float sum4(float4 v) { return __fadd_rn(__fadd_rn(v.x, v.y), __fadd_rn(v.z, v.w)); }
+__device__ __forceinline__ float sqdev4(float4 v, float m) {
+    const float e0 = __fsub_rn(v.x, m), e1 = __fsub_rn(v.y, m), e2 = __fsub_rn(v.z, m), e3 = __fsub_rn(v.w, m);
+    return __fadd_rn(__fmaf_rn(e0, e0, __fmul_rn(e1, e1)), __fmaf_rn(e2, e2, __fmul_rn(e3, e3)));
+}
+__device__ __forceinline__ float ln1(float v, float m, float rstd, float g, float b) {
+    return __fmaf_rn(__fmul_rn(__fsub_rn(v, m), rstd), g, b);
+}
+// The 32 lane partials in the order warp_sum adds them.
+__device__ __forceinline__ float tree32(float* a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < o; i++) a[i] = __fadd_rn(a[i], a[i + o]);
+    return a[0];
+}
+
+// One warp per tile row over the staged accumulator tile (float4 slot q of
+// row r at q ^ slot_swz(r, D)); x and ln are read and written coalesced, G
+// rows in flight per warp. Rows [0, nrows) of the tile (a multiple of G),
+// tile row r -> global row m0 + r. SPL = slots per lane (1: D <= 128, 2: 256).
+template <int SPL, bool FULL>  // FULL: every lane owns SPL slots (D = 128 SPL)
+__device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
+                                float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
+                                bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
     const int lane = threadIdx.x & 31;
+    const int nq = D / 4;
+    const int swz = D >= 128 ? 31 : nq - 1;  // slot_swz mask
+    constexpr int G = 4;
+    auto on = [&](int j) { return FULL || lane + 32 * j < nq; };
     float4 bb[SPL], gg[SPL], be[SPL];
 #pragma unroll
     for (int j = 0; j < SPL; j++) {
-        const int q = lane + 32 * j;
+        const int q = on(j) ? lane + 32 * j : 0;
         bb[j] = reinterpret_cast<const float4*>(bias)[q];
         gg[j] = reinterpret_cast<const float4*>(g)[q];
         be[j] = reinterpret_cast<const float4*>(b)[q];
     }
-    constexpr int G = 4;  // rows in flight per warp
     for (int r0 = warp * G; r0 < nrows; r0 += nwarps * G) {
         float4 a[G][SPL], xv[G][SPL];
 #pragma unroll
@@ -585,8 +619,8 @@ __device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const flo
             const int r = r0 + k, row = m0 + r;
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
-                const int q = lane + 32 * j;
-                a[k][j] = reinterpret_cast<const float4*>(tile + (size_t)r * D)[q ^ (r & 31)];
+                const int q = on(j) ? lane + 32 * j : 0;
+                a[k][j] = reinterpret_cast<const float4*>(tile + (size_t)r * D)[q ^ (r & swz)];
                 xv[k][j] = row < R ? reinterpret_cast<const float4*>(x + (size_t)row * D)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
@@ -598,65 +632,34 @@ __device__ void rows_resid_ln(const float* tile, int D, int m0, int R, const flo
             float s = 0.f;
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
-                v[j] = make_float4(xv[k][j].x + (a[k][j].x + bb[j].x), xv[k][j].y + (a[k][j].y + bb[j].y),
-                                   xv[k][j].z + (a[k][j].z + bb[j].z), xv[k][j].w + (a[k][j].w + bb[j].w));
-                s += (v[j].x + v[j].y) + (v[j].z + v[j].w);
+                v[j] = resid4(xv[k][j], a[k][j], bb[j]);
+                if (on(j)) s = __fadd_rn(s, sum4(v[j]));
             }
             const float mean = warp_sum(s) / (float)D;
             float q2 = 0.f;
 #pragma unroll
-            for (int j = 0; j < SPL; j++) {
-                const float e0 = v[j].x - mean, e1 = v[j].y - mean, e2 = v[j].z - mean, e3 = v[j].w - mean;
-                q2 += (e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3);
-            }
+            for (int j = 0; j < SPL; j++)
+                if (on(j)) q2 = __fadd_rn(q2, sqdev4(v[j], mean));
             const float rstd = 1.0f / sqrtf(warp_sum(q2) / (float)D + 1e-5f);
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
+                if (!on(j)) continue;
                 const int q = lane + 32 * j;
                 reinterpret_cast<float4*>(x + (size_t)row * D)[q] = v[j];
-                float o[4] = {(v[j].x - mean) * rstd * gg[j].x + be[j].x, (v[j].y - mean) * rstd * gg[j].y + be[j].y,
-                              (v[j].z - mean) * rstd * gg[j].z + be[j].z, (v[j].w - mean) * rstd * gg[j].w + be[j].w};
+                float o[4] = {ln1(v[j].x, mean, rstd, gg[j].x, be[j].x), ln1(v[j].y, mean, rstd, gg[j].y, be[j].y),
+                              ln1(v[j].z, mean, rstd, gg[j].z, be[j].z), ln1(v[j].w, mean, rstd, gg[j].w, be[j].w)};
                 BfVec<4>::store(ln + (size_t)row * D + 4 * q, o);
             }
         }
     }
 }
 
-// D-dispatch of rows_resid_ln over the first `nrows` rows of the tile (a
-// multiple of 4; D = 128 SPL 1, 256 SPL 2; D = 32 uses the first 8 lanes of
-// one slot each).
 __device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
                                   const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128) {
-    if (D == 256) rows_resid_ln<2>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
-    else if (D == 128) rows_resid_ln<1>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
-    else {
-        // narrow rows (D = 32): lanes 0..7 each own one float4 slot
-        const int lane = threadIdx.x & 31;
-        for (int r = warp; r < nrows; r += nwarps) {
-            const int row = m0 + r;
-            if (row >= R) break;
-            const bool on = lane < D / 4;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (on) {
-                const float4 a = reinterpret_cast<const float4*>(tile + (size_t)r * D)[lane ^ (r & (D / 4 - 1))];
-                const float4 xv = reinterpret_cast<const float4*>(x + (size_t)row * D)[lane];
-                const float4 bb = reinterpret_cast<const float4*>(bias)[lane];
-                v = make_float4(xv.x + (a.x + bb.x), xv.y + (a.y + bb.y), xv.z + (a.z + bb.z), xv.w + (a.w + bb.w));
-            }
-            const float mean = warp_sum((v.x + v.y) + (v.z + v.w)) / (float)D;
-            float q2 = 0.f;
-            if (on) q2 = (v.x - mean) * (v.x - mean) + (v.y - mean) * (v.y - mean) + (v.z - mean) * (v.z - mean) +
-                         (v.w - mean) * (v.w - mean);
-            const float rstd = 1.0f / sqrtf(warp_sum(q2) / (float)D + 1e-5f);
-            if (on) {
-                const float4 gg = reinterpret_cast<const float4*>(g)[lane], be = reinterpret_cast<const float4*>(b)[lane];
-                reinterpret_cast<float4*>(x + (size_t)row * D)[lane] = v;
-                float o[4] = {(v.x - mean) * rstd * gg.x + be.x, (v.y - mean) * rstd * gg.y + be.y,
-                              (v.z - mean) * rstd * gg.z + be.z, (v.w - mean) * rstd * gg.w + be.w};
-                BfVec<4>::store(ln + (size_t)row * D + 4 * lane, o);
-            }
-        }
-    }
+    if (D == 256) rows_resid_ln_t<2, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else if (D == 128) rows_resid_ln_t<1, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else if (D > 128) rows_resid_ln_t<2, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else rows_resid_ln_t<1, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
 }
 
 enum { EPI_BF16 = 0, EPI_F32 = 1, EPI_RESID_LN = 2 };
@@ -779,6 +782,55 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
+
+// Residual + LayerNorm of tile row r by the thread that owns it (TMEM lane
+// r): v = x + (acc + bias) in place in the f32 row of sX (128-byte swizzled
+// boxes of 32 columns x 128 rows: 16-byte chunk q of row r at box q / 8,
+// chunk (q % 8) ^ (r % 8)), then mean and biased variance over the row (two
+// passes) and LayerNorm(v) as bf16: into swizzled staging boxes of 64
+// columns (sLn) or straight to the global row (lnrow).
+__device__ __forceinline__ float4* xrow_chunk(uint8_t* sX, int r, int q) {
+    return reinterpret_cast<float4*>(sX + (size_t)(q >> 3) * 16384 + (size_t)r * 128 + (((q & 7) ^ (r & 7)) << 4));
+}
+
+__device__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t* sX, const float* sbias, const float* sg,
+                             const float* sb, uint8_t* sLn, bf16* lnrow) {
+    // D <= 128: slot q is lane q's only slot, so lane partial q = 0 + sum4
+    const int nq = D / 4;
+    for (int c = 0; c < D; c += 16) {
+        float a[16];
+        tc::tmem_ld16(ta + c, a);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            float4* p = xrow_chunk(sX, r, (c >> 2) + i);
+            const int o = c + 4 * i;
+            *p = resid4(*p, make_float4(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]),
+                        make_float4(sbias[o], sbias[o + 1], sbias[o + 2], sbias[o + 3]));
+        }
+    }
+    float part[32];
+#pragma unroll
+    for (int l = 0; l < 32; l++) part[l] = l < nq ? __fadd_rn(0.f, sum4(*xrow_chunk(sX, r, l))) : 0.f;
+    const float mean = tree32(part) / (float)D;
+#pragma unroll
+    for (int l = 0; l < 32; l++) part[l] = l < nq ? __fadd_rn(0.f, sqdev4(*xrow_chunk(sX, r, l), mean)) : 0.f;
+    const float rstd = 1.0f / sqrtf(tree32(part) / (float)D + 1e-5f);
+    for (int c = 0; c < D; c += 8) {
+        const float4 v0 = *xrow_chunk(sX, r, c >> 2), v1 = *xrow_chunk(sX, r, (c >> 2) + 1);
+        const float in[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        float o[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) o[i] = ln1(in[i], mean, rstd, sg[c + i], sb[c + i]);
+        if (sLn) {
+            const int j = (c & 63) >> 3;
+            BfVec<8>::store(reinterpret_cast<bf16*>(sLn + (size_t)(c >> 6) * 16384 + (size_t)r * 128 + ((j ^ (r & 7)) << 4)), o);
+        } else if (lnrow) {
+            BfVec<8>::store(lnrow + c, o);
+        }
+    }
+}
+
+constexpr int kLnMaxD = 128;  // widest row the row-per-thread LayerNorm serves
 
 // Fused MLP: x += gelu(LN2(x) @ W1 + b1) @ W2 + b2, then LayerNorm of the new
 // x (the next block's norm1, or the final norm) into `ln`. The hidden layer
@@ -1107,13 +1159,15 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
 //   warp 2      (one lane) issues every MMA: S_g = A @ W1_j into one of two
 //               TMEM S buffers, O += h_g @ W2_j into one of two TMEM O
 //               buffers (one per tile in flight);
-//   warps 3-10  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers);
-//   warps 11-14 stage a finished O buffer (one TMEM lane quarter each),
+//   warps 3-18  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers;
+//               four warps per TMEM lane quarter, 16 columns each);
+//   warps 19-22 stage a finished O buffer (one TMEM lane quarter each),
 //               release it, and run the residual + LayerNorm rows.
 // g counts chunks over all of this CTA's tiles. The arithmetic and its order
 // are those of the other MLP kernels (the same K slices of 16 in the same
 // order), so the result is bit-identical.
-constexpr int kMlpPWarps = 15;
+constexpr int kMlpPGelu = 16;                  // GELU warps (NC = 64: 16 columns each)
+constexpr int kMlpPWarps = 3 + kMlpPGelu + 4;  // + A producer, W producer, MMA issuer; + 4 epilogue
 constexpr int kMlpPThreads = kMlpPWarps * 32;
 
 struct MlpPSmem {
@@ -1123,13 +1177,14 @@ struct MlpPSmem {
         w = a + (size_t)D * 256;                // NS x (W1_j | W2_j)
         h = w + (size_t)NS * 4 * D * NC;        // 2 x [NC/8][128][8]
         b1 = h + (size_t)2 * NC * 256;          // [F] f32
-        epi = (b1 + (size_t)F * 4 + 1023) / 1024 * 1024;  // 4 x [32][D] f32
+        epi = (b1 + (size_t)F * 4 + 1023) / 1024 * 1024;  // x rows: D/32 swizzled boxes of 32 f32 x 128 rows
         total = epi + (size_t)128 * D * 4;
     }
 };
 
 __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
-    const __grid_constant__ CUtensorMap tmA, const bf16* __restrict__ W1, const bf16* __restrict__ W2,
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, const bf16* __restrict__ W1,
+    const bf16* __restrict__ W2,
     const float* __restrict__ b1, const float* __restrict__ b2, int D, int F, int NC, int NS, int R,
     float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b, bf16* __restrict__ ln, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -1138,10 +1193,11 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     uint8_t* sW = smem + L.w;
     uint8_t* sH = smem + L.h;
     float* sb1 = reinterpret_cast<float*>(smem + L.b1);
-    float* sEpi = reinterpret_cast<float*>(smem + L.epi);
+    uint8_t* sX = smem + L.epi;
     constexpr int kMaxStages = 4;
     __shared__ uint64_t a_full, a_empty, w_full[kMaxStages], w_empty[kMaxStages], s_full[2], h_full[2], h_empty[2],
-        o_full[2], o_empty[2];
+        o_full[2], o_empty[2], x_full;
+    __shared__ float sb2[kLnMaxD], sgam[kLnMaxD], sbet[kLnMaxD];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1161,19 +1217,26 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
         }
         for (int i = 0; i < 2; i++) {
             tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&h_full[i], 8 * 32);
+            tc::mbar_init(&h_full[i], kMlpPGelu * 32);
             tc::mbar_init(&h_empty[i], 1);
             tc::mbar_init(&o_full[i], 1);
             tc::mbar_init(&o_empty[i], 4 * 32);
         }
+        tc::mbar_init(&x_full, 1);
         tc::fence_barrier_init();
         failed = 0;
-        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages || ncols > 512) {
+        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages || ncols > 512 || NC != 4 * 16 ||
+            D > kLnMaxD || D % 32) {
             failed = 1;
             atomicExch(err, 2);
         }
     }
     for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
+    for (int i = threadIdx.x; i < D && i < kLnMaxD; i += blockDim.x) {
+        sb2[i] = b2[i];
+        sgam[i] = g[i];
+        sbet[i] = b[i];
+    }
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
@@ -1250,11 +1313,11 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             }
         }
         __syncwarp();
-    } else if (warp < 11) {
+    } else if (warp < 3 + kMlpPGelu) {
         // GELU warps
-        const int half = (warp - 3) >> 2;
+        const int part = (warp - 3) >> 2;  // columns 16 part .. 16 part + 15 of the chunk
         const int r = (warp & 3) * 32 + lane;
-        const int cw = NC / 2;
+        const int cw = 16;
         for (int gi = 0; gi < total; gi++) {
             const int j = gi % nch;
             const bool s_ready = tc::mbar_wait(&s_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed);
@@ -1263,7 +1326,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             tc::tc_fence_after();
             const uint32_t ta = lane_addr(tmem + s_col + (uint32_t)(gi & 1) * NC);
             uint8_t* hb = sH + (size_t)(gi & 1) * NC * 256;
-            for (int c = half * cw; c < (half + 1) * cw; c += 16) {
+            for (int c = part * cw; c < (part + 1) * cw; c += 16) {
                 float a[16];
                 tc::tmem_ld16(ta + c, a);
                 const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
@@ -1283,20 +1346,44 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             tc::mbar_arrive(&h_full[gi & 1]);
         }
     } else {
-        // epilogue warps: one TMEM lane quarter (32 tile rows) each
-        const int q = warp & 3;
-        float* tile = sEpi + (size_t)q * 32 * D;
+        // epilogue warps: thread r owns tile row r (TMEM lane r). The x rows
+        // of the next tile are prefetched by TMA into sX as soon as the
+        // previous tile's x store has read it.
+        const int r = (warp & 3) * 32 + lane;
+        const bool leader = warp == 3 + kMlpPGelu && lane == 0;
+        auto load_x = [&](int it) {
+            const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+            tc::mbar_expect_tx(&x_full, (uint32_t)D * 512);
+            for (int bx = 0; bx < D / 32; bx++) tc::tma_load_2d(sX + bx * 16384, &tmX, bx * 32, m0, &x_full);
+        };
+        if (leader && my_tiles > 0 && !failed) load_x(0);
         for (int it = 0; it < my_tiles; it++) {
-            const bool ready = tc::mbar_wait(&o_full[it & 1], (uint32_t)(it >> 1) & 1u, err, &failed);
-            if (!__all_sync(0xffffffffu, ready)) break;
+            const bool ready = tc::mbar_wait(&o_full[it & 1], (uint32_t)(it >> 1) & 1u, err, &failed) &&
+                               tc::mbar_wait(&x_full, (uint32_t)it & 1u, err, &failed);
+            // one decision for all four epilogue warps (they meet at barrier 1 below)
+            uint32_t all_ready;
+            asm volatile(
+                "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, 1, 128, q;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(all_ready)
+                : "r"(ready ? 1u : 0u)
+                : "memory");
+            if (!all_ready) break;
             tc::tc_fence_after();
-            stage_rows(lane_addr(tmem + (uint32_t)(it & 1) * D), lane, D, 0, D, tile);
+            const int row = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + r;
+            row_resid_ln(lane_addr(tmem + (uint32_t)(it & 1) * D), r, D, sX, sb2, sgam, sbet, nullptr,
+                         row < R ? ln + (size_t)row * D : nullptr);
             tc::tc_fence_before();
             tc::mbar_arrive(&o_empty[it & 1]);
-            __syncwarp();
-            const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + q * 32;
-            rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, 0, 1, 32);
-            __syncwarp();
+            tc::fence_async_shared();
+            asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+            if (leader) {
+                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+                for (int bx = 0; bx < D / 32; bx++) tc::tma_store_2d(&tmX, sX + bx * 16384, bx * 32, m0);
+                tc::bulk_commit();
+                tc::bulk_wait_read();
+                if (it + 1 < my_tiles && !failed) load_x(it + 1);
+            }
         }
     }
     tc::tc_fence_before();
@@ -1675,7 +1762,8 @@ bool BF16Path::mlp_fits(int nc, int ns, int form) const {
     if (form == 0) return ns == 1 && mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
     if (ns < 2 || ns > 4) return false;
     if (form == 1) return MlpSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
-    return form == 2 && 2 * dims_D_ + 2 * nc <= 512 && MlpPSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
+    return form == 2 && nc == 64 && dims_D_ <= kLnMaxD && 2 * dims_D_ + 2 * nc <= 512 &&
+           MlpPSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
 }
 
 void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln,
@@ -1692,8 +1780,9 @@ void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tunin
     }
     if (tu.form == 2) {
         const unsigned grid = (unsigned)std::min((R + 127) / 128, n_sms_);
+        const CUtensorMap m_x = store_map(p.x, D, R, D, true);
         tc_mlp_persistent_kernel<<<grid, kMlpPThreads, MlpPSmem(D, d.F, tu.nc, tu.ns).total, s>>>(
-            m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
+            m_ln, m_x, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
             reinterpret_cast<bf16*>(p.bt[0]), p.err);
         return;
     }
@@ -1741,8 +1830,7 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     std::string log;
     float best_ms = 1e30f;
     // {chunk width, weight stages, form}
-    const int cand[][3] = {{32, 1, 0}, {64, 1, 0}, {32, 2, 1}, {32, 3, 1}, {64, 2, 1}, {64, 3, 1},
-                           {32, 2, 2}, {32, 3, 2}, {32, 4, 2}, {64, 2, 2}};
+    const int cand[][3] = {{32, 1, 0}, {64, 1, 0}, {32, 2, 1}, {32, 3, 1}, {64, 2, 1}, {64, 3, 1}, {64, 2, 2}};
     for (const auto& c : cand) {
         if (!mlp_fits(c[0], c[1], c[2])) continue;
         Tuning t = best;

@@ -57,8 +57,7 @@ def test_every_schedule_gives_identical_results(tmp_path, monkeypatch, dim):
         cache = tmp_path / "tune.txt"
         monkeypatch.setenv("JC_AUTOTUNE_CACHE", str(cache))
         engine.autotune(True)
-        mlp = [(0, 32, 1), (0, 64, 1), (1, 32, 2), (1, 32, 3), (1, 64, 2), (1, 64, 3), (2, 32, 2), (2, 32, 3),
-               (2, 32, 4), (2, 64, 2)]
+        mlp = [(0, 32, 1), (0, 64, 1), (1, 32, 2), (1, 32, 3), (1, 64, 2), (1, 64, 3), (2, 64, 2)]
         scheds = [m + (256,) for m in mlp] + [(0, 64, 1, 64), (0, 64, 1, 128)]
         for form, nc, ns, threads in scheds:
             # a cache file written beforehand fixes the schedule of every row bucket
