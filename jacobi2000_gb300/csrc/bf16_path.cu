@@ -122,6 +122,15 @@ static CUtensorMap tile_store_map(const void* base, int C, int nx, int ny, bool 
                     CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+// One instance's qkv rows as a [ty, tx, 3D] grid, loaded as 64-channel boxes
+// of side x side tokens in the 128-byte swizzled layout (attention tiles).
+static CUtensorMap att_map(const void* base, int D, int tx, int ty, int side) {
+    uint64_t dims[3] = {(uint64_t)(3 * D), (uint64_t)tx, (uint64_t)ty};
+    uint64_t strides[2] = {(uint64_t)3 * D * 2, (uint64_t)tx * 3 * D * 2};
+    uint32_t box[3] = {64, (uint32_t)side, (uint32_t)side};
+    return make_map(base, 3, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
 // One instance's [ny, nx, C] channel-last grid, loaded as 8-channel x 10 x 18 halo boxes.
 static CUtensorMap halo_map(const void* base, int C, int nx, int ny) {
     uint64_t dims[3] = {(uint64_t)C, (uint64_t)nx, (uint64_t)ny};
@@ -454,6 +463,165 @@ __global__ void __launch_bounds__(256) bf_attn_head_kernel(Dims d, const bf16* _
 #pragma unroll
     for (int i = 0; i < HD; i++) acc[i] *= inv;
     store_head<HD>(out + (size_t)r * D + h * HD, acc);
+}
+
+// Radius-1, dilation-1 stencil attention over shared-memory tiles (cpu.rs:
+// 97-164, mask.rs:18-30). A CTA takes one 8 x 8 block of an instance's token
+// grid (half of an 8 x 16 conv tile): TMA brings the block's queries and the
+// keys and values of its 10 x 10 halo into shared memory as 128-byte
+// swizzled boxes (64 channels each; zero fill outside the grid, where the
+// mask excludes the candidates anyway). Thread (token, head) then does the
+// arithmetic of bf_attn_head_r1_kernel, in the same order, on shared-memory
+// operands: the eight lanes of a quarter warp are eight neighbouring tokens
+// of one head, so the swizzle spreads their 16-byte reads over all banks.
+constexpr int kAttTile = 8;                        // tokens per side of a CTA's block
+constexpr int kAttHalo = kAttTile + 2;             // halo side
+constexpr int kAttBoxKV = kAttHalo * kAttHalo * 128;   // one 64-channel halo box: 12800 bytes
+constexpr int kAttBoxKVPad = 13 * 1024;                // 1024-aligned slot of one halo box
+constexpr int kAttBoxQ = kAttTile * kAttTile * 128;    // one 64-channel query box: 8192 bytes
+
+// 16-byte chunk c (0..7) of row rho of a 128-byte swizzled box
+__device__ __forceinline__ const uint4* swz_chunk(const uint8_t* box, int rho, int c) {
+    return reinterpret_cast<const uint4*>(box + (size_t)rho * 128 + ((c ^ (rho & 7)) << 4));
+}
+
+template <int HD>
+__device__ __forceinline__ void load_head_s(const uint8_t* boxes, int box_stride, int rho, int ch0, float* f) {
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const int ch = ch0 + 8 * w;
+        const uint4 u = *swz_chunk(boxes + (size_t)(ch >> 6) * box_stride, rho, (ch & 63) >> 3);
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            f[8 * w + 2 * i] = __uint_as_float(a[i] << 16);
+            f[8 * w + 2 * i + 1] = __uint_as_float(a[i] & 0xffff0000u);
+        }
+    }
+}
+
+template <int HD>
+__device__ __forceinline__ float dot_head_s(const float* q, const uint8_t* boxes, int box_stride, int rho, int ch0) {
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const int ch = ch0 + 8 * w;
+        const uint4 u = *swz_chunk(boxes + (size_t)(ch >> 6) * box_stride, rho, (ch & 63) >> 3);
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            p0 = fmaf(q[8 * w + 2 * i], __uint_as_float(a[i] << 16), p0);
+            p1 = fmaf(q[8 * w + 2 * i + 1], __uint_as_float(a[i] & 0xffff0000u), p1);
+        }
+    }
+    return p0 + p1;
+}
+
+template <int HD>
+__device__ __forceinline__ void axpy_head_s(float wgt, const uint8_t* boxes, int box_stride, int rho, int ch0,
+                                            float* acc) {
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const int ch = ch0 + 8 * w;
+        const uint4 u = *swz_chunk(boxes + (size_t)(ch >> 6) * box_stride, rho, (ch & 63) >> 3);
+        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            acc[8 * w + 2 * i] = fmaf(wgt, __uint_as_float(a[i] << 16), acc[8 * w + 2 * i]);
+            acc[8 * w + 2 * i + 1] = fmaf(wgt, __uint_as_float(a[i] & 0xffff0000u), acc[8 * w + 2 * i + 1]);
+        }
+    }
+}
+
+// Maps of an instance used here: slot kv_slot = halo boxes (64 ch x 10 x 10)
+// over its qkv rows, slot q_slot = query boxes (64 ch x 8 x 8) over the same
+// rows. D = 64 * (boxes per vector); threads = 64 tokens x heads.
+template <int HD>
+__global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtensorMap* __restrict__ maps, int kv_slot,
+                                                           int q_slot, const InstDev* inst, int n_inst,
+                                                           bf16* __restrict__ out, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int D = d.D, nb = D / 64;  // 64-channel boxes per vector
+    uint8_t* sK = smem;                                   // nb halo boxes of the keys
+    uint8_t* sV = sK + (size_t)nb * kAttBoxKVPad;         // nb halo boxes of the values
+    uint8_t* sQ = sV + (size_t)nb * kAttBoxKVPad;         // nb query boxes
+    __shared__ uint64_t bar;
+    __shared__ volatile int failed;
+    const int tile = blockIdx.x, half = blockIdx.y;
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].tt0 <= tile) lo = mid; else hi = mid - 1;
+    }
+    const InstDev& I = inst[lo];
+    const int tiles_x = (I.tx + kConvTX - 1) / kConvTX;
+    const int tl = tile - I.tt0;
+    const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY + half * kAttTile;
+    const CUtensorMap* mkv = maps + kMapsPerInst * lo + kv_slot;
+    const CUtensorMap* mq = maps + kMapsPerInst * lo + q_slot;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_barrier_init();
+        failed = 0;
+        if (tc::smem_u32(smem) & 1023u) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    __syncthreads();
+    if (y0 >= I.ty) return;  // the lower half of a tile that overhangs the grid (uniform per CTA)
+    if (threadIdx.x == 0 && !failed) {
+        tc::tensormap_acquire(mkv);
+        tc::tensormap_acquire(mq);
+        tc::mbar_expect_tx(&bar, (uint32_t)nb * (2 * kAttBoxKV + kAttBoxQ));
+        for (int b = 0; b < nb; b++) {
+            tc::tma_load_3d(sK + (size_t)b * kAttBoxKVPad, mkv, D + 64 * b, x0 - 1, y0 - 1, &bar);
+            tc::tma_load_3d(sV + (size_t)b * kAttBoxKVPad, mkv, 2 * D + 64 * b, x0 - 1, y0 - 1, &bar);
+            tc::tma_load_3d(sQ + (size_t)b * kAttBoxQ, mq, 64 * b, x0, y0, &bar);
+        }
+    }
+    const bool ok = __syncthreads_and(tc::mbar_wait(&bar, 0, err, &failed) ? 1 : 0) != 0;
+    if (!ok) return;
+    const int heads = d.heads;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int h = warp % heads;
+    const int tok = (warp / heads) * 32 + lane;  // 0..63 within the block
+    if (tok >= kAttTile * kAttTile) return;
+    const int lx = tok & 7, ly = tok >> 3;
+    const int qx = x0 + lx, qy = y0 + ly;
+    if (qx >= I.tx || qy >= I.ty) return;
+    const float scale = 1.0f / sqrtf((float)HD);
+    float q[HD];
+    load_head_s<HD>(sQ, kAttBoxQ, ly * kAttTile + lx, h * HD, q);
+    float sc[9];
+    bool in[9];
+    float smax = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int dy = j / 3 - 1, dx = j % 3 - 1;
+        const int ky = qy + dy, kx = qx + dx;
+        in[j] = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
+        const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
+        sc[j] = in[j] ? dot_head_s<HD>(q, sK, kAttBoxKVPad, rho, h * HD) * scale : -INFINITY;
+        smax = fmaxf(smax, sc[j]);
+    }
+    float denom = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        sc[j] = in[j] ? __expf(sc[j] - smax) : 0.f;
+        denom += sc[j];
+    }
+    const float inv = 1.0f / denom;
+    float acc[HD];
+#pragma unroll
+    for (int i = 0; i < HD; i++) acc[i] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int dy = j / 3 - 1, dx = j % 3 - 1;
+        const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
+        if (in[j]) axpy_head_s<HD>(sc[j] * inv, sV, kAttBoxKVPad, rho, h * HD, acc);
+    }
+    store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
 }
 
 // z0 (f32 [rows, HD]) -> zc (bf16 [cells, 48]): upsample along y then x
@@ -1598,6 +1766,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     const int D = d.D, F = d.F, HD = d.HD;
     dims_D_ = D;
     dims_F_ = F;
+    dims_ = d;
     if (D % 32 || D > 256 || 32 % d.heads || F % 64 || HD != 32 || d.C != 3 || d.P != 4 || d.C * d.P * d.P > 64)
         throw Error(JC_LIMIT,
                     "the BF16 path needs dim a multiple of 32 and <= 256, heads dividing 32, a cell-head width of 32, "
@@ -1615,6 +1784,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     def_tuning_ = Tuning{64, 1, 256, 0};
     if (!mlp_fits(64, 1, 0)) def_tuning_.nc = 32;
     if (!mlp_fits(def_tuning_.nc, 1, 0)) throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
+    if (attn_tile_ok(d)) def_tuning_.attn_threads = 0;  // shared-memory attention tiles
     for (int l = 0; l < d.L; l++) {
         const std::string p = "blocks." + std::to_string(l) + ".";
         const auto &q = tget(t, p + "q.weight").data, &k = tget(t, p + "k.weight").data, &v = tget(t, p + "v.weight").data;
@@ -1697,6 +1867,8 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
     set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
+    set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
+    set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
     set_smem(tc_mlp_persistent_kernel, kMlpSmemMax);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
@@ -1712,8 +1884,24 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
 
 // One thread per (token row, head) in CTAs of `threads` threads (64, 128 or
 // 256; the arithmetic of a thread does not depend on it).
+static bool attn_tile_ok(const Dims& d) {
+    return d.mask_kind == 1 && d.radius == 1 && d.dilation == 1 && d.D % 64 == 0 && d.heads <= 4 &&
+           (d.D / d.heads == 32 || d.D / d.heads == 64);
+}
+static size_t attn_tile_smem(const Dims& d) { return (size_t)(d.D / 64) * (2 * kAttBoxKVPad + kAttBoxQ); }
+
 static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
-                             int threads, cudaStream_t s) {
+                             int threads, cudaStream_t s, const Pack* p = nullptr) {
+    if (threads == 0) {
+        // shared-memory tiles: grid (8 x 16 token tiles, their two 8 x 8 halves)
+        const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
+        const dim3 grid((unsigned)p->n_ttiles, 2);
+        if (d.D / d.heads == 32)
+            bf_attn_tile_kernel<32><<<grid, 64 * d.heads, attn_tile_smem(d), s>>>(d, maps, 4, 5, inst, n, attn, p->err);
+        else
+            bf_attn_tile_kernel<64><<<grid, 64 * d.heads, attn_tile_smem(d), s>>>(d, maps, 4, 5, inst, n, attn, p->err);
+        return;
+    }
     const bool r1 = d.mask_kind == 1 && d.radius == 1;
     const int hd = d.D / d.heads;
     const unsigned blocks = (unsigned)(((long long)R * d.heads + threads - 1) / threads);
@@ -1848,8 +2036,10 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
         }
     }
     best_ms = 1e30f;
-    for (int threads : {64, 128, 256}) {
-        const float ms = time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s); }, 3, s);
+    for (int threads : {0, 64, 128, 256}) {
+        if (threads == 0 && !attn_tile_ok(d)) continue;
+        const float ms =
+            time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s, &p); }, 3, s);
         log += ", \"attn_" + std::to_string(threads) + "_ms\": " + std::to_string(ms);
         if (ms < best_ms) {
             best_ms = ms;
@@ -1883,7 +2073,8 @@ void BF16Path::load_cache() {
                         "\"attn_threads\": %d",
                         key, &bucket, &form, &nc, &ns, &th) != 6)
             continue;
-        if (cache_key_ == key && mlp_fits(nc, ns, form) && (th == 64 || th == 128 || th == 256))
+        if (cache_key_ == key && mlp_fits(nc, ns, form) &&
+            (th == 64 || th == 128 || th == 256 || (th == 0 && attn_tile_ok(dims_))))
             tuned_[bucket] = Tuning{nc, ns, th, form};
     }
     std::fclose(f);
@@ -1926,6 +2117,10 @@ void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaS
         m[1] = halo_map(p.bc[0] + (size_t)I.cell0 * p.bc_stride[0], kZcCh, I.nx, I.ny);
         m[2] = tile_store_map(p.bt[3] + (size_t)I.row0 * p.bt_stride[3], d.D, I.tx, I.ty, false);
         m[3] = tile_store_map(p.bc[1] + (size_t)I.cell0 * p.bc_stride[1], d.HD, I.nx, I.ny, true);
+        if (attn_tile_ok(d)) {
+            m[4] = att_map(p.bt[1] + (size_t)I.row0 * p.bt_stride[1], d.D, I.tx, I.ty, kAttHalo);
+            m[5] = att_map(p.bt[1] + (size_t)I.row0 * p.bt_stride[1], d.D, I.tx, I.ty, kAttTile);
+        }
     }
     // synchronous: the host vector is released on return
     cuda_check(cudaMemcpyAsync(p.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s),
@@ -1975,7 +2170,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         }
         {
             KScope k("bf_attention", s);
-            launch_attention(d, qkv, p.inst, n, R, attn, tu.attn_threads, s);
+            launch_attention(d, qkv, p.inst, n, R, attn, tu.attn_threads, s, &p);
             check_launch("bf_attention");
         }
         {

@@ -21,13 +21,14 @@ namespace jc {
 struct Tuning {
     int nc;            // 32 or 64 hidden columns per MLP step
     int ns;            // MLP weight-ring stages (2-4; 1 for the serial form)
-    int attn_threads;  // 64, 128 or 256 threads per attention CTA
+    int attn_threads;  // 64, 128 or 256 threads per attention CTA; 0 = shared-memory tiles
     int form;          // MLP kernel: 0 serial, 1 pipelined per tile, 2 persistent
 };
 
 // 1 (default; environment JC_AUTOTUNE=0 turns it off): BF16 launches time the
 // candidate schedules once per row-count bucket and keep the fastest; 0: the
-// fixed default schedule {serial MLP, nc 64, 256 attention threads}.
+// fixed default schedule {serial MLP, nc 64; shared-memory attention tiles
+// where they apply, else 256 attention threads}.
 extern std::atomic<int> g_autotune;
 
 class BF16Path {
@@ -58,6 +59,7 @@ class BF16Path {
    private:
     static constexpr size_t kMlpSmemMax = 200 * 1024;
     int dims_D_ = 0, dims_F_ = 0;
+    Dims dims_{};
     Tuning def_tuning_{64, 1, 256, 0};
     int n_sms_ = 1;
     bool mlp_fits(int nc, int ns, int form) const;

@@ -13,7 +13,7 @@
 namespace jc {
 
 constexpr int kMaxLayers = 32;
-constexpr int kMapsPerInst = 4;  // BF16 path: ln halo, zc halo, t1 store, c1 store
+constexpr int kMapsPerInst = 6;  // BF16 path: ln halo, zc halo, t1 store, c1 store, qkv halo, q block
 constexpr int kZcStride = 36;  // channel-last stride of the cell-head input: 32 z + 3 state + 1 zero
 
 // Model hyper-parameters shared by every instance of a launch.
