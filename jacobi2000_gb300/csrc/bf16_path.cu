@@ -1730,6 +1730,14 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// Whether the shared-memory attention tiles apply (radius-1, dilation-1
+// stencil; 64-channel boxes; at most 4 heads of width 32 or 64).
+static bool attn_tile_ok(const Dims& d) {
+    return d.mask_kind == 1 && d.radius == 1 && d.dilation == 1 && d.D % 64 == 0 && d.heads <= 4 &&
+           (d.D / d.heads == 32 || d.D / d.heads == 64);
+}
+static size_t attn_tile_smem(const Dims& d) { return (size_t)(d.D / 64) * (2 * kAttBoxKVPad + kAttBoxQ); }
+
 // ---------------------------------------------------------------------------
 // host
 
@@ -1884,11 +1892,6 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
 
 // One thread per (token row, head) in CTAs of `threads` threads (64, 128 or
 // 256; the arithmetic of a thread does not depend on it).
-static bool attn_tile_ok(const Dims& d) {
-    return d.mask_kind == 1 && d.radius == 1 && d.dilation == 1 && d.D % 64 == 0 && d.heads <= 4 &&
-           (d.D / d.heads == 32 || d.D / d.heads == 64);
-}
-static size_t attn_tile_smem(const Dims& d) { return (size_t)(d.D / 64) * (2 * kAttBoxKVPad + kAttBoxQ); }
 
 static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
                              int threads, cudaStream_t s, const Pack* p = nullptr) {
