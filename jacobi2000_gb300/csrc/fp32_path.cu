@@ -376,6 +376,32 @@ __device__ double block_sum_d(double v, double* red) {
     return r;
 }
 
+// Two block-wide f64 sums at once, each in the order of block_sum_d.
+__device__ void block_sum_d2(double& a, double& b, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    a = warp_sum_d(a);
+    b = warp_sum_d(b);
+    __syncthreads();
+    if (lane == 0) {
+        red[warp] = a;
+        red[32 + warp] = b;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double ta = lane < nw ? red[lane] : 0.0, tb = lane < nw ? red[32 + lane] : 0.0;
+        ta = warp_sum_d(ta);
+        tb = warp_sum_d(tb);
+        if (lane == 0) {
+            red[0] = ta;
+            red[32] = tb;
+        }
+    }
+    __syncthreads();
+    a = red[0];
+    b = red[32];
+    __syncthreads();
+}
+
 // Mass then energy projection (eval.rs:148-153 order; project.rs:33-54). One
 // thread-block cluster of kProjCluster CTAs per instance; each CTA keeps its
 // slice of the state in shared memory (when it fits) for the three passes:
@@ -389,7 +415,7 @@ __device__ double block_sum_d(double v, double* red) {
 // every CTA and every run sees the same totals. f64 is used only for these
 // combinations (the FP64 rate of this GPU is a small fraction of its FP32
 // rate, so per-cell f64 arithmetic would dominate the kernel).
-constexpr int kProjCluster = 8;
+constexpr int kProjCluster = 8;  // largest cluster (the launch picks 1..8 CTAs per instance)
 constexpr int kProjThreads = 512;
 constexpr int kProjSmemCells = 16384;  // 192 KB of state per CTA at most
 
@@ -414,93 +440,119 @@ struct Kahan {
     __device__ __forceinline__ double val() const { return (double)s - (double)c; }
 };
 
-// Sum of the cluster's per-CTA partials, in rank order: thread r reads rank
-// r's values through distributed shared memory, thread 0 adds them in order.
-__device__ void cluster_total(cg::cluster_group& cluster, double* mine, const double* local, int nv, double* out) {
-    __shared__ double gathered[kProjCluster][4];
-    if (threadIdx.x < nv) mine[threadIdx.x] = local[threadIdx.x];
+// Reduction segments: an instance's cells are cut into segments of
+// kProjSeg cells; a segment's sums are always formed the same way (thread t
+// takes cells t, t + 512, ... with f32 Kahan compensation, then the fixed
+// block tree in f64), and the instance total adds the segment totals in
+// segment order. A CTA of the cluster owns a contiguous run of segments, so
+// the totals do not depend on the cluster size the launch picked, nor on the
+// other instances of the launch.
+constexpr int kProjSeg = 4096;
+
+// Instance totals of nv (<= 2) values from this CTA's per-segment totals
+// mine[k][v] (k < nk): thread 0 reads every rank's segments through
+// distributed shared memory and adds them in segment order.
+__device__ void cluster_total(cg::cluster_group& cluster, double* mine, int nv, double* out) {
+    const int cs = (int)cluster.num_blocks();
     cluster.sync();
-    if (threadIdx.x < kProjCluster) {
-        const double* peer = cluster.map_shared_rank(mine, (int)threadIdx.x);
-        for (int v = 0; v < nv; v++) gathered[threadIdx.x][v] = peer[v];
-    }
-    __syncthreads();
     if (threadIdx.x == 0) {
-        for (int v = 0; v < nv; v++) {
-            double t = 0.0;
-            for (int r = 0; r < kProjCluster; r++) t += gathered[r][v];
-            out[v] = t;
+        double t[2] = {0.0, 0.0};
+        for (int r = 0; r < cs; r++) {
+            const double* peer = cs == 1 ? mine : cluster.map_shared_rank(mine, r);
+            const int nk = (int)peer[0];  // slot 0 holds the segment count
+            for (int k = 0; k < nk; k++)
+                for (int v = 0; v < nv; v++) t[v] += peer[1 + 2 * k + v];
         }
+        for (int v = 0; v < nv; v++) out[v] = t[v];
     }
     __syncthreads();
 }
 
-__global__ void __cluster_dims__(kProjCluster, 1, 1) __launch_bounds__(kProjThreads)
-projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int cap) {
-    extern __shared__ float sst[];  // [3][cap]: this CTA's slice when it fits
-    __shared__ double red[32];
-    __shared__ double part[3][4];   // per-phase partials, read by the other CTAs of the cluster
+__global__ void __launch_bounds__(kProjThreads)
+projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int cap, int seg_cap) {
+    // [3][cap] f32: this CTA's cells when they fit; then 3 x (1 + 2 seg_cap)
+    // f64: per pass, the segment count and this CTA's segment totals
+    extern __shared__ __align__(16) float sst[];
+    __shared__ double red[64];
     __shared__ double tot[4];
-    __shared__ double local[4];
     cg::cluster_group cluster = cg::this_cluster();
-    const int ii = blockIdx.x / kProjCluster, rank = (int)cluster.block_rank();
+    const int cs = (int)cluster.num_blocks();
+    const int ii = blockIdx.x / cs, rank = (int)cluster.block_rank();
     const InstDev& I = inst[ii];
-    if (I.flags & 4u) return;  // no projection and no energy record for this instance
+    if (I.flags & 4u) return;  // no projection and no energy record for this instance (the whole cluster)
     ProjSlot& S = I.slot ? *I.slot : slots[ii];
     float* s = I.state;
     const unsigned flags = init ? 0u : I.flags;
     const long long n = (long long)I.nx * I.ny;
-    const long long c0 = n * rank / kProjCluster, c1 = n * (rank + 1) / kProjCluster;
-    const int m = (int)(c1 - c0);
+    const int nseg = (int)((n + kProjSeg - 1) / kProjSeg);
+    const int k0 = (int)((long long)nseg * rank / cs), k1 = (int)((long long)nseg * (rank + 1) / cs);
+    const long long c0 = (long long)k0 * kProjSeg, c1 = std::min<long long>((long long)k1 * kProjSeg, n);
+    const int m = (int)(c1 > c0 ? c1 - c0 : 0);
     const bool staged = m <= cap;
+    double* segs = reinterpret_cast<double*>(sst + 3 * (size_t)cap);  // [3][1 + 2 seg_cap]
     // this CTA's cells, in shared memory if they fit, else in place
     float* H = staged ? sst : s + c0;
     float* U = staged ? sst + cap : s + n + c0;
     float* V = staged ? sst + 2 * cap : s + 2 * n + c0;
     if (staged) {
+        // asynchronous copies: every thread's loads are in flight at once
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            H[i] = s[c0 + i];
-            U[i] = s[n + c0 + i];
-            V[i] = s[2 * n + c0 + i];
+            cp_async4(H + i, s + c0 + i, true);
+            cp_async4(U + i, s + n + c0 + i, true);
+            cp_async4(V + i, s + 2 * n + c0 + i, true);
         }
+        cp_async_wait_all();
         __syncthreads();
     }
+    // per-segment sums of term(i) -> (a, b) over this CTA's segments, into
+    // pass slot `ps`, then the instance totals
+    auto reduce = [&](int ps, int nv, auto&& term) {
+        double* mine = segs + (size_t)ps * (1 + 2 * seg_cap);
+        if (threadIdx.x == 0) mine[0] = (double)(k1 - k0);
+        for (int k = k0; k < k1; k++) {
+            Kahan a, b;
+            a.init();
+            b.init();
+            const int base = (k - k0) * kProjSeg;
+            for (int j = threadIdx.x; j < kProjSeg; j += blockDim.x) {
+                const int i = base + j;
+                if (i < m) {
+                    float ta, tb;
+                    term(i, ta, tb);
+                    a.add(ta);
+                    if (nv > 1) b.add(tb);
+                }
+            }
+            double A = a.val(), B = b.val();
+            block_sum_d2(A, B, red);
+            if (threadIdx.x == 0) {
+                mine[1 + 2 * (k - k0)] = A;
+                mine[2 + 2 * (k - k0)] = B;
+            }
+        }
+        __syncthreads();
+        cluster_total(cluster, mine, nv, tot);
+    };
     const double prev = S.energy;
     // pass 1: mass
     double M = 0.0;
     if (init || (flags & 1u)) {
-        Kahan a;
-        a.init();
-        for (int i = threadIdx.x; i < m; i += blockDim.x) a.add(H[i]);
-        if (threadIdx.x == 0) local[0] = 0.0;
-        double blk = block_sum_d(a.val(), red);
-        if (threadIdx.x == 0) local[0] = blk;
-        __syncthreads();
-        cluster_total(cluster, part[0], local, 1, tot);
+        reduce(0, 1, [&](int i, float& a, float& b) {
+            a = H[i];
+            b = 0.f;
+        });
         M = tot[0];
     }
     // pass 2: mass shift, then potential and kinetic energy
-    {
-        const float delta = (flags & 1u) ? (float)(S.mass0 - M / (double)n) : 0.0f;
-        Kahan p, k;
-        p.init();
-        k.init();
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            float h = H[i];
-            if (flags & 1u) {
-                h = __fadd_rn(h, delta);
-                H[i] = h;
-            }
-            float pot, kin;
-            pk_terms(d, h, U[i], V[i], pot, kin);
-            p.add(pot);
-            k.add(kin);
+    const float delta = (flags & 1u) ? (float)(S.mass0 - M / (double)n) : 0.0f;
+    reduce(1, 2, [&](int i, float& pot, float& kin) {
+        float h = H[i];
+        if (flags & 1u) {
+            h = __fadd_rn(h, delta);
+            H[i] = h;
         }
-        double P = block_sum_d(p.val(), red), K = block_sum_d(k.val(), red);
-        if (threadIdx.x == 0) { local[0] = P; local[1] = K; }
-        __syncthreads();
-        cluster_total(cluster, part[1], local, 2, tot);
-    }
+        pk_terms(d, h, U[i], V[i], pot, kin);
+    });
     double P = tot[0], K = tot[1];
     if (init) {
         if (rank == 0 && threadIdx.x == 0) {
@@ -518,25 +570,15 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
             double sc = sqrt(budget / (K > 1e-12 ? K : 1e-12));
             sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
             const float s32 = (float)sc;
-            Kahan p, k;
-            p.init();
-            k.init();
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            reduce(2, 2, [&](int i, float& pot, float& kin) {
                 float u = __fadd_rn(__fmul_rn(U[i], d.norm_std[1]), d.norm_mean[1]);
                 float v = __fadd_rn(__fmul_rn(V[i], d.norm_std[2]), d.norm_mean[2]);
                 u = __fdiv_rn(__fsub_rn(__fmul_rn(u, s32), d.norm_mean[1]), d.norm_std[1]);
                 v = __fdiv_rn(__fsub_rn(__fmul_rn(v, s32), d.norm_mean[2]), d.norm_std[2]);
                 U[i] = u;
                 V[i] = v;
-                float pot, kin;
                 pk_terms(d, H[i], u, v, pot, kin);
-                p.add(pot);
-                k.add(kin);
-            }
-            double P2 = block_sum_d(p.val(), red), K2 = block_sum_d(k.val(), red);
-            if (threadIdx.x == 0) { local[0] = P2; local[1] = K2; }
-            __syncthreads();
-            cluster_total(cluster, part[2], local, 2, tot);
+            });
             P = tot[0];
             K = tot[1];
             if (rank == 0 && threadIdx.x == 0) S.last_scale = sc;
@@ -558,7 +600,7 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
             }
         }
     }
-    cluster.sync();  // peers may still read this CTA's partials
+    cluster.sync();  // peers may still read this CTA's segment totals
 }
 
 }  // namespace f32k
@@ -635,14 +677,34 @@ void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cuda_check_attr(cudaFuncSetAttribute(f32k::projection_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             3 * f32k::kProjSmemCells * 4));
+                                             200 * 1024));
         attr = true;
     }
-    // shared memory for the largest slice of this launch, up to the cap
-    const long long slice = (p.max_inst_cells + f32k::kProjCluster - 1) / f32k::kProjCluster;
-    const int cap = (int)std::min<long long>(std::max<long long>(slice, 1), f32k::kProjSmemCells);
-    f32k::projection_kernel<<<p.n_inst * f32k::kProjCluster, f32k::kProjThreads, (size_t)3 * cap * 4, s>>>(
-        d, p.inst, p.proj, init, cap);
+    // cluster size: the smallest whose slices fit in shared memory, and about
+    // one CTA per SM (152 here) when the instances are few; the sums do not
+    // depend on it (segment totals in segment order)
+    const long long nseg = (p.max_inst_cells + f32k::kProjSeg - 1) / f32k::kProjSeg;
+    int cs = 1;
+    while (cs < f32k::kProjCluster && (nseg + cs - 1) / cs * f32k::kProjSeg > f32k::kProjSmemCells) cs *= 2;
+    while (cs < f32k::kProjCluster && (long long)p.n_inst * cs < 152 && nseg >= 2LL * cs) cs *= 2;
+    const long long seg_cap = (nseg + cs - 1) / cs;
+    // staged in shared memory when a CTA's cells fit, else passes run in place
+    const int cap = seg_cap * f32k::kProjSeg <= f32k::kProjSmemCells ? (int)(seg_cap * f32k::kProjSeg) : 1;
+    const size_t smem = (size_t)3 * cap * 4 + (size_t)3 * (1 + 2 * seg_cap) * 8;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(p.n_inst * cs));
+    cfg.blockDim = dim3(f32k::kProjThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute cl[1];
+    cl[0].id = cudaLaunchAttributeClusterDimension;
+    cl[0].val.clusterDim.x = (unsigned)cs;
+    cl[0].val.clusterDim.y = 1;
+    cl[0].val.clusterDim.z = 1;
+    cfg.attrs = cl;
+    cfg.numAttrs = 1;
+    cuda_check_attr(
+        cudaLaunchKernelEx(&cfg, f32k::projection_kernel, d, (const InstDev*)p.inst, p.proj, init, cap, (int)seg_cap));
     check_launch("projection");
 }
 
