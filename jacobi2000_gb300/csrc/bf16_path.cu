@@ -1730,6 +1730,181 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// Persistent form of conv1 (cpu.rs:343-346: 3x3 conv of the cell-head input,
+// then GELU): one CTA walks cell tiles tile = blockIdx.x + k gridDim.x with
+// its stages on separate warps, so the halo loads, the MMAs and the epilogue
+// of consecutive tiles overlap:
+//   warp 0     (one lane) TMA-loads each tile's halo into one of two slots;
+//   warp 1     (one lane) issues the 9 taps x C/16 MMAs of a tile into one of
+//              two TMEM accumulators (all nine taps' weights stay resident);
+//   warps 2-5  (one TMEM lane quarter each) add the bias, apply GELU, stage
+//              the f32 tile in one of two 128-byte swizzled boxes and store
+//              it with TMA.
+// The MMA order and the epilogue arithmetic are those of tc_conv3_kernel, so
+// the output is bit-identical.
+constexpr int kC1PThreads = 6 * 32;
+
+struct C1PSmem {
+    size_t halo, w, stage, total;
+    __host__ __device__ C1PSmem(int C, int BN) {
+        halo = 0;                                                  // 2 x [C/8][18][10][8]
+        w = halo + 2 * (size_t)(C / 8) * kHaloPlane;               // 9 x [C/8][BN][8]
+        stage = (w + (size_t)9 * C * BN * 2 + 1023) / 1024 * 1024;  // 2 x 16 KB boxes
+        total = stage + 2 * 16384;
+    }
+};
+
+__global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const CUtensorMap* __restrict__ maps,
+                                                                           const bf16* __restrict__ Wt,
+                                                                           const float* __restrict__ bias, int C,
+                                                                           int n_tiles, const InstDev* inst,
+                                                                           int n_inst, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr int BN = 32;  // conv1 outputs: one 128-byte f32 box row per position
+    const C1PSmem L(C, BN);
+    uint8_t* sHalo = smem + L.halo;
+    uint8_t* sW = smem + L.w;
+    uint8_t* sStage = smem + L.stage;
+    const size_t halo_bytes = (size_t)(C / 8) * kHaloPlane;
+    __shared__ uint64_t w_full, h_full[2], h_empty[2], a_full[2], a_empty[2];
+    __shared__ float sbias[BN];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&w_full, 1);
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(&h_full[i], 1);
+            tc::mbar_init(&h_empty[i], 1);
+            tc::mbar_init(&a_full[i], 1);
+            tc::mbar_init(&a_empty[i], 4 * 32);
+        }
+        tc::fence_barrier_init();
+        failed = 0;
+        if (tc::smem_u32(smem) & 1023u) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    if (threadIdx.x < BN) sbias[threadIdx.x] = bias[threadIdx.x];
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 2 * BN);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    // tile -> (instance, origin)
+    auto locate = [&](int tile, int& ii, int& x0, int& y0) {
+        int lo = 0, hi = n_inst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (inst[mid].ct0 <= tile) lo = mid; else hi = mid - 1;
+        }
+        ii = lo;
+        const InstDev& I = inst[lo];
+        const int tiles_x = (I.nx + kConvTX - 1) / kConvTX;
+        const int tl = tile - I.ct0;
+        x0 = (tl % tiles_x) * kConvTX;
+        y0 = (tl / tiles_x) * kConvTY;
+    };
+    if (warp == 0) {
+        if (lane == 0 && !failed) {
+            // halo producer
+            for (int it = 0; it < my_tiles; it++) {
+                const int b = it & 1;
+                if (it >= 2 && !tc::mbar_wait(&h_empty[b], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) break;
+                int ii, x0, y0;
+                locate((int)blockIdx.x + it * (int)gridDim.x, ii, x0, y0);
+                const CUtensorMap* map = maps + kMapsPerInst * ii + 1;
+                tc::tensormap_acquire(map);
+                tc::mbar_expect_tx(&h_full[b], (uint32_t)(C / 8) * (kHaloW * kHaloH * 16));
+                for (int kc = 0; kc < C / 8; kc++)
+                    tc::tma_load_3d(sHalo + b * halo_bytes + kc * kHaloPlane, map, kc * 8, x0 - 1, y0 - 1, &h_full[b]);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && !failed) {
+            // MMA issuer: the nine taps' weights once, then every tile
+            tc::mbar_expect_tx(&w_full, (uint32_t)9 * C * BN * 2);
+            tc::bulk_load(sW, Wt, (uint32_t)9 * C * BN * 2, &w_full);
+            bool good = tc::mbar_wait(&w_full, 0, err, &failed);
+            const uint32_t idesc = tc::idesc_bf16(128, BN);
+            const uint32_t w0 = tc::smem_u32(sW);
+            for (int it = 0; it < my_tiles && good; it++) {
+                const int b = it & 1;
+                good = tc::mbar_wait(&h_full[b], (uint32_t)(it >> 1) & 1u, err, &failed) &&
+                       (it < 2 || tc::mbar_wait(&a_empty[b], (uint32_t)((it - 2) >> 1) & 1u, err, &failed));
+                if (!good) break;
+                tc::tc_fence_after();
+                const uint32_t h0 = tc::smem_u32(sHalo + b * halo_bytes);
+                const uint32_t acc = tmem + (uint32_t)b * BN;
+                for (int t = 0; t < 9; t++) {
+                    const int ky = t / 3, kx = t % 3;
+                    const uint32_t b0 = w0 + (uint32_t)t * C * BN * 2;
+                    for (int k = 0; k < C / 16; k++) {
+                        uint64_t ad = tc::sdesc(h0 + 2 * k * kHaloPlane + (ky * kHaloW + kx) * 16, kHaloPlane, kHaloW * 16);
+                        uint64_t bd = tc::sdesc(b0 + 2 * k * BN * 16, BN * 16, 128);
+                        tc::mma_bf16(acc, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
+                    }
+                }
+                tc::mma_commit(&h_empty[b]);
+                tc::mma_commit(&a_full[b]);
+            }
+        }
+        __syncwarp();
+    } else {
+        // epilogue: thread r = TMEM lane r = tile position (y0 + r / 8, x0 + r % 8)
+        const int r = (warp & 3) * 32 + lane;
+        const bool leader = warp == 2 && lane == 0;
+        for (int it = 0; it < my_tiles; it++) {
+            const int b = it & 1;
+            const bool ready = tc::mbar_wait(&a_full[b], (uint32_t)(it >> 1) & 1u, err, &failed);
+            uint32_t all_ready;
+            asm volatile(
+                "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, 1, 128, q;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(all_ready)
+                : "r"(ready ? 1u : 0u)
+                : "memory");
+            if (!all_ready) break;
+            tc::tc_fence_after();
+            // the staging box used two tiles ago must have been read by its store
+            if (leader && it >= 2) tc::bulk_wait_read_1();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            uint8_t* box = sStage + (size_t)b * 16384 + (size_t)r * 128;
+            const uint32_t ta = lane_addr(tmem + (uint32_t)b * BN);
+            for (int c = 0; c < BN; c += 16) {
+                float a[16];
+                tc::tmem_ld16(ta + c, a);
+#pragma unroll
+                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + sbias[c + i]);
+                const int j0 = c / 4;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    *reinterpret_cast<float4*>(box + (((j0 + q) ^ (r & 7)) << 4)) =
+                        make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&a_empty[b]);
+            tc::fence_async_shared();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (leader) {
+                int ii, x0, y0;
+                locate((int)blockIdx.x + it * (int)gridDim.x, ii, x0, y0);
+                const CUtensorMap* omap = maps + kMapsPerInst * ii + 3;
+                tc::tensormap_acquire(omap);
+                tc::tma_store_3d(omap, sStage + (size_t)b * 16384, 0, x0, y0);
+                tc::bulk_commit();
+            }
+        }
+        if (leader) tc::bulk_wait_read();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 2 * BN);
+}
+
 // Whether the shared-memory attention tiles apply (radius-1, dilation-1
 // stencil; 64-channel boxes; at most 4 heads of width 32 or 64).
 static bool attn_tile_ok(const Dims& d) {
@@ -1875,6 +2050,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
     set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
+    set_smem(tc_conv1_persistent_kernel, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
     set_smem(tc_mlp_persistent_kernel, kMlpSmemMax);
@@ -2212,8 +2388,9 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     }
     {
         KScope k("tc_conv1", s);
-        tc_conv3_kernel<CONV_CELL1><<<dim3(p.n_ctiles, 1), 128, conv3_launch_smem(kZcCh, d.HD, 9, 4), s>>>(
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), 1, 3, wc1, w.c1_b, kZcCh, d.HD, 9, p.inst, n, p.err);
+        const unsigned grid = (unsigned)std::min(p.n_ctiles, 2 * n_sms_);
+        tc_conv1_persistent_kernel<<<grid, kC1PThreads, C1PSmem(kZcCh, d.HD).total, s>>>(
+            reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n, p.err);
         check_launch("tc_conv1");
     }
     conv2_step(d, c1, w, p, mode, "bf_conv2_step", s);

@@ -118,8 +118,10 @@ __device__ __forceinline__ void tma_store_3d(const void* tmap, const void* src, 
                  : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// Waits until the committed bulk stores have read their shared memory.
+// Waits until the committed bulk stores have read their shared memory (all,
+// or all but the most recent group).
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 
 // Generic-proxy writes to shared memory become visible to the tensor core.
 __device__ __forceinline__ void fence_async_shared() {
