@@ -1559,6 +1559,151 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// One decision for the `n` threads (whole warps) that meet at named barrier `bar`.
+__device__ __forceinline__ bool all_of(bool v, int bar, int n) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(bar), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
+// Persistent output projection + residual + LayerNorm (cpu.rs:300-313) for
+// dims up to 128: x += attn @ Wp + bp, ln = LayerNorm2(x). One CTA per SM
+// walks row tiles with its stages on separate warps:
+//   warp 0     (one lane) TMA-loads each tile's attention rows and f32
+//              residual rows (128-byte swizzled boxes) into one of two slots;
+//   warp 1     (one lane) loads Wp once and issues each tile's MMAs into one
+//              of two TMEM accumulators;
+//   warps 2-5  thread r owns tile row r: the residual update in place in the
+//              slot's x rows, the LayerNorm (row_resid_ln, the shared
+//              arithmetic), ln rows straight to global, the new x rows back
+//              with a TMA store.
+constexpr int kPLThreads = 6 * 32;
+
+struct PLSmem {
+    size_t b, a, x, total;
+    __host__ __device__ explicit PLSmem(int D) {
+        b = 0;                                             // Wp [D/8][D][8]
+        a = (size_t)D * D * 2;                             // 2 x [D/8][128][8]
+        x = (a + 2 * (size_t)D * 256 + 1023) / 1024 * 1024;  // 2 x D/32 boxes of 32 f32 x 128 rows
+        total = x + 2 * (size_t)D * 512;
+    }
+};
+
+__global__ void __launch_bounds__(kPLThreads, 1) tc_projln_persistent_kernel(
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, const bf16* __restrict__ Wp,
+    const float* __restrict__ bias, const float* __restrict__ gam, const float* __restrict__ bet,
+    bf16* __restrict__ ln, int D, int R, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const PLSmem L(D);
+    uint8_t* sB = smem + L.b;
+    uint8_t* sA = smem + L.a;
+    uint8_t* sX = smem + L.x;
+    __shared__ uint64_t b_full, in_full[2], in_empty[2], acc_full[2], acc_empty[2];
+    __shared__ float sbias[kLnMaxD], sg[kLnMaxD], sb[kLnMaxD];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_tiles = (R + 127) / 128;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const uint32_t ncols = D <= 32 ? 64 : (D <= 64 ? 128 : 256);  // two accumulators
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&b_full, 1);
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(&in_full[i], 1);
+            tc::mbar_init(&in_empty[i], 2);  // the MMAs have read A, the epilogue's store has read x
+            tc::mbar_init(&acc_full[i], 1);
+            tc::mbar_init(&acc_empty[i], 4 * 32);
+        }
+        tc::fence_barrier_init();
+        failed = 0;
+        if ((tc::smem_u32(smem) & 1023u) || D > kLnMaxD || D % 32) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    for (int i = threadIdx.x; i < D; i += blockDim.x) {
+        sbias[i] = bias[i];
+        sg[i] = gam[i];
+        sb[i] = bet[i];
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const size_t a_bytes = (size_t)D * 256, x_bytes = (size_t)D * 512;
+    if (warp == 0) {
+        if (lane == 0 && !failed) {
+            for (int it = 0; it < my_tiles; it++) {
+                const int s = it & 1;
+                if (it >= 2 && !tc::mbar_wait(&in_empty[s], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) break;
+                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+                tc::mbar_expect_tx(&in_full[s], (uint32_t)(a_bytes + x_bytes));
+                for (int kc = 0; kc < D / 8; kc++)
+                    tc::tma_load_2d(sA + s * a_bytes + kc * 2048, &tmA, kc * 8, m0, &in_full[s]);
+                for (int bx = 0; bx < D / 32; bx++)
+                    tc::tma_load_2d(sX + s * x_bytes + bx * 16384, &tmX, bx * 32, m0, &in_full[s]);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && !failed) {
+            tc::mbar_expect_tx(&b_full, (uint32_t)D * D * 2);
+            tc::bulk_load(sB, Wp, (uint32_t)D * D * 2, &b_full);
+            bool good = tc::mbar_wait(&b_full, 0, err, &failed);
+            const uint32_t idesc = tc::idesc_bf16(128, D);
+            const uint32_t b0 = tc::smem_u32(sB);
+            for (int it = 0; it < my_tiles && good; it++) {
+                const int s = it & 1;
+                good = tc::mbar_wait(&in_full[s], (uint32_t)(it >> 1) & 1u, err, &failed) &&
+                       (it < 2 || tc::mbar_wait(&acc_empty[s], (uint32_t)((it - 2) >> 1) & 1u, err, &failed));
+                if (!good) break;
+                tc::tc_fence_after();
+                const uint32_t a0 = tc::smem_u32(sA + s * a_bytes);
+                const uint32_t acc = tmem + (uint32_t)s * D;
+                for (int k = 0; k < D / 16; k++)
+                    tc::mma_bf16(acc, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(b0 + k * 2 * D * 16, D * 16, 128),
+                                 idesc, k > 0 ? 1u : 0u);
+                tc::mma_commit(&in_empty[s]);
+                tc::mma_commit(&acc_full[s]);
+            }
+        }
+        __syncwarp();
+    } else {
+        const int r = (warp & 3) * 32 + lane;
+        const bool leader = warp == 2 && lane == 0;
+        for (int it = 0; it < my_tiles; it++) {
+            const int s = it & 1;
+            const bool ready = tc::mbar_wait(&acc_full[s], (uint32_t)(it >> 1) & 1u, err, &failed) &&
+                               tc::mbar_wait(&in_full[s], (uint32_t)(it >> 1) & 1u, err, &failed);
+            if (!all_of(ready, 1, 128)) break;
+            tc::tc_fence_after();
+            const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+            const int row = m0 + r;
+            row_resid_ln(lane_addr(tmem + (uint32_t)s * D), r, D, sX + s * x_bytes, sbias, sg, sb, nullptr,
+                         row < R ? ln + (size_t)row * D : nullptr);
+            tc::tc_fence_before();
+            tc::mbar_arrive(&acc_empty[s]);
+            tc::fence_async_shared();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (leader) {
+                for (int bx = 0; bx < D / 32; bx++) tc::tma_store_2d(&tmX, sX + s * x_bytes + bx * 16384, bx * 32, m0);
+                tc::bulk_commit();
+                tc::bulk_wait_read();
+                tc::mbar_arrive(&in_empty[s]);
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
 // 3x3 zero-padded convolution over each instance's grid as an implicit GEMM
 // (cpu.rs:171-205): tile = 8 x 16 positions (M = 128, row r <-> position
 // (y0 + r/8, x0 + r%8)); the halo tile [C/8 planes][18][10][8] is loaded by
@@ -2050,6 +2195,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
     set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
+    set_smem(tc_projln_persistent_kernel, 225 * 1024);  // 227 KB per CTA less the static shared memory
     set_smem(tc_conv1_persistent_kernel, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
@@ -2318,6 +2464,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     float* c1 = reinterpret_cast<float*>(p.bc[1]);
     const CUtensorMap m_ln = rows_map(ln, D, R), m_attn = rows_map(attn, D, R), m_t1 = rows_map(t1, D, R);
     const CUtensorMap m_qkv_out = store_map(qkv, 3 * D, R, 3 * D, false), m_z0_out = store_map(p.z0, d.HD, R, d.HD, true);
+    const CUtensorMap m_x = store_map(p.x, D, R, D, true);
     const unsigned gm = (unsigned)((R + 127) / 128);
     const Tuning tu = tuning_for(R);
     {
@@ -2354,9 +2501,16 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         }
         {
             KScope k("tc_proj_ln", s);
-            GemmEpi ep{B.bp, ln, nullptr, p.x, B.n2g, B.n2b, D};
-            const size_t smem = std::max((size_t)D * 256 + (size_t)D * D * 2, (size_t)128 * D * 4);
-            tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(m_attn, m_attn, wp[l], D, D, R, ep, p.err);
+            if (D <= kLnMaxD) {
+                const unsigned grid = (unsigned)std::min((int)gm, n_sms_);
+                tc_projln_persistent_kernel<<<grid, kPLThreads, PLSmem(D).total, s>>>(m_attn, m_x, wp[l], B.bp, B.n2g,
+                                                                                    B.n2b, ln, D, R, p.err);
+            } else {
+                GemmEpi ep{B.bp, ln, nullptr, p.x, B.n2g, B.n2b, D};
+                const size_t smem = std::max((size_t)D * 256 + (size_t)D * D * 2, (size_t)128 * D * 4);
+                tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(m_attn, m_attn, wp[l], D, D, R, ep,
+                                                                            p.err);
+            }
             check_launch("tc_proj_ln");
         }
         {
