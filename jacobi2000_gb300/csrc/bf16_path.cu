@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;                       // [K/8][128][8]
     uint8_t* sB = smem + (size_t)K * 256;     // [K/8][BN][8]
-    __shared__ float sbias[256];
+    __shared__ __align__(16) float sbias[256];
     __shared__ uint64_t bar_load, bar_mma;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
@@ -1221,7 +1221,7 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     uint8_t* sB1 = sA + (size_t)D * 256;          // [D/8][NC][8]
     uint8_t* sB2 = sB1 + (size_t)D * NC * 2;      // [NC/8][D][8]
     uint8_t* sH = sB2 + (size_t)D * NC * 2;       // [NC/8][128][8]
-    __shared__ float sb1[1024];
+    __shared__ __align__(16) float sb1[1024];
     __shared__ uint64_t bar_a, bar_w, bar_s, bar_o;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
@@ -1365,7 +1365,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     constexpr int kMaxStages = 4;
     __shared__ uint64_t a_full, a_empty, w_full[kMaxStages], w_empty[kMaxStages], s_full[2], h_full[2], h_empty[2],
         o_full[2], o_empty[2], x_full;
-    __shared__ float sb2[kLnMaxD], sgam[kLnMaxD], sbet[kLnMaxD];
+    __shared__ __align__(16) float sb2[kLnMaxD], sgam[kLnMaxD], sbet[kLnMaxD];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1604,7 +1604,7 @@ __global__ void __launch_bounds__(kPLThreads, 1) tc_projln_persistent_kernel(
     uint8_t* sA = smem + L.a;
     uint8_t* sX = smem + L.x;
     __shared__ uint64_t b_full, in_full[2], in_empty[2], acc_full[2], acc_empty[2];
-    __shared__ float sbias[kLnMaxD], sg[kLnMaxD], sb[kLnMaxD];
+    __shared__ __align__(16) float sbias[kLnMaxD], sg[kLnMaxD], sb[kLnMaxD];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1704,6 +1704,150 @@ __global__ void __launch_bounds__(kPLThreads, 1) tc_projln_persistent_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// Persistent q/k/v projection (cpu.rs:291-297, the three linears as one GEMM
+// over the concatenated weights): one CTA per SM walks row tiles; the whole
+// weight matrix stays in shared memory. Items are (tile, N block):
+//   warp 0     (one lane) TMA-loads each tile's LayerNorm rows into one of two
+//              slots;
+//   warp 1     (one lane) loads the weights once and issues each item's MMAs
+//              into one of two TMEM accumulators;
+//   warps 2-5  add the bias, round to bf16 into one of two 128-byte swizzled
+//              staging areas and store the item with TMA.
+constexpr int kQKVPThreads = 6 * 32;
+
+struct QKVPSmem {
+    size_t b, a, stage, total;
+    __host__ __device__ QKVPSmem(int D, int BN) {
+        b = 0;                                            // [3D/BN][D/8][BN][8]
+        a = (size_t)3 * D * D * 2;                        // 2 x [D/8][128][8]
+        stage = (a + 2 * (size_t)D * 256 + 1023) / 1024 * 1024;  // 2 x ceil(BN/64) boxes of 16 KB
+        total = stage + 2 * (size_t)((BN + 63) / 64) * 16384;
+    }
+};
+
+__global__ void __launch_bounds__(kQKVPThreads, 1) tc_qkv_persistent_kernel(
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmO, const bf16* __restrict__ W,
+    const float* __restrict__ bias, int D, int BN, int R, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const QKVPSmem L(D, BN);
+    uint8_t* sB = smem + L.b;
+    uint8_t* sA = smem + L.a;
+    uint8_t* sStage = smem + L.stage;
+    __shared__ uint64_t b_full, a_full[2], a_empty[2], acc_full[2], acc_empty[2];
+    __shared__ __align__(16) float sbias[3 * 128];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int NB = 3 * D / BN;
+    const int n_tiles = (R + 127) / 128;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int total = my_tiles * NB;
+    uint32_t ncols = 32;
+    while (ncols < 2u * BN) ncols <<= 1;
+    const size_t a_bytes = (size_t)D * 256, st_bytes = (size_t)((BN + 63) / 64) * 16384;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&b_full, 1);
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(&a_full[i], 1);
+            tc::mbar_init(&a_empty[i], 1);
+            tc::mbar_init(&acc_full[i], 1);
+            tc::mbar_init(&acc_empty[i], 4 * 32);
+        }
+        tc::fence_barrier_init();
+        failed = 0;
+        if ((tc::smem_u32(smem) & 1023u) || D > 128 || 3 * D % BN || ncols > 512) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    for (int i = threadIdx.x; i < 3 * D && i < 3 * 128; i += blockDim.x) sbias[i] = bias[i];
+    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    if (warp == 0) {
+        if (lane == 0 && !failed) {
+            for (int it = 0; it < my_tiles; it++) {
+                const int s = it & 1;
+                if (it >= 2 && !tc::mbar_wait(&a_empty[s], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) break;
+                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+                tc::mbar_expect_tx(&a_full[s], (uint32_t)a_bytes);
+                for (int kc = 0; kc < D / 8; kc++)
+                    tc::tma_load_2d(sA + s * a_bytes + kc * 2048, &tmA, kc * 8, m0, &a_full[s]);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && !failed) {
+            tc::mbar_expect_tx(&b_full, (uint32_t)3 * D * D * 2);
+            tc::bulk_load(sB, W, (uint32_t)3 * D * D * 2, &b_full);
+            bool good = tc::mbar_wait(&b_full, 0, err, &failed);
+            const uint32_t idesc = tc::idesc_bf16(128, BN);
+            const uint32_t b0 = tc::smem_u32(sB);
+            for (int g = 0; g < total && good; g++) {
+                const int it = g / NB, nb = g % NB, s = it & 1;
+                if (nb == 0) good = tc::mbar_wait(&a_full[s], (uint32_t)(it >> 1) & 1u, err, &failed);
+                if (good && g >= 2) good = tc::mbar_wait(&acc_empty[g & 1], (uint32_t)((g - 2) >> 1) & 1u, err, &failed);
+                if (!good) break;
+                tc::tc_fence_after();
+                const uint32_t a0 = tc::smem_u32(sA + s * a_bytes);
+                const uint32_t bb = b0 + (uint32_t)nb * D * BN * 2;
+                const uint32_t acc = tmem + (uint32_t)(g & 1) * BN;
+                for (int k = 0; k < D / 16; k++)
+                    tc::mma_bf16(acc, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(bb + k * 2 * BN * 16, BN * 16, 128),
+                                 idesc, k > 0 ? 1u : 0u);
+                tc::mma_commit(&acc_full[g & 1]);
+                if (nb == NB - 1) tc::mma_commit(&a_empty[s]);  // the tile's last read of A
+            }
+        }
+        __syncwarp();
+    } else {
+        const int r = (warp & 3) * 32 + lane;
+        const bool leader = warp == 2 && lane == 0;
+        for (int g = 0; g < total; g++) {
+            const int it = g / NB, nb = g % NB;
+            const bool ready = tc::mbar_wait(&acc_full[g & 1], (uint32_t)(g >> 1) & 1u, err, &failed);
+            if (!all_of(ready, 1, 128)) break;
+            tc::tc_fence_after();
+            // the staging area used two items ago must have been read by its store
+            if (leader && g >= 2) tc::bulk_wait_read_1();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            uint8_t* st = sStage + (size_t)(g & 1) * st_bytes;
+            const uint32_t ta = lane_addr(tmem + (uint32_t)(g & 1) * BN);
+            for (int c = 0; c < BN; c += 16) {
+                float a[16];
+                tc::tmem_ld16(ta + c, a);
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    const float4 bv = *reinterpret_cast<const float4*>(sbias + nb * BN + c + i);
+                    a[i] += bv.x;
+                    a[i + 1] += bv.y;
+                    a[i + 2] += bv.z;
+                    a[i + 3] += bv.w;
+                }
+                uint8_t* box = st + (size_t)(c / 64) * 16384 + (size_t)r * 128;
+                const int j0 = (c % 64) / 8;
+                BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
+                BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&acc_empty[g & 1]);
+            tc::fence_async_shared();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (leader) {
+                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
+                for (int c = 0; c < BN; c += 64) tc::tma_store_2d(&tmO, st + (size_t)(c / 64) * 16384, nb * BN + c, m0);
+                tc::bulk_commit();
+            }
+        }
+        if (leader) tc::bulk_wait_read();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
 // 3x3 zero-padded convolution over each instance's grid as an implicit GEMM
 // (cpu.rs:171-205): tile = 8 x 16 positions (M = 128, row r <-> position
 // (y0 + r/8, x0 + r%8)); the halo tile [C/8 planes][18][10][8] is loaded by
@@ -1741,7 +1885,7 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     uint8_t* sB = smem + (size_t)(C / 8) * kHaloPlane;       // NS x [C/8][BN][8]
     constexpr int kMaxNS = 9;
     __shared__ uint64_t bar_h, bar_b[kMaxNS], bar_m[kMaxNS], bar_done;
-    __shared__ float sbias[256];
+    __shared__ __align__(16) float sbias[256];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5;
@@ -1912,7 +2056,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
     uint8_t* sStage = smem + L.stage;
     const size_t halo_bytes = (size_t)(C / 8) * kHaloPlane;
     __shared__ uint64_t w_full, h_full[2], h_empty[2], a_full[2], a_empty[2];
-    __shared__ float sbias[BN];
+    __shared__ __align__(16) float sbias[BN];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2196,6 +2340,7 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
     set_smem(tc_projln_persistent_kernel, 225 * 1024);  // 227 KB per CTA less the static shared memory
+    set_smem(tc_qkv_persistent_kernel, 225 * 1024);
     set_smem(tc_conv1_persistent_kernel, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
@@ -2488,10 +2633,16 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         {
             KScope k("tc_qkv", s);
             const int BN = bn_qkv;
-            GemmEpi ep{B.bqkv, qkv, nullptr, nullptr, nullptr, nullptr, 3 * D};
-            const size_t smem = std::max((size_t)D * 256 + (size_t)D * BN * 2, (size_t)((BN + 63) / 64) * 16384);
-            tc_gemm_kernel<EPI_BF16><<<dim3(gm, 3 * D / BN), 128, smem, s>>>(m_ln, m_qkv_out, wqkv[l], D, BN, R, ep,
-                                                                         p.err);
+            if (D <= 128) {
+                const unsigned grid = (unsigned)std::min((int)gm, n_sms_);
+                tc_qkv_persistent_kernel<<<grid, kQKVPThreads, QKVPSmem(D, BN).total, s>>>(m_ln, m_qkv_out, wqkv[l],
+                                                                                         B.bqkv, D, BN, R, p.err);
+            } else {
+                GemmEpi ep{B.bqkv, qkv, nullptr, nullptr, nullptr, nullptr, 3 * D};
+                const size_t smem = std::max((size_t)D * 256 + (size_t)D * BN * 2, (size_t)((BN + 63) / 64) * 16384);
+                tc_gemm_kernel<EPI_BF16><<<dim3(gm, 3 * D / BN), 128, smem, s>>>(m_ln, m_qkv_out, wqkv[l], D, BN, R, ep,
+                                                                             p.err);
+            }
             check_launch("tc_qkv");
         }
         {
