@@ -1316,34 +1316,50 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
 }
 
+// One decision for the `n` threads (whole warps) that meet at named barrier `bar`.
+__device__ __forceinline__ bool all_of(bool v, int bar, int n) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(bar), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
 // Persistent form of the fused MLP: one CTA per SM walks row tiles (tile =
 // blockIdx.x + k * gridDim.x) with every stage on its own warps, so the
 // tensor core, the GELU arithmetic and the residual + LayerNorm epilogue of
 // consecutive tiles overlap:
 //   warp 0      (one lane) TMA-loads the A tile (single buffer, refilled once
 //               the tile's last S MMA has read it);
-//   warp 1      (one lane) streams the weight chunks W1_j | W2_j through an
-//               NS-stage ring, continuing across tiles;
-//   warp 2      (one lane) issues every MMA: S_g = A @ W1_j into one of two
+//   warps 1, 2  (one lane each) stream the W1 and the W2 chunks through two
+//               separate NS-stage rings, continuing across tiles (W1_j is
+//               released when S_j is done, W2_j when O += h_j W2_j is, so
+//               neither waits on the other);
+//   warp 3      (one lane) issues every MMA: S_g = A @ W1_j into one of two
 //               TMEM S buffers, O += h_g @ W2_j into one of two TMEM O
 //               buffers (one per tile in flight);
-//   warps 3-18  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers;
+//   warps 4-19  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers;
 //               four warps per TMEM lane quarter, 16 columns each);
-//   warps 19-22 stage a finished O buffer (one TMEM lane quarter each),
-//               release it, and run the residual + LayerNorm rows.
+//   warps 20-23 thread r owns tile row r: the residual update of the tile's
+//               f32 x rows (prefetched by TMA), the LayerNorm in the shared
+//               arithmetic, ln rows to global, x rows back by TMA.
 // g counts chunks over all of this CTA's tiles. The arithmetic and its order
 // are those of the other MLP kernels (the same K slices of 16 in the same
-// order), so the result is bit-identical.
+// order, the same LayerNorm arithmetic), so the result is bit-identical.
 constexpr int kMlpPGelu = 16;                  // GELU warps (NC = 64: 16 columns each)
-constexpr int kMlpPWarps = 3 + kMlpPGelu + 4;  // + A producer, W producer, MMA issuer; + 4 epilogue
+constexpr int kMlpPWarps = 4 + kMlpPGelu + 4;  // + A, W1, W2 producers, MMA issuer; + 4 epilogue
 constexpr int kMlpPThreads = kMlpPWarps * 32;
 
 struct MlpPSmem {
-    size_t a, w, h, b1, epi, total;
+    size_t a, w1, w2, h, b1, epi, total;
     __host__ __device__ MlpPSmem(int D, int F, int NC, int NS) {
         a = 0;                                  // [D/8][128][8]
-        w = a + (size_t)D * 256;                // NS x (W1_j | W2_j)
-        h = w + (size_t)NS * 4 * D * NC;        // 2 x [NC/8][128][8]
+        w1 = a + (size_t)D * 256;               // NS x W1_j [D/8][NC][8]
+        w2 = w1 + (size_t)NS * 2 * D * NC;      // NS x W2_j [NC/8][D][8]
+        h = w2 + (size_t)NS * 2 * D * NC;       // 2 x [NC/8][128][8]
         b1 = h + (size_t)2 * NC * 256;          // [F] f32
         epi = (b1 + (size_t)F * 4 + 1023) / 1024 * 1024;  // x rows: D/32 swizzled boxes of 32 f32 x 128 rows
         total = epi + (size_t)128 * D * 4;
@@ -1358,13 +1374,14 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     extern __shared__ __align__(1024) uint8_t smem[];
     const MlpPSmem L(D, F, NC, NS);
     uint8_t* sA = smem + L.a;
-    uint8_t* sW = smem + L.w;
+    uint8_t* sW1 = smem + L.w1;
+    uint8_t* sW2 = smem + L.w2;
     uint8_t* sH = smem + L.h;
     float* sb1 = reinterpret_cast<float*>(smem + L.b1);
     uint8_t* sX = smem + L.epi;
     constexpr int kMaxStages = 4;
-    __shared__ uint64_t a_full, a_empty, w_full[kMaxStages], w_empty[kMaxStages], s_full[2], h_full[2], h_empty[2],
-        o_full[2], o_empty[2], x_full;
+    __shared__ uint64_t a_full, a_empty, w1_full[kMaxStages], w1_empty[kMaxStages], w2_full[kMaxStages],
+        w2_empty[kMaxStages], s_full[2], h_full[2], h_empty[2], o_full[2], o_empty[2], x_full;
     __shared__ __align__(16) float sb2[kLnMaxD], sgam[kLnMaxD], sbet[kLnMaxD];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
@@ -1380,8 +1397,10 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
         tc::mbar_init(&a_full, 1);
         tc::mbar_init(&a_empty, 1);
         for (int i = 0; i < NS && i < kMaxStages; i++) {
-            tc::mbar_init(&w_full[i], 1);
-            tc::mbar_init(&w_empty[i], 1);
+            tc::mbar_init(&w1_full[i], 1);
+            tc::mbar_init(&w1_empty[i], 1);
+            tc::mbar_init(&w2_full[i], 1);
+            tc::mbar_init(&w2_empty[i], 1);
         }
         for (int i = 0; i < 2; i++) {
             tc::mbar_init(&s_full[i], 1);
@@ -1422,34 +1441,39 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
+    } else if (warp == 1 || warp == 2) {
         if (lane == 0 && !failed) {
-            // weight producer
+            // W1 (warp 1) or W2 (warp 2) producer
+            const bool first = warp == 1;
+            uint64_t* full = first ? w1_full : w2_full;
+            uint64_t* empty = first ? w1_empty : w2_empty;
+            uint8_t* ring = first ? sW1 : sW2;
+            const bf16* src = first ? W1 : W2;
             for (int gi = 0; gi < total; gi++) {
                 const int st = gi % NS, j = gi % nch;
-                if (gi >= NS && !tc::mbar_wait(&w_empty[st], (uint32_t)(gi / NS - 1) & 1u, err, &failed)) break;
-                uint8_t* dst = sW + (size_t)st * 2 * wbytes;
-                tc::mbar_expect_tx(&w_full[st], 2 * wbytes);
-                tc::bulk_load(dst, W1 + (size_t)j * D * NC, wbytes, &w_full[st]);
-                tc::bulk_load(dst + wbytes, W2 + (size_t)j * D * NC, wbytes, &w_full[st]);
+                if (gi >= NS && !tc::mbar_wait(&empty[st], (uint32_t)(gi / NS - 1) & 1u, err, &failed)) break;
+                tc::mbar_expect_tx(&full[st], wbytes);
+                tc::bulk_load(ring + (size_t)st * wbytes, src + (size_t)j * D * NC, wbytes, &full[st]);
             }
         }
         __syncwarp();
-    } else if (warp == 2) {
+    } else if (warp == 3) {
         if (lane == 0 && !failed) {
             // MMA issuer
-            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH), w0 = tc::smem_u32(sW);
+            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH);
+            const uint32_t w1s = tc::smem_u32(sW1), w2s = tc::smem_u32(sW2);
             const uint32_t idesc_s = tc::idesc_bf16(128, NC), idesc_o = tc::idesc_bf16(128, D);
             auto issue_s = [&](int gi) -> bool {
                 const int st = gi % NS, j = gi % nch, it = gi / nch;
                 if (j == 0 && !tc::mbar_wait(&a_full, (uint32_t)it & 1u, err, &failed)) return false;
-                if (!tc::mbar_wait(&w_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) return false;
+                if (!tc::mbar_wait(&w1_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) return false;
                 tc::tc_fence_after();
-                const uint32_t ws = w0 + (uint32_t)st * 2 * wbytes;
+                const uint32_t ws = w1s + (uint32_t)st * wbytes;
                 const uint32_t tS = tmem + s_col + (uint32_t)(gi & 1) * NC;
                 for (int k = 0; k < D / 16; k++)
                     tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(ws + k * 2 * NC * 16, NC * 16, 128),
                                  idesc_s, k > 0 ? 1u : 0u);
+                tc::mma_commit(&w1_empty[st]);
                 tc::mma_commit(&s_full[gi & 1]);
                 if (j == nch - 1) tc::mma_commit(&a_empty);  // the tile's last read of A
                 return true;
@@ -1467,25 +1491,33 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
                     good = false;
                     break;
                 }
+                // h_g is written, so S buffer g & 1 is free: S_{g+2} goes first,
+                // so the GELU warps never wait on this thread's wait for W2_g
+                if (gi + 2 < total && !issue_s(gi + 2)) {
+                    good = false;
+                    break;
+                }
+                if (!tc::mbar_wait(&w2_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) {
+                    good = false;
+                    break;
+                }
                 tc::tc_fence_after();
-                const uint32_t ws2 = w0 + (uint32_t)st * 2 * wbytes + wbytes;
+                const uint32_t ws2 = w2s + (uint32_t)st * wbytes;
                 const uint32_t hs = h0 + (uint32_t)(gi & 1) * NC * 256;
                 const uint32_t tO = tmem + (uint32_t)(it & 1) * D;
                 for (int k = 0; k < NC / 16; k++)
                     tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(ws2 + k * 2 * D * 16, D * 16, 128),
                                  idesc_o, (j > 0 || k > 0) ? 1u : 0u);
-                tc::mma_commit(&w_empty[st]);
+                tc::mma_commit(&w2_empty[st]);
                 tc::mma_commit(&h_empty[gi & 1]);
                 if (j == nch - 1) tc::mma_commit(&o_full[it & 1]);
-                if (gi + 2 < total) good = issue_s(gi + 2);
             }
         }
         __syncwarp();
-    } else if (warp < 3 + kMlpPGelu) {
+    } else if (warp < 4 + kMlpPGelu) {
         // GELU warps
-        const int part = (warp - 3) >> 2;  // columns 16 part .. 16 part + 15 of the chunk
+        const int part = (warp - 4) >> 2;  // columns 16 part .. 16 part + 15 of the chunk
         const int r = (warp & 3) * 32 + lane;
-        const int cw = 16;
         for (int gi = 0; gi < total; gi++) {
             const int j = gi % nch;
             const bool s_ready = tc::mbar_wait(&s_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed);
@@ -1494,21 +1526,20 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             tc::tc_fence_after();
             const uint32_t ta = lane_addr(tmem + s_col + (uint32_t)(gi & 1) * NC);
             uint8_t* hb = sH + (size_t)(gi & 1) * NC * 256;
-            for (int c = part * cw; c < (part + 1) * cw; c += 16) {
-                float a[16];
-                tc::tmem_ld16(ta + c, a);
-                const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
+            const int c = part * 16;
+            float a[16];
+            tc::tmem_ld16(ta + c, a);
+            const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const float4 bv = bb[i];
-                    a[4 * i] = gelu_fast(a[4 * i] + bv.x);
-                    a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
-                    a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
-                    a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
-                }
-                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
-                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
+            for (int i = 0; i < 4; i++) {
+                const float4 bv = bb[i];
+                a[4 * i] = gelu_fast(a[4 * i] + bv.x);
+                a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
+                a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
+                a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
             }
+            BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
+            BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
             tc::fence_async_shared();
             tc::tc_fence_before();
             tc::mbar_arrive(&h_full[gi & 1]);
@@ -1518,7 +1549,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
         // of the next tile are prefetched by TMA into sX as soon as the
         // previous tile's x store has read it.
         const int r = (warp & 3) * 32 + lane;
-        const bool leader = warp == 3 + kMlpPGelu && lane == 0;
+        const bool leader = warp == 4 + kMlpPGelu && lane == 0;
         auto load_x = [&](int it) {
             const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
             tc::mbar_expect_tx(&x_full, (uint32_t)D * 512);
@@ -1528,15 +1559,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
         for (int it = 0; it < my_tiles; it++) {
             const bool ready = tc::mbar_wait(&o_full[it & 1], (uint32_t)(it >> 1) & 1u, err, &failed) &&
                                tc::mbar_wait(&x_full, (uint32_t)it & 1u, err, &failed);
-            // one decision for all four epilogue warps (they meet at barrier 1 below)
-            uint32_t all_ready;
-            asm volatile(
-                "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, 1, 128, q;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(all_ready)
-                : "r"(ready ? 1u : 0u)
-                : "memory");
-            if (!all_ready) break;
+            if (!all_of(ready, 1, 128)) break;  // the four epilogue warps meet at barrier 1 below
             tc::tc_fence_after();
             const int row = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + r;
             row_resid_ln(lane_addr(tmem + (uint32_t)(it & 1) * D), r, D, sX, sb2, sgam, sbet, nullptr,
@@ -1544,7 +1567,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             tc::tc_fence_before();
             tc::mbar_arrive(&o_empty[it & 1]);
             tc::fence_async_shared();
-            asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+            asm volatile("bar.sync 1, 128;" ::: "memory");
             if (leader) {
                 const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
                 for (int bx = 0; bx < D / 32; bx++) tc::tma_store_2d(&tmX, sX + bx * 16384, bx * 32, m0);
@@ -1559,17 +1582,6 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
-// One decision for the `n` threads (whole warps) that meet at named barrier `bar`.
-__device__ __forceinline__ bool all_of(bool v, int bar, int n) {
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.and.pred p, %2, %3, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(r)
-        : "r"(v ? 1u : 0u), "r"(bar), "r"(n)
-        : "memory");
-    return r != 0;
-}
 
 // Persistent output projection + residual + LayerNorm (cpu.rs:300-313) for
 // dims up to 128: x += attn @ Wp + bp, ln = LayerNorm2(x). One CTA per SM
