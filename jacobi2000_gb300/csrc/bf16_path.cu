@@ -624,24 +624,49 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
     store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
 }
 
-// z0 (f32 [rows, HD]) -> zc (bf16 [cells, 48]): upsample along y then x
-// (cpu.rs:211-245), state channels appended (cpu.rs:339-342), zero padding.
+// to_cells' output (f32 [rows, HD]) -> the cell-head input zc (bf16 [cells,
+// 48]): upsample along y then x (cpu.rs:211-245; weights (i + 1/2) / P, the
+// far neighbour clamped to the grid), the state appended split exactly into
+// bf16 parts (cpu.rs:339-342), zero padding. One CTA per 8 x 16 cell tile
+// (the conv tiles): the 5 x 3 tokens it reads are staged in shared memory
+// (row pitch HD + 4 floats against bank conflicts), thread r makes cell
+// (y0 + r / 8, x0 + r % 8).
+constexpr int kUpTokY = kConvTY / 4 + 1, kUpTokX = kConvTX / 4 + 1, kUpPitch = 36;
+
 template <int HD, int C>
-__global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst, int n_inst,
-                                   long long NC, bf16* __restrict__ zc) {
-    static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh, "zc layout");
-    long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= NC) return;
-    const InstDev& I = inst[inst_of_cell(inst, n_inst, cell)];
-    long long cl = cell - I.cell0;
-    int y = (int)(cl / I.nx), x = (int)(cl % I.nx);
-    int yt = y / d.P, iy = y % d.P, xt = x / d.P, ix = x % d.P;
-    int yt2 = min(yt + 1, I.ty - 1), xt2 = min(xt + 1, I.tx - 1);
-    float wy = ((float)iy + 0.5f) / (float)d.P, wx = ((float)ix + 0.5f) / (float)d.P;
-    const float4* a = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt) * HD);
-    const float4* b = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt * I.tx + xt2) * HD);
-    const float4* c = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt) * HD);
-    const float4* e = reinterpret_cast<const float4*>(z0 + (size_t)(I.row0 + yt2 * I.tx + xt2) * HD);
+__global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst,
+                                                          int n_inst, bf16* __restrict__ zc) {
+    static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh && HD + 4 <= kUpPitch, "zc layout");
+    constexpr int P = 4;  // patch (the BF16 path is built for 4); (i + 1/2) / 4 is exact as a product
+    __shared__ __align__(16) float win[kUpTokY * kUpTokX * kUpPitch];
+    const int tile = blockIdx.x;
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].ct0 <= tile) lo = mid; else hi = mid - 1;
+    }
+    const InstDev& I = inst[lo];
+    const int tiles_x = (I.nx + kConvTX - 1) / kConvTX;
+    const int tl = tile - I.ct0;
+    const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY;
+    const int ty0 = y0 / P, tx0 = x0 / P;
+    for (int e = threadIdx.x; e < kUpTokY * kUpTokX * (HD / 4); e += blockDim.x) {
+        const int q = e % (HD / 4), t = e / (HD / 4), ty = ty0 + t / kUpTokX, tx = tx0 + t % kUpTokX;
+        const bool in = ty < I.ty && tx < I.tx;
+        cp_async16(win + t * kUpPitch + 4 * q, in ? z0 + (size_t)(I.row0 + ty * I.tx + tx) * HD + 4 * q : z0, in);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int r = threadIdx.x;
+    const int y = y0 + r / kConvTX, x = x0 + r % kConvTX;
+    if (y >= I.ny || x >= I.nx) return;
+    const int yt = y / P, iy = y % P, xt = x / P, ix = x % P;
+    const int yt2 = min(yt + 1, I.ty - 1), xt2 = min(xt + 1, I.tx - 1);
+    const float wy = ((float)iy + 0.5f) * (1.0f / P), wx = ((float)ix + 0.5f) * (1.0f / P);
+    auto tok = [&](int ty, int tx) {
+        return reinterpret_cast<const float4*>(win + ((ty - ty0) * kUpTokX + (tx - tx0)) * kUpPitch);
+    };
+    const float4 *a = tok(yt, xt), *b = tok(yt, xt2), *c = tok(yt2, xt), *e = tok(yt2, xt2);
     const float uy = 1.0f - wy, ux = 1.0f - wx;
     float vals[kZcCh];
 #pragma unroll
@@ -654,7 +679,7 @@ __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const I
         vals[4 * q + 2] = (A.z * uy + Cc.z * wy) * ux + (B.z * uy + E.z * wy) * wx;
         vals[4 * q + 3] = (A.w * uy + Cc.w * wy) * ux + (B.w * uy + E.w * wy) * wx;
     }
-    const size_t plane = (size_t)I.nx * I.ny;
+    const size_t plane = (size_t)I.nx * I.ny, cl = (size_t)y * I.nx + x;
 #pragma unroll
     for (int ch = 0; ch < C; ch++) {
         const float sv = I.state[ch * plane + cl];
@@ -663,7 +688,7 @@ __global__ void bf_upsample_kernel(Dims d, const float* __restrict__ z0, const I
         vals[kZcState + 3 + ch] = sv - hi;  // exact in f32; rounded to bf16 below
         vals[kZcState + 6 + ch] = hi;
     }
-    uint4* o = reinterpret_cast<uint4*>(zc + (size_t)cell * kZcCh);
+    uint4* o = reinterpret_cast<uint4*>(zc + ((size_t)I.cell0 + cl) * kZcCh);
 #pragma unroll
     for (int q = 0; q < kZcCh / 8; q++) {
         uint32_t w[4];
@@ -2697,10 +2722,9 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         tc_gemm_kernel<EPI_F32><<<dim3(gm, 1), 128, smem, s>>>(m_t1, m_z0_out, wtc, D, d.HD, R, ep, p.err);
         check_launch("tc_to_cells");
     }
-    const long long NC = p.NC;
     {
         KScope k("bf_upsample", s);
-        bf_upsample_kernel<32, 3><<<(unsigned)((NC + 255) / 256), 256, 0, s>>>(d, p.z0, p.inst, n, NC, zc);
+        bf_upsample_kernel<32, 3><<<(unsigned)p.n_ctiles, 128, 0, s>>>(d, p.z0, p.inst, n, zc);
         check_launch("bf_upsample");
     }
     {
