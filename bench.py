@@ -63,6 +63,7 @@ def parse_args():
     ap.add_argument("--served-requests", type=int, default=240)
     ap.add_argument("--served-fp32-requests", type=int, default=24)
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-task batch measurement")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the 256x256 error report against the f64 oracle")
     return ap.parse_args()
 
 
@@ -352,6 +353,52 @@ def mixed_batch_bench(args, steps=3):
     return out
 
 
+def accuracy_c3(ticks=(10, 25, 50)):
+    """Config: 256x256 checkpoints at dim 128 / 4 layers (seed 0) and dim 256 /
+    6 layers (seed 1), 8 drops, mass + energy projection each tick. Per-field
+    normwise error (max|a - b| / max|b|) of the BF16 and the FP32 path against
+    the f64 oracle for one forward and along a 50-tick rollout, and the largest
+    relative energy violation of each."""
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.checkpoint import parse_config, synthetic_checkpoint, write_safetensors_bytes, meta_of
+    from jacobi2000_gb300.ic import random_drops
+    from oracle import oracle
+
+    def err(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        return [float(np.abs(a[i] - b[i]).max() / max(np.abs(b[i]).max(), 1e-30)) for i in range(3)]
+
+    oracle.set_threads(os.cpu_count() or 1)
+    oracle.set_attention_mode("gather")
+    me = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+    H = max(ticks)
+    out = []
+    for dim, layers, seed in ((128, 4, 0), (256, 6, 1)):
+        t, cj = synthetic_checkpoint(256, dim, layers, seed)
+        cfg = parse_config(cj, t)
+        x0 = random_drops(cfg, seed=7)
+        meta = meta_of(cfg)
+        t0 = time.perf_counter()
+        orc = oracle.OracleModel(cfg, t)
+        want_fwd = orc.forward(x0.astype(np.float64), meta.astype(np.float64), f64=True)
+        _, e64, v64, traj64 = orc.rollout(x0.astype(np.float64), meta.astype(np.float64), H, oracle.MASS | oracle.ENERGY,
+                                          f64=True, trajectory=True)
+        oracle_s = time.perf_counter() - t0
+        row = {"model": f"dim {dim}, {layers} layers, 256x256, seed {seed}", "oracle_s": oracle_s,
+               "f64_max_energy_violation": float(v64), "paths": {}}
+        for name, prec in (("bf16", engine.BF16), ("fp32", engine.FP32)):
+            with engine.Model.from_bytes(write_safetensors_bytes(t), cj, prec) as m:
+                fwd = m.forward(x0, meta)
+                final, e, traj = m.rollout(x0, meta, H, me, trajectory=True)
+            viol = float(np.max(np.maximum((e[1:] - e[:-1] * cfg.energy_r_max) / e[:-1], 0.0)))
+            row["paths"][name] = {"forward": max(err(fwd, want_fwd)),
+                                  "rollout": {str(k): max(err(traj[k], traj64[k])) for k in ticks},
+                                  "max_energy_violation": viol}
+        out.append(row)
+    return {"measure": "max over fields of max|a - b| / max|b| against the f64 oracle", "ticks": list(ticks),
+            "cases": out}
+
+
 def cpu_sample(cfg, t, x0, meta, ticks: int):
     """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
     masked scan) on all host cores, over `ticks` ticks of one instance."""
@@ -513,6 +560,7 @@ def main():
 
     served = served_bench(args) if rank == 0 else None
     mixed = mixed_batch_bench(args) if rank == 0 and not args.no_mixed else None
+    accuracy = accuracy_c3() if rank == 0 and not args.no_accuracy else None
 
     cpu = None
     if rank == 0:
@@ -529,7 +577,7 @@ def main():
                 "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
                                "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,
-                "mixed_batch": mixed,
+                "mixed_batch": mixed, "accuracy": accuracy,
                 "gpu_launches": launches_per_step * args.steps,
                 "kernels": table, "peaks": pk_kind}
         print(json.dumps(line), flush=True)

@@ -17,6 +17,7 @@
 // no-swizzle core-matrix layout and each of the 9 taps is the same tile
 // addressed through a shifted shared-memory descriptor.
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -47,6 +48,14 @@ static uint16_t f2bf(float f) {
     if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);  // NaN stays NaN
     u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
     return (uint16_t)(u >> 16);
+}
+
+// f32 -> IEEE binary16 bits, round to nearest even (host)
+static uint16_t f2h(float f) {
+    const __half h = __float2half_rn(f);
+    uint16_t u;
+    std::memcpy(&u, &h, 2);
+    return u;
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -142,10 +151,11 @@ static CUtensorMap halo_map(const void* base, int C, int nx, int ny) {
 // ---------------------------------------------------------------------------
 // device
 
-// bf16 cell-head input channels: 32 z, then the state split exactly into
-// bf16 parts, s = hi + lo: [hi (3), lo (3), hi (3)] multiplied by the conv1
-// weights [W_hi, W_hi, W_lo], so the state enters conv1 with ~16-bit rather
-// than 8-bit precision; the remaining 7 channels are zero.
+// Cell-head input channels (f16, conv1's operand type; f16 keeps 3 more
+// mantissa bits than bf16 and the values are far inside its range): 32 z,
+// then the state split exactly into f16 parts, s = hi + lo: [hi (3), lo (3),
+// hi (3)] multiplied by the conv1 weights [W_hi, W_hi, W_lo], so the state
+// enters conv1 with ~22-bit precision; the remaining 7 channels are zero.
 constexpr int kZcCh = 48;
 constexpr int kZcState = 32;
 constexpr int kHaloW = kConvTX + 2, kHaloH = kConvTY + 2;
@@ -624,10 +634,10 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
     store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
 }
 
-// to_cells' output (f32 [rows, HD]) -> the cell-head input zc (bf16 [cells,
-// 48]): upsample along y then x (cpu.rs:211-245; weights (i + 1/2) / P, the
-// far neighbour clamped to the grid), the state appended split exactly into
-// bf16 parts (cpu.rs:339-342), zero padding. One CTA per 8 x 16 cell tile
+// to_cells' output (f32 [rows, HD]) -> the cell-head input zc (f16 [cells,
+// 48], conv1's operand type): upsample along y then x (cpu.rs:211-245;
+// weights (i + 1/2) / P, the far neighbour clamped to the grid), the state
+// appended split exactly into f16 parts (cpu.rs:339-342), zero padding. One CTA per 8 x 16 cell tile
 // (the conv tiles): the 5 x 3 tokens it reads are staged in shared memory
 // (row pitch HD + 4 floats against bank conflicts), thread r makes cell
 // (y0 + r / 8, x0 + r % 8).
@@ -635,7 +645,7 @@ constexpr int kUpTokY = kConvTY / 4 + 1, kUpTokX = kConvTX / 4 + 1, kUpPitch = 3
 
 template <int HD, int C>
 __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst,
-                                                          int n_inst, bf16* __restrict__ zc) {
+                                                          int n_inst, __half* __restrict__ zc) {
     static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh && HD + 4 <= kUpPitch, "zc layout");
     constexpr int P = 4;  // patch (the BF16 path is built for 4); (i + 1/2) / 4 is exact as a product
     __shared__ __align__(16) float win[kUpTokY * kUpTokX * kUpPitch];
@@ -683,9 +693,9 @@ __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* _
 #pragma unroll
     for (int ch = 0; ch < C; ch++) {
         const float sv = I.state[ch * plane + cl];
-        const float hi = bf2f(__float2bfloat16(sv));
+        const float hi = __half2float(__float2half_rn(sv));
         vals[kZcState + ch] = hi;
-        vals[kZcState + 3 + ch] = sv - hi;  // exact in f32; rounded to bf16 below
+        vals[kZcState + 3 + ch] = sv - hi;  // exact in f32; rounded to f16 below
         vals[kZcState + 6 + ch] = hi;
     }
     uint4* o = reinterpret_cast<uint4*>(zc + ((size_t)I.cell0 + cl) * kZcCh);
@@ -694,7 +704,7 @@ __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* _
         uint32_t w[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            __nv_bfloat162 h = __floats2bfloat162_rn(vals[8 * q + 2 * i], vals[8 * q + 2 * i + 1]);
+            __half2 h = __floats2half2_rn(vals[8 * q + 2 * i], vals[8 * q + 2 * i + 1]);
             w[i] = *reinterpret_cast<uint32_t*>(&h);
         }
         o[q] = make_uint4(w[0], w[1], w[2], w[3]);
@@ -2155,7 +2165,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
             tc::mbar_expect_tx(&w_full, (uint32_t)9 * C * BN * 2);
             tc::bulk_load(sW, Wt, (uint32_t)9 * C * BN * 2, &w_full);
             bool good = tc::mbar_wait(&w_full, 0, err, &failed);
-            const uint32_t idesc = tc::idesc_bf16(128, BN);
+            const uint32_t idesc = tc::idesc_f16(128, BN);  // f16 input and weights
             const uint32_t w0 = tc::smem_u32(sW);
             for (int it = 0; it < my_tiles && good; it++) {
                 const int b = it & 1;
@@ -2338,16 +2348,11 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
         wtc = upload_bf16(arena, blocked(HD, D, HD, [&](int n, int kk) { return w[(size_t)n * D + kk]; }));
     }
     {
-        // conv1: per tap [48/8][32][8] over the zc channels: z (32), then the
-        // state's [hi, lo, hi] parts with weights [W_hi, W_hi, W_lo]
+        // conv1 (f16 operands): per tap [48/8][32][8] over the zc channels: z
+        // (32), then the state's [hi, lo, hi] parts with weights [W_hi, W_hi, W_lo]
         const auto& w = tget(t, "head.conv1.weight").data;  // [HD][HD+C][3][3]
         const int cin = HD + d.C;
-        auto bf_round = [](float v) {
-            uint32_t u = (uint32_t)f2bf(v) << 16;
-            float r;
-            std::memcpy(&r, &u, 4);
-            return r;
-        };
+        auto h_round = [](float v) { return __half2float(__float2half_rn(v)); };
         std::vector<uint16_t> o((size_t)9 * kZcCh * HD);
         size_t i = 0;
         for (int tap = 0; tap < 9; tap++)
@@ -2361,12 +2366,12 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
                         } else if (ch < kZcState + 9) {
                             const int part = (ch - kZcState) / 3, c = (ch - kZcState) % 3;
                             const float full = w[((size_t)n * cin + HD + c) * 9 + tap];
-                            const float hi = bf_round(full);
+                            const float hi = h_round(full);
                             v = part < 2 ? hi : full - hi;
                         }
-                        o[i++] = f2bf(v);
+                        o[i++] = f2h(v);
                     }
-        wc1 = upload_bf16(arena, o);
+        wc1 = upload_bf16(arena, o);  // f16 bits
     }
     cache_key_ = "d" + std::to_string(D) + "_l" + std::to_string(d.L) + "_f" + std::to_string(F) + "_r" +
                  std::to_string(d.radius) + "_k" + std::to_string(d.mask_kind) + "_g" + std::to_string(d.dilation);
@@ -2642,7 +2647,6 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     bf16* qkv = reinterpret_cast<bf16*>(p.bt[1]);
     bf16* attn = reinterpret_cast<bf16*>(p.bt[2]);
     bf16* t1 = reinterpret_cast<bf16*>(p.bt[3]);
-    bf16* zc = reinterpret_cast<bf16*>(p.bc[0]);
     float* c1 = reinterpret_cast<float*>(p.bc[1]);
     const CUtensorMap m_ln = rows_map(ln, D, R), m_attn = rows_map(attn, D, R), m_t1 = rows_map(t1, D, R);
     const CUtensorMap m_qkv_out = store_map(qkv, 3 * D, R, 3 * D, false), m_z0_out = store_map(p.z0, d.HD, R, d.HD, true);
@@ -2724,7 +2728,8 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     }
     {
         KScope k("bf_upsample", s);
-        bf_upsample_kernel<32, 3><<<(unsigned)p.n_ctiles, 128, 0, s>>>(d, p.z0, p.inst, n, zc);
+        bf_upsample_kernel<32, 3><<<(unsigned)p.n_ctiles, 128, 0, s>>>(d, p.z0, p.inst, n,
+                                                                       reinterpret_cast<__half*>(p.bc[0]));
         check_launch("bf_upsample");
     }
     {

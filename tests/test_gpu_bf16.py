@@ -90,3 +90,25 @@ def test_bf16_batch_equals_single():
         assert np.array_equal(final2, alone)
     for m in models:
         m.close()
+
+
+@pytest.mark.parametrize("dim,layers,seed", [(128, 4, 0), (256, 6, 1)])
+def test_bf16_and_fp32_forward_256x256_against_f64_oracle(dim, layers, seed):
+    """The 256x256 checkpoints (dim 128 / 4 layers and dim 256 / 6 layers):
+    one forward of each path against the f64 oracle (BF16 <= 1e-2, FP32 <=
+    1e-4 per field)."""
+    import os
+
+    from oracle import oracle as orc_mod
+
+    orc_mod.set_threads(os.cpu_count() or 1)
+    orc_mod.set_attention_mode("gather")
+    t, cj = synthetic_checkpoint(256, dim, layers, seed)
+    cfg = parse_config(cj, t)
+    x = random_drops(cfg, seed=11)
+    meta = meta_of(cfg)
+    want = OracleModel(cfg, t).forward(x.astype(np.float64), meta.astype(np.float64), f64=True)
+    for prec, tol in ((engine.BF16, TOL), (engine.FP32, 1e-4)):
+        with engine.Model.from_bytes(write_safetensors_bytes(t), cj, prec) as m:
+            got = m.forward(x, meta)
+        assert max(field_errors(got, want)) <= tol, (prec, field_errors(got, want))
