@@ -276,6 +276,76 @@ void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int
  * on the batch it runs in. */
 int32_t jc_autotune(int32_t enable);
 
+/* ---- Evaluation on the device ----------------------------------------------
+ * The `eval-metrics` loop (crates/engine-cli/src/eval.rs:126-176) with its
+ * reference solver and scores on the GPU: solvers::ShallowWater
+ * (crates/solvers/src/shallow_water.rs), engine::metrics
+ * (crates/engine/src/metrics.rs) and the model's rollout, side by side. */
+
+/* solvers::Params (crates/solvers/src/shallow_water.rs:16-29). */
+typedef struct {
+    int32_t nx, ny;
+    float dx, dt, g, depth, nu;
+} jc_sw_params;
+
+/* `steps` ShallowWater::step calls (shallow_water.rs:149-238) on each of
+ * `count` independent solver states, in place. states: [count][3][ny][nx], the
+ * planes h (total depth), u, v in physical units. The arithmetic is the
+ * reference's f32 arithmetic, operation for operation, so the results are
+ * bit-identical to it. jc_sw_run takes host buffers and blocks;
+ * jc_sw_run_device takes a device buffer, enqueues on `stream` (a
+ * cudaStream_t, null = legacy default stream) and returns. */
+jc_status jc_sw_run(const jc_sw_params* p, float* states, int32_t count, int32_t steps);
+jc_status jc_sw_run_device(const jc_sw_params* p, float* d_states, int32_t count, int32_t steps,
+                           void* stream);
+
+/* State::add_drop (shallow_water.rs:102-111) on one host h plane [ny][nx]:
+ * h += amp exp(-((x - cx)^2 + (y - cy)^2) / (2 sigma^2)), with the C
+ * library's expf as the reference's f32::exp. */
+jc_status jc_sw_add_drop(const jc_sw_params* p, float* h, float cx, float cy, float amp, float sigma);
+
+/* One Gaussian drop: centre in cell coordinates, amplitude, radius in cells. */
+typedef struct {
+    float cx, cy, amp, sigma;
+} jc_drop;
+
+/* One eval-metrics row (eval.rs:101-108, 158-171): Pearson correlation over
+ * (h, u, v) and over h, amplitude ratio (model peak |h| over solver peak
+ * |h|), wavefront lag in cells (cross-correlation of the radial |h|
+ * profiles, sub-cell refined) and bias ((mean model h - mean solver h) / std
+ * solver h). */
+typedef struct {
+    float corr, corr_h, amplitude_ratio, lag, bias;
+} jc_eval_row;
+
+/* Scores `count` normalized model states x [count][3][ny][nx] against solver
+ * states truth [count][3][ny][nx] (physical h, u, v), each about its drop
+ * centre centres[2 k], centres[2 k + 1]. cfg supplies nx, ny and the
+ * normalizer. Host buffers. Peaks, amplitude ratios, radial profiles and
+ * the f32 means and standard deviation of the bias follow metrics.rs's
+ * summation order exactly; the f64 correlation sums are tree-ordered, which
+ * can move a correlation by one f32 rounding step. */
+jc_status jc_eval_score(const jc_config* cfg, const float* x, const float* truth, const float* centres,
+                        int32_t count, jc_eval_row* rows);
+
+/* An evaluator for one model: device buffers for up to max_trajectories
+ * trajectories and a batch runner for the model's rollouts. */
+typedef struct jc_eval jc_eval;
+jc_status jc_eval_create(jc_model* m, int32_t max_trajectories, jc_eval** out);
+void jc_eval_destroy(jc_eval* e);
+
+/* eval-metrics for the given drops. Trajectory k starts from State::flat
+ * (h = depth, u = v = 0) plus drops[k]; the reference solver and the model
+ * (step, then the projections in `flags`, per tick) advance side by side in
+ * one captured graph, and at each horizon every trajectory is scored as in
+ * jc_eval_score. horizons: strictly ascending, >= 1. rows: [n_horizons][n].
+ * max_violation (optional): the largest relative energy violation
+ * max((E_t - E_{t-1} r_max) / E_{t-1}, 0) over all trajectories and ticks.
+ * The drops are the caller's: the reference's trajectory sampler and its
+ * horizon filter (eval.rs:126-134) live on the caller's side. */
+jc_status jc_eval_run(jc_eval* e, const jc_drop* drops, int32_t n, const int32_t* horizons,
+                      int32_t n_horizons, uint32_t flags, jc_eval_row* rows, double* max_violation);
+
 /* Thread-local description of the last failure on this thread ("" if none). */
 const char* jc_last_error(void);
 

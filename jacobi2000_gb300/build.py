@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr",
          "-I", str(ROOT / "include")]
 
-SOURCES = ["fp32_path.cu", "bf16_path.cu", "runtime.cu", "server.cu", "recon.cu", "noalloc.cu", "capi.cpp"]
+SOURCES = ["fp32_path.cu", "bf16_path.cu", "runtime.cu", "server.cu", "recon.cu", "noalloc.cu", "evaluate.cu",
+           "capi.cpp"]
 
 
 def _deps() -> list[Path]:

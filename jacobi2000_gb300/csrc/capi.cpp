@@ -234,6 +234,47 @@ void jc_project_energy(float* x, double prev_energy, const jc_config* c, int64_t
     }
 }
 
+jc_status jc_sw_run(const jc_sw_params* p, float* states, int32_t count, int32_t steps) {
+    if (!p) return fail(JC_BAD_ARGUMENT, "params are null");
+    return guard([&] { jc::sw_run_host(*p, states, count, steps); });
+}
+
+jc_status jc_sw_run_device(const jc_sw_params* p, float* d_states, int32_t count, int32_t steps, void* stream) {
+    if (!p) return fail(JC_BAD_ARGUMENT, "params are null");
+    return guard([&] { jc::sw_run_device(*p, d_states, count, steps, (cudaStream_t)stream); });
+}
+
+jc_status jc_sw_add_drop(const jc_sw_params* p, float* h, float cx, float cy, float amp, float sigma) {
+    if (!p) return fail(JC_BAD_ARGUMENT, "params are null");
+    return guard([&] { jc::sw_add_drop_host(*p, h, cx, cy, amp, sigma); });
+}
+
+jc_status jc_eval_score(const jc_config* cfg, const float* x, const float* truth, const float* centres,
+                        int32_t count, jc_eval_row* rows) {
+    if (!cfg) return fail(JC_BAD_ARGUMENT, "config is null");
+    return guard([&] { jc::eval_score_host(*cfg, x, truth, centres, count, rows); });
+}
+
+jc_status jc_eval_create(jc_model* m, int32_t max_trajectories, jc_eval** out) {
+    if (!m || !out) return fail(JC_BAD_ARGUMENT, "null argument");
+    *out = nullptr;
+    return guard([&] { *out = jc::eval_create(m, max_trajectories); });
+}
+
+void jc_eval_destroy(jc_eval* e) {
+    if (!e) return;
+    try {
+        jc::eval_destroy(e);
+    } catch (...) {
+    }
+}
+
+jc_status jc_eval_run(jc_eval* e, const jc_drop* drops, int32_t n, const int32_t* horizons, int32_t n_horizons,
+                      uint32_t flags, jc_eval_row* rows, double* max_violation) {
+    if (!e) return fail(JC_BAD_ARGUMENT, "evaluator is null");
+    return guard([&] { jc::eval_run(e, drops, n, horizons, n_horizons, flags, rows, max_violation); });
+}
+
 const char* jc_last_error(void) { return g_last_error.c_str(); }
 
 int32_t jc_autotune(int32_t enable) {

@@ -948,6 +948,7 @@ void Batch::enqueue(const Plan& p, cudaStream_t s, bool capture) const {
             models_[G.model]->forward_pack(v, kWriteNextState, s);
             projection(dims_, v, 0, s);
         }
+        if (hook_) hook_->after_tick(t, s);
     }
     if (p.recons.empty()) return;
     const int nrec = (int)p.recons.size();
@@ -1029,7 +1030,7 @@ void Batch::upload_recon(const Plan& p, const jc_instance* in, bool device_ptrs,
                    "reconstruct meta", JC_MAP);
 }
 
-void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t s) {
+void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t s, TickHook* hook) {
     if (!s) s = stream_;
     Plan p = plan(in, n);
     if (n == 0) return;
@@ -1076,17 +1077,27 @@ void Batch::rollout(const jc_instance* in, int n, bool device_ptrs, cudaStream_t
             key.push_back((long long)(uintptr_t)d.pos);
         }
     }
+    if (hook) {
+        std::vector<float*> st(n, nullptr);
+        for (size_t k = 0; k < p.order.size(); k++) st[p.order[k]] = ws_.states + p.state_off[k];
+        hook->bind(st, s);
+        key.push_back(-2000000000LL);
+        key.push_back(hook->key());
+    }
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         cudaGraph_t g;
         cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+        hook_ = hook;
         try {
             enqueue(p, s, true);
         } catch (...) {
+            hook_ = nullptr;
             cudaStreamEndCapture(s, &g);
             if (g) cudaGraphDestroy(g);
             throw;
         }
+        hook_ = nullptr;
         cuda_check(cudaStreamEndCapture(s, &g), "end capture");
         cudaGraphExec_t ge;
         cudaError_t err = cudaGraphInstantiate(&ge, g, 0);

@@ -135,13 +135,27 @@ class Model {
     cudaGraphExec_t graph_for(const GraphKey& k, double* e, float* t);
 };
 
+// Work that a batch rollout enqueues after every tick, inside its captured
+// graph (the evaluator steps its solver and scores there).
+struct TickHook {
+    virtual ~TickHook() = default;
+    // Before capture or launch: per caller instance index, the device state
+    // that the tick loop updates in place. Enqueues any upload on `s`.
+    virtual void bind(const std::vector<float*>& states, cudaStream_t s) = 0;
+    // After tick t (1-based) of every instance.
+    virtual void after_tick(int t, cudaStream_t s) const = 0;
+    // Identifies the launches after_tick makes (buffers, shapes), for the
+    // graph cache.
+    virtual long long key() const = 0;
+};
+
 // Many instances of (possibly) different grids, one launch sequence per tick.
 // Instances whose models share every tensor but `pos` share launches.
 class Batch {
    public:
     Batch(jc_model* const* models, int n_models, int max_inst, long long max_cells);
     ~Batch();
-    void rollout(const jc_instance* inst, int n, bool device_ptrs, cudaStream_t s);
+    void rollout(const jc_instance* inst, int n, bool device_ptrs, cudaStream_t s, TickHook* hook = nullptr);
     std::map<std::string, std::pair<int, double>> profile(const jc_instance* inst, int n, bool device_ptrs);
 
    private:
@@ -195,6 +209,7 @@ class Batch {
     void upload_recon(const Plan& p, const jc_instance* in, bool device_ptrs, cudaStream_t s);
     void prepare_maps(const Plan& p, cudaStream_t s) const;
     std::map<std::vector<long long>, cudaGraphExec_t> graphs_;
+    const TickHook* hook_ = nullptr;  // set while a hooked rollout is captured
 };
 
 // Serving loop (server.cu).
@@ -204,6 +219,18 @@ void server_destroy(jc_server* s);
 uint64_t server_submit(jc_server* s, const jc_request* r);
 void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* info, double timeout);
 void server_stats(jc_server* s, jc_server_stats* st);
+
+// Evaluation path (evaluate.cu): the reference solver, the scores and the
+// evaluator behind jc_sw_*, jc_eval_score and jc_eval_*.
+void sw_run_host(const jc_sw_params& p, float* states, int count, int steps);
+void sw_run_device(const jc_sw_params& p, float* d_states, int count, int steps, cudaStream_t s);
+void sw_add_drop_host(const jc_sw_params& p, float* h, float cx, float cy, float amp, float sigma);
+void eval_score_host(const jc_config& c, const float* x, const float* truth, const float* centres, int count,
+                     jc_eval_row* rows);
+jc_eval* eval_create(jc_model* m, int max_traj);
+void eval_destroy(jc_eval* e);
+void eval_run(jc_eval* e, const jc_drop* drops, int n, const int32_t* horizons, int nh, uint32_t flags,
+              jc_eval_row* rows, double* max_violation);
 
 // The FP32 forward of m's own grid with every buffer in the library's fixed
 // no-alloc scratch array (noalloc.cu); allocates nothing.

@@ -427,3 +427,146 @@ class Server:
         st = JcServerStats()
         _check(self._L.jc_server_get_stats(self._h, C.byref(st)))
         return {f: getattr(st, f) for f, _ in JcServerStats._fields_}
+
+
+# ---- evaluation on the device (jc_sw_*, jc_eval_*) -------------------------------
+
+class JcSwParams(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32)] + [(n, C.c_float) for n in ("dx", "dt", "g", "depth", "nu")]
+
+
+class JcDrop(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("cx", "cy", "amp", "sigma")]
+
+
+class JcEvalRow(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("corr", "corr_h", "amplitude_ratio", "lag", "bias")]
+
+
+EVAL_FIELDS = [f for f, _ in JcEvalRow._fields_]
+EXPORTED += ["jc_sw_run", "jc_sw_run_device", "jc_sw_add_drop", "jc_eval_score", "jc_eval_create", "jc_eval_destroy",
+             "jc_eval_run"]
+
+
+def _declare_eval(L):
+    if getattr(L, "_eval_declared", False):
+        return
+    vp = C.c_void_p
+    F = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    swp = C.POINTER(JcSwParams)
+    L.jc_sw_run.argtypes = [swp, F, C.c_int32, C.c_int32]
+    L.jc_sw_run_device.argtypes = [swp, vp, C.c_int32, C.c_int32, vp]
+    L.jc_sw_add_drop.argtypes = [swp, F, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.jc_eval_score.argtypes = [C.POINTER(JcConfig), F, F, F, C.c_int32, C.POINTER(JcEvalRow)]
+    L.jc_eval_create.argtypes = [vp, C.c_int32, C.POINTER(vp)]
+    L.jc_eval_destroy.argtypes = [vp]
+    L.jc_eval_destroy.restype = None
+    L.jc_eval_run.argtypes = [vp, C.POINTER(JcDrop), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint32,
+                              C.POINTER(JcEvalRow), C.POINTER(C.c_double)]
+    for fn in ("jc_sw_run", "jc_sw_run_device", "jc_sw_add_drop", "jc_eval_score", "jc_eval_create", "jc_eval_run"):
+        getattr(L, fn).restype = C.c_int
+    L._eval_declared = True
+
+
+def sw_params(config: JcConfig) -> JcSwParams:
+    """solvers::Params of a model's config (crates/engine/src/config.rs:102-104)."""
+    return JcSwParams(config.nx, config.ny, config.dx, config.dt, config.g, config.depth, config.nu)
+
+
+def sw_flat(p: JcSwParams, count: int = 1) -> np.ndarray:
+    """State::flat for `count` solver states: [count, 3, ny, nx], h = depth."""
+    s = np.zeros((count, 3, p.ny, p.nx), dtype=np.float32)
+    s[:, 0] = np.float32(p.depth)
+    return s
+
+
+def sw_add_drop(p: JcSwParams, h: np.ndarray, cx: float, cy: float, amp: float, sigma: float) -> None:
+    """State::add_drop in place on an h plane [ny, nx] (float32, contiguous)."""
+    L = load_library()
+    _declare_eval(L)
+    if h.dtype != np.float32 or not h.flags.c_contiguous or h.size != p.nx * p.ny:
+        raise ValueError("h must be a contiguous float32 [ny, nx] plane")
+    _check(L.jc_sw_add_drop(C.byref(p), h.reshape(-1), cx, cy, amp, sigma))
+
+
+def sw_run(p: JcSwParams, states: np.ndarray, steps: int) -> np.ndarray:
+    """`steps` reference solver ticks of every state ([count, 3, ny, nx] or
+    [3, ny, nx]) on the GPU; returns the advanced states."""
+    L = load_library()
+    _declare_eval(L)
+    s = np.array(states, dtype=np.float32, copy=True, order="C")
+    count = s.size // (3 * p.nx * p.ny)
+    if count * 3 * p.nx * p.ny != s.size:
+        raise ValueError("states must be [count, 3, ny, nx]")
+    _check(L.jc_sw_run(C.byref(p), s.reshape(-1), count, int(steps)))
+    return s
+
+
+def eval_score(config: JcConfig, x, truth, centres) -> np.ndarray:
+    """Scores model states x [count, 3, ny, nx] (normalized) against solver
+    states [count, 3, ny, nx] about centres [count, 2]; returns a structured
+    array with the fields of EVAL_FIELDS."""
+    L = load_library()
+    _declare_eval(L)
+    n = config.nx * config.ny
+    xa = np.ascontiguousarray(x, dtype=np.float32).reshape(-1)
+    ta = np.ascontiguousarray(truth, dtype=np.float32).reshape(-1)
+    ca = np.ascontiguousarray(centres, dtype=np.float32).reshape(-1)
+    count = xa.size // (3 * n)
+    if xa.size != count * 3 * n or ta.size != xa.size or ca.size != 2 * count:
+        raise ValueError("shape mismatch")
+    rows = (JcEvalRow * max(count, 1))()
+    _check(L.jc_eval_score(C.byref(config), xa, ta, ca, count, rows))
+    return _rows_array(rows, count)
+
+
+def _rows_array(rows, count: int) -> np.ndarray:
+    out = np.zeros(count, dtype=[(f, np.float32) for f in EVAL_FIELDS])
+    for k in range(count):
+        for f in EVAL_FIELDS:
+            out[f][k] = getattr(rows[k], f)
+    return out
+
+
+class Evaluator:
+    """eval-metrics on the device for one model (jc_eval_*): the reference
+    solver and the model advance side by side and every trajectory is scored
+    at each horizon."""
+
+    def __init__(self, model: Model, max_trajectories: int):
+        L = load_library()
+        _declare_eval(L)
+        self._L = L
+        self.model = model
+        self.max_trajectories = int(max_trajectories)
+        h = C.c_void_p()
+        _check(L.jc_eval_create(model._h, self.max_trajectories, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.jc_eval_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, drops, horizons, flags: int = PROJECT_MASS):
+        """drops: [(cx, cy, amp, sigma)]. Returns (rows [len(horizons),
+        len(drops)] structured by EVAL_FIELDS, max relative energy violation)."""
+        n, nh = len(drops), len(horizons)
+        d = (JcDrop * max(n, 1))(*[JcDrop(*map(float, dr)) for dr in drops])
+        hz = (C.c_int32 * max(nh, 1))(*[int(h) for h in horizons])
+        rows = (JcEvalRow * max(n * nh, 1))()
+        viol = C.c_double(0.0)
+        _check(self._L.jc_eval_run(self._h, d, n, hz, nh, int(flags), rows, C.byref(viol)))
+        return _rows_array(rows, n * nh).reshape(nh, n), float(viol.value)

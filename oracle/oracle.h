@@ -101,6 +101,35 @@ double orc_energy_sum64(const float* x, const orc_config* c, int n);
 void   orc_project_mass_sum64(float* x, double target, int n);
 void   orc_project_energy_sum64(float* x, double prev_energy, const orc_config* c, int n);
 
+/* ---- evaluation path (solver.c) ----
+ * Shallow-water solver parameters (crates/solvers/src/shallow_water.rs:16-29). */
+typedef struct {
+    int nx, ny;
+    float dx, dt, g, depth, nu;
+} orc_sw_params;
+
+/* State::add_drop: h += amp exp(-r^2 / (2 sigma^2)), expf of the C library. */
+void   orc_sw_add_drop(const orc_sw_params* p, float* h, float cx, float cy, float amp, float sigma);
+double orc_sw_mass(const float* h, int n);
+/* `steps` ShallowWater::step calls on the planes h, u, v [ny, nx]. */
+void   orc_sw_steps(const orc_sw_params* p, float* h, float* u, float* v, int steps);
+
+/* metrics.rs restated. */
+float orc_correlation(const float* a, const float* b, int n);
+float orc_peak(const float* f, int n);
+float orc_mean(const float* f, int n);
+float orc_std_dev(const float* f, int n);
+float orc_bias(const float* model, const float* solver, int n);
+int   orc_radial_profile(const float* f, int nx, int ny, float cx, float cy, double* out, int cap);
+float orc_xcorr_lag(const double* model, const double* solver, int n, int max_lag);
+void  orc_encode(const float norm_mean[3], const float norm_std[3], float norm_depth, const float* h,
+                 const float* u, const float* v, int n, float* out);
+/* One eval-metrics row: corr (h,u,v), corr (h), amplitude ratio, wavefront
+ * lag (cells), bias. */
+void  orc_eval_score(const float norm_mean[3], const float norm_std[3], float norm_depth, int nx, int ny,
+                     const float* x, const float* h, const float* u, const float* v, float cx, float cy,
+                     float row[5]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,7 +47,7 @@ class _Weights(C.Structure):
 
 def build(quiet: bool = True) -> Path:
     """Compile oracle.c with its Makefile (gcc, OpenMP, no FMA contraction)."""
-    srcs = [HERE / "oracle.c", HERE / "oracle_impl.inc", HERE / "oracle.h"]
+    srcs = [HERE / "oracle.c", HERE / "oracle_impl.inc", HERE / "solver.c", HERE / "oracle.h"]
     if LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return LIB_PATH
     out = subprocess.run(["make", "-C", str(HERE)], capture_output=True, text=True)
@@ -209,6 +209,167 @@ class OracleModel:
         else:
             lib().orc_project_energy_f32(y, float(prev_energy), C.byref(self._c), self.cfg.cells)
         return y.reshape(np.shape(x))
+
+
+# ---- evaluation path (solver.c): the reference solver and the metrics ----
+
+class _SwParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int)] + [(n, C.c_float) for n in ("dx", "dt", "g", "depth", "nu")]
+
+
+def _bind_eval(L):
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    swp = C.POINTER(_SwParams)
+    L.orc_sw_add_drop.argtypes = [swp, f32p, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.orc_sw_mass.argtypes = [f32p, C.c_int]
+    L.orc_sw_mass.restype = C.c_double
+    L.orc_sw_steps.argtypes = [swp, f32p, f32p, f32p, C.c_int]
+    for fn in ("orc_correlation", "orc_bias"):
+        getattr(L, fn).argtypes = [f32p, f32p, C.c_int]
+        getattr(L, fn).restype = C.c_float
+    for fn in ("orc_peak", "orc_mean", "orc_std_dev"):
+        getattr(L, fn).argtypes = [f32p, C.c_int]
+        getattr(L, fn).restype = C.c_float
+    L.orc_radial_profile.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, f64p, C.c_int]
+    L.orc_radial_profile.restype = C.c_int
+    L.orc_xcorr_lag.argtypes = [f64p, f64p, C.c_int, C.c_int]
+    L.orc_xcorr_lag.restype = C.c_float
+    fa3 = C.c_float * 3
+    L.orc_encode.argtypes = [fa3, fa3, C.c_float, f32p, f32p, f32p, C.c_int, f32p]
+    L.orc_eval_score.argtypes = [fa3, fa3, C.c_float, C.c_int, C.c_int, f32p, f32p, f32p, f32p, C.c_float,
+                                 C.c_float, f32p]
+
+
+def _elib():
+    L = lib()
+    if not getattr(L, "_eval_bound", False):
+        _bind_eval(L)
+        L._eval_bound = True
+    return L
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def sw_params(cfg) -> _SwParams:
+    """solvers::Params of a model config (crates/engine/src/config.rs:102-104)."""
+    p = _SwParams()
+    p.nx, p.ny = int(cfg.nx), int(cfg.ny)
+    p.dx, p.dt, p.g, p.depth, p.nu = float(cfg.dx), float(cfg.dt), float(cfg.g), float(cfg.depth), float(cfg.nu)
+    return p
+
+
+def sw_flat(p: _SwParams, count: int = 1) -> np.ndarray:
+    """State::flat for `count` states: [count, 3, ny, nx] (h = depth, u = v = 0)."""
+    s = np.zeros((count, 3, p.ny, p.nx), dtype=np.float32)
+    s[:, 0] = np.float32(p.depth)
+    return s
+
+
+def sw_add_drop(p: _SwParams, h: np.ndarray, cx: float, cy: float, amp: float, sigma: float) -> None:
+    """In place on the h plane [ny, nx] (float32, contiguous)."""
+    assert h.dtype == np.float32 and h.flags.c_contiguous
+    _elib().orc_sw_add_drop(C.byref(p), h.reshape(-1), cx, cy, amp, sigma)
+
+
+def sw_steps(p: _SwParams, state: np.ndarray, steps: int) -> None:
+    """`steps` solver ticks in place on one state [3, ny, nx] (float32)."""
+    assert state.dtype == np.float32 and state.flags.c_contiguous and state.shape == (3, p.ny, p.nx)
+    h, u, v = state[0], state[1], state[2]
+    _elib().orc_sw_steps(C.byref(p), h, u, v, int(steps))
+
+
+def sw_mass(h) -> float:
+    h = _f32(h).ravel()
+    return _elib().orc_sw_mass(h, h.size)
+
+
+def correlation(a, b) -> float:
+    a, b = _f32(a).ravel(), _f32(b).ravel()
+    return _elib().orc_correlation(a, b, a.size)
+
+
+def peak(f) -> float:
+    f = _f32(f).ravel()
+    return _elib().orc_peak(f, f.size)
+
+
+def mean(f) -> float:
+    f = _f32(f).ravel()
+    return _elib().orc_mean(f, f.size)
+
+
+def std_dev(f) -> float:
+    f = _f32(f).ravel()
+    return _elib().orc_std_dev(f, f.size)
+
+
+def bias(model, solver) -> float:
+    a, b = _f32(model).ravel(), _f32(solver).ravel()
+    return _elib().orc_bias(a, b, a.size)
+
+
+def radial_profile(f, nx: int, ny: int, cx: float, cy: float) -> np.ndarray:
+    out = np.zeros(nx + ny + 2, dtype=np.float64)
+    k = _elib().orc_radial_profile(_f32(f).ravel(), nx, ny, cx, cy, out, out.size)
+    return out[:k]
+
+
+def xcorr_lag(model_prof, solver_prof, max_lag: int = 8) -> float:
+    m = np.ascontiguousarray(model_prof, dtype=np.float64)
+    s = np.ascontiguousarray(solver_prof, dtype=np.float64)
+    return _elib().orc_xcorr_lag(m, s, m.size, int(max_lag))
+
+
+def _norm_args(cfg):
+    fa3 = C.c_float * 3
+    return fa3(*[float(v) for v in cfg.norm_mean]), fa3(*[float(v) for v in cfg.norm_std]), float(cfg.norm_depth)
+
+
+def encode(cfg, truth) -> np.ndarray:
+    """Normalizer::encode of a solver state [3, ny, nx] -> [3, ny, nx]."""
+    t = _f32(truth).reshape(3, -1)
+    out = np.empty(t.size, dtype=np.float32)
+    nm, ns, nd = _norm_args(cfg)
+    _elib().orc_encode(nm, ns, nd, t[0], t[1], t[2], t.shape[1], out)
+    return out.reshape(np.shape(truth))
+
+
+def eval_score(cfg, x, truth, cx: float, cy: float) -> np.ndarray:
+    """(corr, corr_h, amplitude_ratio, lag, bias) of model state x against the
+    solver state `truth` (eval.rs:158-171)."""
+    x = _f32(x).ravel()
+    t = _f32(truth).reshape(3, -1)
+    row = np.zeros(5, dtype=np.float32)
+    nm, ns, nd = _norm_args(cfg)
+    _elib().orc_eval_score(nm, ns, nd, int(cfg.nx), int(cfg.ny), x, t[0], t[1], t[2], cx, cy, row)
+    return row
+
+
+def eval_metrics(model: "OracleModel", drops, horizons, flags: int, meta):
+    """The eval-metrics loop (crates/engine-cli/src/eval.rs:126-176) for the
+    given drops (cx, cy, amp, sigma): returns rows [len(horizons), len(drops), 5]
+    and the largest relative energy violation over all rollouts."""
+    cfg = model.cfg
+    p = sw_params(cfg)
+    horizons = sorted(int(h) for h in horizons)
+    last = horizons[-1]
+    rows = np.zeros((len(horizons), len(drops), 5), dtype=np.float32)
+    worst = 0.0
+    for j, (cx, cy, amp, sigma) in enumerate(drops):
+        truth = sw_flat(p)[0]
+        sw_add_drop(p, truth[0], cx, cy, amp, sigma)
+        x0 = encode(cfg, truth)
+        _, _, viol, traj = model.rollout(x0, meta, last, flags, trajectory=True)
+        worst = max(worst, viol)
+        t_done = 0
+        for i, hz in enumerate(horizons):
+            sw_steps(p, truth, hz - t_done)
+            t_done = hz
+            rows[i, j] = eval_score(cfg, traj[hz], truth, cx, cy)
+    return rows, worst
 
 
 def identity_config(n: int, g: float = 9.81, r_max: float = 1.0):

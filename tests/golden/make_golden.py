@@ -139,6 +139,58 @@ def main(ref_root: Path) -> None:
                                                     if not k.endswith("_f64")})
     np.savez_compressed(HERE / "extra_f64.npz", **{k: v for k, v in out.items() if k.endswith("_f64")})
     print("wrote", sorted(out))
+    metrics_golden(ref_root)
+
+
+def metrics_golden(ref_root: Path) -> None:
+    """3. ``metrics.npz``: the eval-metrics scores of fixed fields, computed by
+    the reference's Python scoring twin (training/jacobi2000_pt/metrics.py,
+    the formulas of crates/engine/src/metrics.rs). A 48x40 solver-like state
+    (two Gaussian drops on depth 1, small seeded u and v) is the truth; the
+    model state is the same with the drops widened and shifted (a lagging,
+    weaker wave) plus seeded noise."""
+    sys.path.insert(0, str(ref_root / "training"))
+    from jacobi2000_pt import metrics as M
+
+    nx, ny, cx, cy = 48, 40, 22.3, 19.6
+    mean = np.array([0.0008, 0.0004, 0.0005], dtype=np.float32)
+    std = np.array([0.0063, 0.0138, 0.0135], dtype=np.float32)
+    depth = np.float32(1.0)
+    rng = np.random.default_rng(11)
+    yy, xx = np.meshgrid(np.arange(ny, dtype=np.float32), np.arange(nx, dtype=np.float32), indexing="ij")
+
+    def ring(r0, w, amp):
+        r = np.sqrt((xx - np.float32(cx)) ** 2 + (yy - np.float32(cy)) ** 2)
+        return (amp * np.exp(-((r - r0) ** 2) / (2 * w * w))).astype(np.float32)
+
+    truth = np.zeros((3, ny, nx), dtype=np.float32)
+    truth[0] = depth + ring(6.0, 1.5, 0.03) + ring(0.0, 2.0, -0.01)
+    truth[1] = (0.01 * rng.standard_normal((ny, nx))).astype(np.float32)
+    truth[2] = (0.01 * rng.standard_normal((ny, nx))).astype(np.float32)
+    model_phys = np.zeros_like(truth)
+    model_phys[0] = depth + ring(7.3, 1.8, 0.024) + ring(0.0, 2.2, -0.008) + \
+        (0.001 * rng.standard_normal((ny, nx))).astype(np.float32)
+    model_phys[1] = truth[1] + (0.002 * rng.standard_normal((ny, nx))).astype(np.float32)
+    model_phys[2] = truth[2] + (0.002 * rng.standard_normal((ny, nx))).astype(np.float32)
+
+    def encode(s):  # norm.rs:27-34, f32 element by element
+        out = np.empty_like(s)
+        out[0] = ((s[0] - depth) - mean[0]) / std[0]
+        out[1] = (s[1] - mean[1]) / std[1]
+        out[2] = (s[2] - mean[2]) / std[2]
+        return out
+
+    x = encode(model_phys)
+    target = encode(truth)
+    n = nx * ny
+    sc = M.score(x.ravel(), target.ravel(), float(mean[0]), float(std[0]), nx, ny, cx, cy)
+    ph = M.decode_h(x.ravel(), mean[0], std[0], n)
+    th = M.decode_h(target.ravel(), mean[0], std[0], n)
+    np.savez_compressed(HERE / "metrics.npz", nx=nx, ny=ny, cx=cx, cy=cy, norm_mean=mean, norm_std=std,
+                        norm_depth=depth, truth=truth, x=x, target=target,
+                        prof_model=M.radial_profile(ph, nx, ny, cx, cy), prof_truth=M.radial_profile(th, nx, ny, cx, cy),
+                        row=np.array([sc.corr, sc.corr_h, sc.amplitude_ratio, sc.xcorr_lag, sc.bias], dtype=np.float64))
+    print("wrote metrics.npz", sc)
 
 
 if __name__ == "__main__":

@@ -108,3 +108,51 @@ def test_host_projections_match_the_oracle():
     y = engine.project_energy(x, 0.999 * e0, jcfg, n)
     assert np.array_equal(y, orc.project_energy(x, 0.999 * e0, sum64=True))
     assert engine.energy(y, jcfg, n) <= 0.999 * e0 * (1 + 1e-6)
+
+
+def test_solver_and_scoring_arguments_are_checked_before_device_work():
+    L = engine.load_library()
+    engine._declare_eval(L)
+    s = np.zeros(3 * 16, dtype=np.float32)
+    bad = engine.JcSwParams(0, 16, 1.0, 0.1, 9.81, 1.0, 0.0)
+    assert engine.STATUS[L.jc_sw_run(C.byref(bad), s, 1, 3)] == "BAD_SHAPE"
+    bad = engine.JcSwParams(4, 4, 0.0, 0.1, 9.81, 1.0, 0.0)
+    assert engine.STATUS[L.jc_sw_run(C.byref(bad), s, 1, 3)] == "BAD_ARGUMENT"
+    ok = engine.JcSwParams(4, 4, 1.0, 0.1, 9.81, 1.0, 0.0)
+    assert engine.STATUS[L.jc_sw_run(C.byref(ok), s, 1, -1)] == "BAD_ARGUMENT"
+    assert engine.STATUS[L.jc_sw_run(C.byref(ok), s, 1, 0)] == "OK"  # nothing to do
+    rows = (engine.JcEvalRow * 1)()
+    cfg = engine.JcConfig()
+    cfg.nx, cfg.ny = 4, 4
+    cfg.norm_std[:] = [1.0, 1.0, 1.0]
+    x = np.zeros(48, dtype=np.float32)
+    c = np.array([1e9, 2.0], dtype=np.float32)
+    assert engine.STATUS[L.jc_eval_score(C.byref(cfg), x, x, c, 1, rows)] == "BAD_ARGUMENT"
+    assert engine.STATUS[L.jc_eval_score(C.byref(cfg), x, x, c, 0, rows)] == "OK"
+
+
+def test_host_add_drop_matches_the_oracle():
+    from oracle import oracle as O
+
+    p = engine.JcSwParams(33, 21, 1.0, 0.0903, 9.81, 1.0, 1e-3)
+    a = engine.sw_flat(p)[0]
+    engine.sw_add_drop(p, a[0], 12.7, 9.1, 0.06, 4.2)
+    q = O._SwParams()
+    q.nx, q.ny, q.dx, q.dt, q.g, q.depth, q.nu = 33, 21, 1.0, 0.0903, 9.81, 1.0, 1e-3
+    b = O.sw_flat(q)[0]
+    O.sw_add_drop(q, b[0], 12.7, 9.1, 0.06, 4.2)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_eval_drop_sampler_keeps_waves_off_the_walls():
+    from jacobi2000_gb300.evaluate import cells_per_tick, draw_drops, horizon_ticks
+
+    cfg = engine.JcConfig()
+    cfg.nx, cfg.ny, cfg.dx, cfg.dt, cfg.g, cfg.depth = 128, 96, 1.0, 0.0903, 9.81, 1.0
+    drops, skipped = draw_drops(cfg, 20, 0, 50.0)
+    assert len(drops) == 20 and skipped > 0
+    for cx, cy, amp, sigma in drops:
+        assert 8.0 <= cx < 120.0 and 8.0 <= cy < 88.0 and 0.03 <= amp < 0.07 and 3.0 <= sigma < 5.5
+        assert horizon_ticks(cfg, cx, cy) >= 50.0
+    assert abs(float(cells_per_tick(cfg)) - np.sqrt(9.81) * 0.0903) < 1e-6
+    assert draw_drops(cfg, 20, 0, 50.0) == (drops, skipped)
