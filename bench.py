@@ -64,6 +64,7 @@ def parse_args():
     ap.add_argument("--served-fp32-requests", type=int, default=24)
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-task batch measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 256x256 error report against the f64 oracle")
+    ap.add_argument("--no-eval", action="store_true", help="skip the eval-metrics measurement")
     return ap.parse_args()
 
 
@@ -399,6 +400,82 @@ def accuracy_c3(ticks=(10, 25, 50)):
             "cases": out}
 
 
+def eval_bench(args, steps=3):
+    """The eval-metrics row (crates/engine-cli/src/eval.rs at its defaults:
+    horizons 10/25/50, mass projection): 64 single-drop trajectories drawn as
+    eval.rs draws them on the workload's grid, all in one jc_eval_run (model,
+    solver and scoring in one captured graph), for the BF16 and the FP32
+    model; the solver kernel alone on 256 states of 256x256 (24 compulsory
+    bytes per cell-step, inputs larger than L2); and the oracle's eval loop
+    (f32 forward with the reference's masked scan, C solver, C scores) on one
+    trajectory on the host cores."""
+    import torch
+
+    from jacobi2000_gb300 import engine, evaluate
+    from jacobi2000_gb300.checkpoint import meta_of, parse_config, synthetic_checkpoint, write_safetensors_bytes
+    from oracle import oracle
+
+    horizons, ntraj = [10, 25, 50], 64
+    t, cj = synthetic_checkpoint(args.side, args.dim, args.layers, 0)
+    cfg = parse_config(cj, t)
+    out = {"config": {"grid": f"{args.side}x{args.side}", "model": f"dim {args.dim}, {args.layers} layers",
+                      "trajectories": ntraj, "horizons": horizons, "flags": "mass projection"}}
+    rows32 = None
+    for prec, key in ((engine.BF16, "bf16"), (engine.FP32, "fp32")):
+        m = engine.Model.from_bytes(write_safetensors_bytes(t), cj, prec)
+        drops, skipped = evaluate.draw_drops(m.config, ntraj, 0, 50.0)
+        with engine.Evaluator(m, ntraj) as ev:
+            ev.run(drops, horizons)
+            times = []
+            for _ in range(steps):
+                t0 = time.perf_counter()
+                rows, viol = ev.run(drops, horizons)
+                times.append(time.perf_counter() - t0)
+        sec = statistics.median(times)
+        out[key] = {"s_per_eval": sec, "trajectories_per_s": ntraj / sec,
+                    "model_cell_ticks_per_s": ntraj * cfg.nx * cfg.ny * horizons[-1] / sec,
+                    "mean_corr_at": {str(h): float(rows[i]["corr"].mean()) for i, h in enumerate(horizons)}}
+        if prec == engine.FP32:
+            rows32 = rows
+        m.close()
+    # the solver kernel alone, CUDA events on the launching stream
+    L = engine.load_library()
+    engine._declare_eval(L)
+    count, side, nsteps = 256, 256, 50
+    p = engine.JcSwParams(side, side, 1.0, cfg.dt, cfg.g, cfg.depth, cfg.nu)
+    st = torch.zeros((count, 3, side, side), device="cuda")
+    st[:, 0] = 1.0
+    stream = torch.cuda.current_stream()
+    engine._check(L.jc_sw_run_device(engine.C.byref(p), st.data_ptr(), count, 4, stream.cuda_stream))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    engine._check(L.jc_sw_run_device(engine.C.byref(p), st.data_ptr(), count, nsteps, stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_s = e0.elapsed_time(e1) / nsteps / 1e3
+    cells = count * side * side
+    pk, pk_kind = peaks()
+    gbs = cells * 24 / step_s / 1e9
+    out["sw_step"] = {"workload": f"{count} states of {side}x{side}", "us_per_step": step_s * 1e6,
+                      "cell_steps_per_s": cells / step_s,
+                      "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                   "frac": gbs / pk["hbm_gbs"], "bytes_per_cell_step": 24,
+                                   "peak_kind": f"{pk_kind} copy bandwidth"}}
+    del st
+    # the oracle's eval loop on one trajectory
+    oracle.set_threads(os.cpu_count() or 1)
+    oracle.set_attention_mode("scan")
+    om = oracle.OracleModel(cfg, t)
+    t0 = time.perf_counter()
+    want, _ = oracle.eval_metrics(om, drops[:1], horizons, oracle.MASS | oracle.SUM64, meta_of(cfg))
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"trajectories_per_s": 1.0 / cpu_s, "cores": oracle.get_threads(), "kind": "port",
+                           "sample": f"1 trajectory x {horizons[-1]} ticks, {cpu_s:.1f} s"}
+    out["fp32_vs_oracle_max_abs_corr_diff"] = float(np.abs(rows32[:, 0]["corr"] - want[:, 0, 0]).max())
+    return out
+
+
 def cpu_sample(cfg, t, x0, meta, ticks: int):
     """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
     masked scan) on all host cores, over `ticks` ticks of one instance."""
@@ -561,6 +638,7 @@ def main():
     served = served_bench(args) if rank == 0 else None
     mixed = mixed_batch_bench(args) if rank == 0 and not args.no_mixed else None
     accuracy = accuracy_c3() if rank == 0 and not args.no_accuracy else None
+    evalm = eval_bench(args) if rank == 0 and not args.no_eval else None
 
     cpu = None
     if rank == 0:
@@ -577,7 +655,7 @@ def main():
                 "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
                                "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,
-                "mixed_batch": mixed, "accuracy": accuracy,
+                "mixed_batch": mixed, "accuracy": accuracy, "eval_metrics": evalm,
                 "gpu_launches": launches_per_step * args.steps,
                 "kernels": table, "peaks": pk_kind}
         print(json.dumps(line), flush=True)

@@ -21,9 +21,10 @@ namespace ev {
 
 // ---- solver: shallow_water.rs:149-238 ---------------------------------------
 
-constexpr int kSwTX = 32, kSwTY = 16, kSwThreads = kSwTX * kSwTY;  // output tile, one cell per thread
-constexpr int kSwPX = kSwTX + 4, kSwPY = kSwTY + 4;                // inputs with a 2-cell apron
-constexpr int kSwNX = kSwTX + 2, kSwNY = kSwTY + 2;                // new depth with a 1-cell apron
+constexpr int kSwTX = 64, kSwTY = 32;     // output tile
+constexpr int kSwThreads = 512;           // 4 cells per thread
+constexpr int kSwPX = kSwTX + 4, kSwPY = kSwTY + 4;  // inputs with a 2-cell apron
+constexpr int kSwNX = kSwTX + 2, kSwNY = kSwTY + 2;  // new depth with a 1-cell apron
 
 struct SwDev {
     int nx, ny;
@@ -49,14 +50,20 @@ __device__ __forceinline__ float face_flux(float ha, float hb, float qa, float q
     return __fmul_rn(__fmul_rn(__fmul_rn(0.5f, __fadd_rn(ha, hb)), 0.5f), __fadd_rn(qa, qb));
 }
 
+struct SwSmem {
+    float h[kSwPY][kSwPX + 1], u[kSwPY][kSwPX + 1], v[kSwPY][kSwPX + 1];
+    float hn[kSwNY][kSwNX + 1];
+};
+
 // One forward-backward step of every state: continuity in flux form (zero
 // flux through the walls), then momentum on the new surface with mirrored
 // ghost cells (h even, normal velocity odd, tangential velocity even).
-// grid (x tiles, y tiles, states); src and dst are [states][3][ny][nx].
+// grid (x tiles, y tiles, states); src and dst are [states][3][ny][nx]. A
+// 64x32 tile per CTA keeps enough loads in flight per SM to cover the DRAM
+// latency (the step is a pure stream: 12 bytes read and 12 written per cell).
 __global__ void __launch_bounds__(kSwThreads)
 sw_step_kernel(SwDev p, const float* __restrict__ src, float* __restrict__ dst) {
-    __shared__ float sh[kSwPY][kSwPX + 1], su[kSwPY][kSwPX + 1], sv[kSwPY][kSwPX + 1];
-    __shared__ float shn[kSwNY][kSwNX + 1];
+    __shared__ SwSmem sm;
     const int nx = p.nx, ny = p.ny;
     const long long n = (long long)nx * ny;
     const float* H = src + (long long)blockIdx.z * 3 * n;
@@ -66,62 +73,70 @@ sw_step_kernel(SwDev p, const float* __restrict__ src, float* __restrict__ dst) 
     const int tid = threadIdx.x;
     // inputs on [y0-2, y0+TY+2) x [x0-2, x0+TX+2); apron positions outside
     // the grid hold a clamped neighbour and are never read below
+#pragma unroll
     for (int i = tid; i < kSwPY * kSwPX; i += kSwThreads) {
         const int ly = i / kSwPX, lx = i - ly * kSwPX;
         const int gx = min(max(x0 - 2 + lx, 0), nx - 1), gy = min(max(y0 - 2 + ly, 0), ny - 1);
         const long long o = (long long)gy * nx + gx;
-        sh[ly][lx] = H[o];
-        su[ly][lx] = U[o];
-        sv[ly][lx] = V[o];
+        sm.h[ly][lx] = __ldg(H + o);
+        sm.u[ly][lx] = __ldg(U + o);
+        sm.v[ly][lx] = __ldg(V + o);
     }
     __syncthreads();
     // continuity on the tile and its 1-cell apron (cells inside the grid)
+#pragma unroll
     for (int i = tid; i < kSwNY * kSwNX; i += kSwThreads) {
         const int ly = i / kSwNX, lx = i - ly * kSwNX;
         const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
         if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
         const int sx = lx + 1, sy = ly + 1;
-        const float h = sh[sy][sx];
-        const float fxl = gx == 0 ? 0.f : face_flux(sh[sy][sx - 1], h, su[sy][sx - 1], su[sy][sx]);
-        const float fxr = gx == nx - 1 ? 0.f : face_flux(h, sh[sy][sx + 1], su[sy][sx], su[sy][sx + 1]);
-        const float fyl = gy == 0 ? 0.f : face_flux(sh[sy - 1][sx], h, sv[sy - 1][sx], sv[sy][sx]);
-        const float fyr = gy == ny - 1 ? 0.f : face_flux(h, sh[sy + 1][sx], sv[sy][sx], sv[sy + 1][sx]);
-        shn[ly][lx] = __fsub_rn(h, __fmul_rn(p.r, __fadd_rn(__fsub_rn(fxr, fxl), __fsub_rn(fyr, fyl))));
+        const float h = sm.h[sy][sx];
+        const float fxl = gx == 0 ? 0.f : face_flux(sm.h[sy][sx - 1], h, sm.u[sy][sx - 1], sm.u[sy][sx]);
+        const float fxr = gx == nx - 1 ? 0.f : face_flux(h, sm.h[sy][sx + 1], sm.u[sy][sx], sm.u[sy][sx + 1]);
+        const float fyl = gy == 0 ? 0.f : face_flux(sm.h[sy - 1][sx], h, sm.v[sy - 1][sx], sm.v[sy][sx]);
+        const float fyr = gy == ny - 1 ? 0.f : face_flux(h, sm.h[sy + 1][sx], sm.v[sy][sx], sm.v[sy + 1][sx]);
+        sm.hn[ly][lx] = __fsub_rn(h, __fmul_rn(p.r, __fadd_rn(__fsub_rn(fxr, fxl), __fsub_rn(fyr, fyl))));
     }
     __syncthreads();
-    const int tx = tid % kSwTX, ty = tid / kSwTX;
-    const int gx = x0 + tx, gy = y0 + ty;
-    if (gx >= nx || gy >= ny) return;
-    // momentum, centred differences on the new surface (:188-232)
-    const int sx = tx + 2, sy = ty + 2;  // in sh, su, sv
-    const int qx = tx + 1, qy = ty + 1;  // in shn
-    const int dxm = gx == 0 ? 0 : -1, dxp = gx == nx - 1 ? 0 : 1;
-    const int dym = gy == 0 ? 0 : -1, dyp = gy == ny - 1 ? 0 : 1;
-    const float sxm = gx == 0 ? -1.f : 1.f, sxp = gx == nx - 1 ? -1.f : 1.f;
-    const float sym = gy == 0 ? -1.f : 1.f, syp = gy == ny - 1 ? -1.f : 1.f;
-    const float hl = shn[qy][qx + dxm], hr = shn[qy][qx + dxp];
-    const float hd = shn[qy + dym][qx], hu = shn[qy + dyp][qx];
-    const float ul = __fmul_rn(sxm, su[sy][sx + dxm]), ur = __fmul_rn(sxp, su[sy][sx + dxp]);
-    const float ud = su[sy + dym][sx], uu = su[sy + dyp][sx];
-    const float vl = sv[sy][sx + dxm], vr = sv[sy][sx + dxp];
-    const float vd = __fmul_rn(sym, sv[sy + dym][sx]), vu = __fmul_rn(syp, sv[sy + dyp][sx]);
-    const float u0 = su[sy][sx], v0 = sv[sy][sx];
-    const float dudx = __fmul_rn(__fsub_rn(ur, ul), p.inv2dx), dudy = __fmul_rn(__fsub_rn(uu, ud), p.inv2dx);
-    const float dvdx = __fmul_rn(__fsub_rn(vr, vl), p.inv2dx), dvdy = __fmul_rn(__fsub_rn(vu, vd), p.inv2dx);
-    const float dhdx = __fmul_rn(__fsub_rn(hr, hl), p.inv2dx), dhdy = __fmul_rn(__fsub_rn(hu, hd), p.inv2dx);
-    const float lap_u =
-        __fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ul, ur), ud), uu), __fmul_rn(4.0f, u0)), p.invdx2);
-    const float lap_v =
-        __fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(vl, vr), vd), vu), __fmul_rn(4.0f, v0)), p.invdx2);
-    const float tu = __fadd_rn(__fsub_rn(__fsub_rn(__fmul_rn(-u0, dudx), __fmul_rn(v0, dudy)), __fmul_rn(p.g, dhdx)),
-                               __fmul_rn(p.nu, lap_u));
-    const float tv = __fadd_rn(__fsub_rn(__fsub_rn(__fmul_rn(-u0, dvdx), __fmul_rn(v0, dvdy)), __fmul_rn(p.g, dhdy)),
-                               __fmul_rn(p.nu, lap_v));
-    const long long o = (long long)gy * nx + gx;
     float* D = dst + (long long)blockIdx.z * 3 * n;
-    D[o] = shn[qy][qx];
-    D[n + o] = __fadd_rn(u0, __fmul_rn(p.dt, tu));
-    D[2 * n + o] = __fadd_rn(v0, __fmul_rn(p.dt, tv));
+    // momentum, centred differences on the new surface (:188-232)
+#pragma unroll
+    for (int c = 0; c < (kSwTX * kSwTY) / kSwThreads; c++) {
+        const int j = tid + c * kSwThreads;
+        const int tx = j % kSwTX, ty = j / kSwTX;
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= nx || gy >= ny) continue;
+        const int sx = tx + 2, sy = ty + 2;  // in h, u, v
+        const int qx = tx + 1, qy = ty + 1;  // in hn
+        const int dxm = gx == 0 ? 0 : -1, dxp = gx == nx - 1 ? 0 : 1;
+        const int dym = gy == 0 ? 0 : -1, dyp = gy == ny - 1 ? 0 : 1;
+        const float sxm = gx == 0 ? -1.f : 1.f, sxp = gx == nx - 1 ? -1.f : 1.f;
+        const float sym = gy == 0 ? -1.f : 1.f, syp = gy == ny - 1 ? -1.f : 1.f;
+        const float hl = sm.hn[qy][qx + dxm], hr = sm.hn[qy][qx + dxp];
+        const float hd = sm.hn[qy + dym][qx], hu = sm.hn[qy + dyp][qx];
+        const float ul = __fmul_rn(sxm, sm.u[sy][sx + dxm]), ur = __fmul_rn(sxp, sm.u[sy][sx + dxp]);
+        const float ud = sm.u[sy + dym][sx], uu = sm.u[sy + dyp][sx];
+        const float vl = sm.v[sy][sx + dxm], vr = sm.v[sy][sx + dxp];
+        const float vd = __fmul_rn(sym, sm.v[sy + dym][sx]), vu = __fmul_rn(syp, sm.v[sy + dyp][sx]);
+        const float u0 = sm.u[sy][sx], v0 = sm.v[sy][sx];
+        const float dudx = __fmul_rn(__fsub_rn(ur, ul), p.inv2dx), dudy = __fmul_rn(__fsub_rn(uu, ud), p.inv2dx);
+        const float dvdx = __fmul_rn(__fsub_rn(vr, vl), p.inv2dx), dvdy = __fmul_rn(__fsub_rn(vu, vd), p.inv2dx);
+        const float dhdx = __fmul_rn(__fsub_rn(hr, hl), p.inv2dx), dhdy = __fmul_rn(__fsub_rn(hu, hd), p.inv2dx);
+        const float lap_u =
+            __fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ul, ur), ud), uu), __fmul_rn(4.0f, u0)), p.invdx2);
+        const float lap_v =
+            __fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(vl, vr), vd), vu), __fmul_rn(4.0f, v0)), p.invdx2);
+        const float tu = __fadd_rn(
+            __fsub_rn(__fsub_rn(__fmul_rn(-u0, dudx), __fmul_rn(v0, dudy)), __fmul_rn(p.g, dhdx)),
+            __fmul_rn(p.nu, lap_u));
+        const float tv = __fadd_rn(
+            __fsub_rn(__fsub_rn(__fmul_rn(-u0, dvdx), __fmul_rn(v0, dvdy)), __fmul_rn(p.g, dhdy)),
+            __fmul_rn(p.nu, lap_v));
+        const long long o = (long long)gy * nx + gx;
+        D[o] = sm.hn[qy][qx];
+        D[n + o] = __fadd_rn(u0, __fmul_rn(p.dt, tu));
+        D[2 * n + o] = __fadd_rn(v0, __fmul_rn(p.dt, tv));
+    }
 }
 
 void sw_step(const SwDev& p, const float* src, float* dst, int count, cudaStream_t s) {
