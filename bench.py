@@ -473,6 +473,33 @@ def eval_bench(args, steps=3):
     out["cpu_baseline"] = {"trajectories_per_s": 1.0 / cpu_s, "cores": oracle.get_threads(), "kind": "port",
                            "sample": f"1 trajectory x {horizons[-1]} ticks, {cpu_s:.1f} s"}
     out["fp32_vs_oracle_max_abs_corr_diff"] = float(np.abs(rows32[:, 0]["corr"] - want[:, 0, 0]).max())
+
+    # rewind round trip: forward N then back N with the reverse checkpoint
+    # (a second seeded family), all trajectories and horizons batched
+    tr, cjr = synthetic_checkpoint(args.side, args.dim, args.layers, 1)
+    fm = engine.Model.from_bytes(write_safetensors_bytes(t), cj, engine.BF16)
+    rm = engine.Model.from_bytes(write_safetensors_bytes(tr), cjr, engine.BF16)
+    with engine.RoundTrip(fm, rm, ntraj, len(horizons)) as rt:
+        rt.run(drops, horizons)
+        times = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            rrows = rt.run(drops, horizons)
+            times.append(time.perf_counter() - t0)
+    fm.close()
+    rm.close()
+    sec = statistics.median(times)
+    traj_ticks = ntraj * (horizons[-1] + sum(horizons))
+    omr = oracle.OracleModel(parse_config(cjr, tr), tr)
+    t0 = time.perf_counter()
+    oracle.roundtrip(om, omr, drops[:1], horizons, oracle.MASS | oracle.SUM64, meta_of(cfg))
+    cpu_rt = time.perf_counter() - t0
+    out["roundtrip"] = {"config": f"{ntraj} trajectories, horizons {horizons}, bf16 forward and reverse models",
+                        "s_per_run": sec, "trajectories_per_s": ntraj / sec,
+                        "model_cell_ticks_per_s": traj_ticks * cfg.nx * cfg.ny / sec,
+                        "mean_corr_at": {str(h): float(rrows[i]["corr"].mean()) for i, h in enumerate(horizons)},
+                        "cpu_baseline": {"trajectories_per_s": 1.0 / cpu_rt, "cores": oracle.get_threads(),
+                                         "kind": "port", "sample": f"1 trajectory, {cpu_rt:.1f} s"}}
     return out
 
 

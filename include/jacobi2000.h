@@ -346,6 +346,37 @@ void jc_eval_destroy(jc_eval* e);
 jc_status jc_eval_run(jc_eval* e, const jc_drop* drops, int32_t n, const int32_t* horizons,
                       int32_t n_horizons, uint32_t flags, jc_eval_row* rows, double* max_violation);
 
+/* ---- Rewind round trip ------------------------------------------------------
+ * Forward N ticks with a forward checkpoint, then N ticks with its reverse
+ * checkpoint (same grid and hyper-parameters), scored against the start
+ * state: the round-trip runs of the reference
+ * (docs/runs/2026-09-20-rewind-round-trip.md:17-32), which drive
+ * engine::Model::step with both checkpoints (crates/web/src/lib.rs:383-409 is
+ * the interactive rewind). All trajectories and horizons run as batches on
+ * the device. */
+typedef struct jc_roundtrip jc_roundtrip;
+
+/* One round-trip row: Pearson correlation over (h, u, v) of the rewound and
+ * the start state (metrics.rs:9-23), amplitude ratio (peak |h| of the rewound
+ * over the start state, decoded as metrics.rs:105-107), RMSE of the rewound
+ * against the start state and RMSE of the N-tick state against the start
+ * state (metrics.rs:109-112, normalized units; the latter is what a rewind
+ * that changes nothing would score). */
+typedef struct {
+    float corr, amplitude_ratio, rmse, change_rmse;
+} jc_roundtrip_row;
+
+jc_status jc_roundtrip_create(jc_model* forward, jc_model* reverse, int32_t max_trajectories,
+                              int32_t max_horizons, jc_roundtrip** out);
+void jc_roundtrip_destroy(jc_roundtrip* r);
+
+/* Trajectory k starts from State::flat plus drops[k] (encoded); horizons are
+ * strictly ascending and >= 1; `flags` (JC_PROJECT_*) apply to both
+ * directions, the projections' references taken at the start of each
+ * direction. rows: [n_horizons][n]. */
+jc_status jc_roundtrip_run(jc_roundtrip* r, const jc_drop* drops, int32_t n, const int32_t* horizons,
+                           int32_t n_horizons, uint32_t flags, jc_roundtrip_row* rows);
+
 /* Thread-local description of the last failure on this thread ("" if none). */
 const char* jc_last_error(void);
 

@@ -275,6 +275,27 @@ jc_status jc_eval_run(jc_eval* e, const jc_drop* drops, int32_t n, const int32_t
     return guard([&] { jc::eval_run(e, drops, n, horizons, n_horizons, flags, rows, max_violation); });
 }
 
+jc_status jc_roundtrip_create(jc_model* forward, jc_model* reverse, int32_t max_trajectories, int32_t max_horizons,
+                              jc_roundtrip** out) {
+    if (!forward || !reverse || !out) return fail(JC_BAD_ARGUMENT, "null argument");
+    *out = nullptr;
+    return guard([&] { *out = jc::roundtrip_create(forward, reverse, max_trajectories, max_horizons); });
+}
+
+void jc_roundtrip_destroy(jc_roundtrip* r) {
+    if (!r) return;
+    try {
+        jc::roundtrip_destroy(r);
+    } catch (...) {
+    }
+}
+
+jc_status jc_roundtrip_run(jc_roundtrip* r, const jc_drop* drops, int32_t n, const int32_t* horizons,
+                           int32_t n_horizons, uint32_t flags, jc_roundtrip_row* rows) {
+    if (!r) return fail(JC_BAD_ARGUMENT, "round trip is null");
+    return guard([&] { jc::roundtrip_run(r, drops, n, horizons, n_horizons, flags, rows); });
+}
+
 const char* jc_last_error(void) { return g_last_error.c_str(); }
 
 int32_t jc_autotune(int32_t enable) {

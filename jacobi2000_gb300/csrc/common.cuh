@@ -99,6 +99,13 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid
 // Waits for every copy this thread issued (a __syncthreads() must follow
 // before other threads read the data).
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Closes this thread's group of copies issued since the last commit.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of this thread's committed groups are in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 // Neumaier compensated accumulator in f64.
 struct Neu {

@@ -23,6 +23,13 @@ struct Dims {
     float norm_mean[3], norm_std[3], norm_depth, g, energy_r_max;
 };
 
+// head.conv2 weights as the conv2 kernel takes them by value (in its
+// parameter space): w[(ci * 9 + tap) * 3 + co], bias b[co]; C = 3, HD = 32.
+struct Conv2Params {
+    float w[32 * 9 * 3];
+    float b[3];
+};
+
 // FP32 device weights, in the layouts the FP32 kernels read.
 struct WeightsF32 {
     const float *embed_w, *embed_b;   // [C*P*P, D], [D]
@@ -40,6 +47,7 @@ struct WeightsF32 {
     const float *tc_w, *tc_b;         // [D, HD]
     const float *c1_w, *c1_b;         // [9*kZcStride, HD]
     const float *c2_w, *c2_b;         // [C, HD, 3, 3] as stored, [C]
+    const Conv2Params* c2p;           // host copy of c2_w / c2_b in the conv2 kernel's order
 };
 
 // A packed launch over the first n_inst instances of `inst`, with the

@@ -14,7 +14,7 @@
 #include <memory>
 #include <vector>
 
-#include "runtime.hpp"
+#include "evaluate.hpp"
 
 namespace jc {
 namespace ev {
@@ -527,6 +527,15 @@ void check_centre(float cx, float cy) {
         throw Error(JC_BAD_ARGUMENT, "drop centres must be finite and within 1e6 cells");
 }
 
+void initial_state(const jc_config& c, const jc_drop& d, float* phys, float* x) {
+    check_centre(d.cx, d.cy);
+    const long long cells = (long long)c.nx * c.ny;
+    std::fill(phys, phys + cells, c.depth);
+    std::fill(phys + cells, phys + 3 * cells, 0.0f);
+    add_drop(c.nx, c.ny, phys, d.cx, d.cy, d.amp, d.sigma);
+    encode(c, phys, phys + cells, phys + 2 * cells, cells, x);
+}
+
 // ---- the evaluator ------------------------------------------------------------
 
 class Evaluator : public TickHook {
@@ -576,12 +585,7 @@ class Evaluator : public TickHook {
         float* X = h_states_ + max_ * len_;
         std::vector<float> cen(2 * n);
         for (int k = 0; k < n; k++) {
-            check_centre(drops[k].cx, drops[k].cy);
-            float* s = H + k * len_;
-            std::fill(s, s + cells_, c.depth);
-            std::fill(s + cells_, s + len_, 0.0f);
-            add_drop(c.nx, c.ny, s, drops[k].cx, drops[k].cy, drops[k].amp, drops[k].sigma);
-            encode(c, s, s + cells_, s + 2 * cells_, cells_, X + k * len_);
+            initial_state(c, drops[k], H + k * len_, X + k * len_);
             cen[2 * k] = drops[k].cx;
             cen[2 * k + 1] = drops[k].cy;
         }

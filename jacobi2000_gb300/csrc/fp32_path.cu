@@ -242,109 +242,101 @@ __global__ void upsample_concat_kernel(Dims d, const float* __restrict__ z0, con
     o[d.HD / 4] = make_float4(tail[0], tail[1], tail[2], tail[3]);
 }
 
-// head.conv2 (3x3, HD -> C, cpu.rs:348-349) then the step's residual
-// (cpu.rs:84-88), for C = 3 and HD = 32. One CTA per 16x16 cell tile: the
-// tile's c1 values plus a one-cell halo are staged channel-major in shared
-// memory (consecutive threads read consecutive cells: no bank conflicts), the
-// weights as [ci][tap] float4 (3 outputs + 0). One thread per cell.
 // head.conv2 (3x3, HD -> C, zero padding; cpu.rs:171-205, 347-348) and the
-// step's residual (cpu.rs:84-88) over one 16 x 16 cell tile per CTA. The
-// halo tile of c1 is staged channel-last in shared memory, half of the
-// channels at a time, by asynchronous copies (all in flight at once), with a
-// position pitch of HD/2 + 4 floats so the 16-byte reads of eight
-// neighbouring positions fall in distinct banks; the small footprint keeps
-// seven CTAs per SM, whose loads and arithmetic overlap. Each of the 64
-// threads owns a vertical strip of 4 cells: per group of 4 input channels it
-// reads the 6 x 3 halo values once and the channels' 9 taps x C weights once,
-// and reuses both across the strip (432 FMAs per 54 shared-memory reads).
-// Per cell, the sum runs in the reference's order: bias, then channel, ky, kx.
-constexpr int kConv2Threads = 64;
-constexpr int kConv2Pitch = 20;  // floats per halo position (HD / 2 = 16 + 4 pad)
-constexpr int kConv2Smem = ((kCellTile + 2) * (kCellTile + 2) * kConv2Pitch + 32 * 9 * 4) * 4;
+// step's residual (cpu.rs:84-88) over one 16 x 16 cell tile per CTA, for
+// C = 3 and HD = 32. The tile's c1 values plus a one-cell halo arrive in four
+// stages of 8 channels (32 bytes per position, whole DRAM sectors) by
+// asynchronous copies, double-buffered so the next stage is in flight while
+// the current one is summed; a stage holds two planes of 4 channels, one
+// 16-byte chunk per position, so the halo reads of a thread are fixed offsets
+// from one base address. The weights come by value in the kernel's parameter
+// space and enter the FMAs as constant operands (no loads). Each of the 128
+// threads owns a vertical pair of cells and reuses each halo value across the
+// pair. Per cell, the sum runs in the reference's order: bias, then channel,
+// ky, kx.
+constexpr int kConv2Threads = 128;
+constexpr int kConv2S = kCellTile + 2;                // halo tile side
+constexpr int kConv2Plane = kConv2S * kConv2S * 4;    // floats per 4-channel plane
+constexpr int kConv2Smem = 2 * 2 * kConv2Plane * 4;   // two stages of two planes
 
 template <int C, int HD>
-__global__ void __launch_bounds__(kConv2Threads) conv2_step_kernel(const float* __restrict__ c1,
-                                                                   const float* __restrict__ w2,
-                                                                   const float* __restrict__ b2, const InstDev* inst,
-                                                                   int n_inst, int mode) {
+__global__ void __launch_bounds__(kConv2Threads, 8) conv2_step_kernel(const float* __restrict__ c1,
+                                                                      const __grid_constant__ Conv2Params cw,
+                                                                      const InstDev* inst, int n_inst, int mode) {
     static_assert(C == 3 && HD == 32, "conv2 is built for 3 channels and a cell-head width of 32");
-    constexpr int S = kCellTile + 2, QH = HD / 8, P = kConv2Pitch;  // QH float4 groups per channel half
+    constexpr int S = kConv2S, NG = HD / 8;
     extern __shared__ __align__(16) float c2smem[];
-    float* tile = c2smem;                                        // [S*S][P], one channel half
-    float4* ws = reinterpret_cast<float4*>(c2smem + S * S * P);  // [HD][9] (C outputs + pad)
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (inst[mid].tile0 <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
     }
-    const InstDev& I = inst[lo];
+    const InstDev I = inst[lo];
     const int tiles_x = (I.nx + kCellTile - 1) / kCellTile;
     const int tl = blockIdx.x - I.tile0;
     const int y0 = (tl / tiles_x) * kCellTile, x0 = (tl % tiles_x) * kCellTile;
-    auto load_half = [&](int h) {
-        for (int e = threadIdx.x; e < S * S * QH; e += blockDim.x) {
-            const int q = e % QH, p = e / QH, sy = p / S, sx = p % S;
+    auto load_stage = [&](int g) {
+        float* dst = c2smem + (g & 1) * 2 * kConv2Plane;
+        for (int e = threadIdx.x; e < S * S * 2; e += kConv2Threads) {
+            const int j = e & 1, p = e >> 1, sy = p / S, sx = p - sy * S;
             const int y = y0 + sy - 1, x = x0 + sx - 1;
             const bool in = y >= 0 && x >= 0 && y < I.ny && x < I.nx;
-            const float* src = in ? c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 4 * (QH * h + q) : c1;
-            cp_async16(tile + p * P + 4 * q, src, in);  // zero outside the grid
+            const float* src = in ? c1 + ((size_t)I.cell0 + (size_t)y * I.nx + x) * HD + 8 * g + 4 * j : c1;
+            cp_async16(dst + j * kConv2Plane + 4 * p, src, in);  // zero outside the grid
         }
+        cp_async_commit();
     };
-    load_half(0);
-    for (int i = threadIdx.x; i < HD * 9; i += blockDim.x) {
-        const int ci = i / 9, tap = i % 9;
-        float w[4] = {0.f, 0.f, 0.f, 0.f};
+    load_stage(0);
+    const int tx = threadIdx.x % kCellTile, sy = (threadIdx.x / kCellTile) * 2;  // cells (tx, sy), (tx, sy + 1)
+    float acc[2][C];
 #pragma unroll
-        for (int co = 0; co < C; co++) w[co] = w2[(co * HD + ci) * 9 + tap];
-        ws[i] = make_float4(w[0], w[1], w[2], w[3]);
-    }
-    const int tx = threadIdx.x % kCellTile, sy = (threadIdx.x / kCellTile) * 4;  // cells (tx, sy..sy+3)
-    float acc[4][C];
+    for (int i = 0; i < 2; i++)
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+        for (int co = 0; co < C; co++) acc[i][co] = cw.b[co];
 #pragma unroll
-        for (int co = 0; co < C; co++) acc[i][co] = b2[co];
-#pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-        if (h == 1) {
-            __syncthreads();  // every thread is done with the first half
-            load_half(1);
+    for (int g = 0; g < NG; g++) {
+        if (g + 1 < NG) {
+            load_stage(g + 1);
+            cp_async_wait_group<1>();
+        } else {
+            cp_async_wait_group<0>();
         }
-        cp_async_wait_all();
         __syncthreads();
-#pragma unroll 1
-        for (int q = 0; q < QH; q++) {
-            float4 a[6][3];  // halo rows sy..sy+5, columns tx..tx+2, channels 4 (QH h + q) ..
 #pragma unroll
-            for (int r = 0; r < 6; r++)
+        for (int j = 0; j < 2; j++) {
+            const float4* pl =
+                reinterpret_cast<const float4*>(c2smem + (g & 1) * 2 * kConv2Plane + j * kConv2Plane) + sy * S + tx;
+            float4 a[4][3];  // halo rows sy..sy+3, columns tx..tx+2, channels 8 g + 4 j ..
 #pragma unroll
-                for (int kx = 0; kx < 3; kx++)
-                    a[r][kx] = reinterpret_cast<const float4*>(tile + ((sy + r) * S + tx + kx) * P)[q];
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) a[r][kx] = pl[r * S + kx];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
-                const int ci = 4 * (QH * h + q) + c;
+                const int ci = 8 * g + 4 * j + c;
 #pragma unroll
                 for (int ky = 0; ky < 3; ky++)
 #pragma unroll
                     for (int kx = 0; kx < 3; kx++) {
-                        const float4 w = ws[ci * 9 + ky * 3 + kx];
+                        const float* w = cw.w + (ci * 9 + ky * 3 + kx) * 3;
 #pragma unroll
-                        for (int i = 0; i < 4; i++) {
+                        for (int i = 0; i < 2; i++) {
                             const float4 av = a[i + ky][kx];
                             const float v = c == 0 ? av.x : c == 1 ? av.y : c == 2 ? av.z : av.w;
-                            acc[i][0] = fmaf(v, w.x, acc[i][0]);
-                            acc[i][1] = fmaf(v, w.y, acc[i][1]);
-                            acc[i][2] = fmaf(v, w.z, acc[i][2]);
+                            acc[i][0] = fmaf(v, w[0], acc[i][0]);
+                            acc[i][1] = fmaf(v, w[1], acc[i][1]);
+                            acc[i][2] = fmaf(v, w[2], acc[i][2]);
                         }
                     }
             }
         }
+        __syncthreads();  // every thread is done with this buffer before it is refilled
     }
     const size_t plane = (size_t)I.nx * I.ny;
     const int x = x0 + tx;
     if (x >= I.nx) return;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < 2; i++) {
         const int y = y0 + sy + i;
         if (y >= I.ny) break;
         const size_t cl = (size_t)y * I.nx + x;
@@ -667,7 +659,8 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, f32k::kConv2Smem));
         attr = true;
     }
-    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, f32k::kConv2Threads, f32k::kConv2Smem, s>>>(c1, w.c2_w, w.c2_b, p.inst,
+    if (!w.c2p) throw std::runtime_error("conv2 weights missing");
+    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, f32k::kConv2Threads, f32k::kConv2Smem, s>>>(c1, *w.c2p, p.inst,
                                                                                           p.n_inst, mode);
     check_launch(name);
 }

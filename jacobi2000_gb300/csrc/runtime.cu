@@ -414,6 +414,16 @@ static void upload_weights(const TensorMap& t, const Dims& dims, DeviceArena& ar
     }
     f.c2_w = up("head.conv2.weight");
     f.c2_b = up("head.conv2.bias");
+    if (C == 3 && HD == 32) {
+        const auto &src = get(t, "head.conv2.weight").data, &bias = get(t, "head.conv2.bias").data;
+        w.conv2.reset(new Conv2Params());
+        for (int co = 0; co < C; co++) {
+            w.conv2->b[co] = bias[co];
+            for (int ci = 0; ci < HD; ci++)
+                for (int k = 0; k < 9; k++) w.conv2->w[(ci * 9 + k) * 3 + co] = src[((size_t)co * HD + ci) * 9 + k];
+        }
+        f.c2p = w.conv2.get();
+    }
     uint64_t h = 1469598103934665603ull;
     for (auto& kv : t) {
         if (kv.first == "pos") continue;

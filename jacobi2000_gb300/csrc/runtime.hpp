@@ -77,6 +77,7 @@ struct DeviceWeights {
     WeightsF32 f32{};
     const float* pos = nullptr;  // [T, D]
     std::unique_ptr<BF16Path> bf16;
+    std::unique_ptr<Conv2Params> conv2;  // host copy behind f32.c2p
     uint64_t shared_hash = 0;    // hash of every tensor but `pos`
 };
 
@@ -231,6 +232,12 @@ jc_eval* eval_create(jc_model* m, int max_traj);
 void eval_destroy(jc_eval* e);
 void eval_run(jc_eval* e, const jc_drop* drops, int n, const int32_t* horizons, int nh, uint32_t flags,
               jc_eval_row* rows, double* max_violation);
+
+// Rewind round trip (roundtrip.cu), behind jc_roundtrip_*.
+jc_roundtrip* roundtrip_create(jc_model* fwd, jc_model* rev, int max_traj, int max_h);
+void roundtrip_destroy(jc_roundtrip* r);
+void roundtrip_run(jc_roundtrip* r, const jc_drop* drops, int n, const int32_t* horizons, int nh, uint32_t flags,
+                   jc_roundtrip_row* rows);
 
 // The FP32 forward of m's own grid with every buffer in the library's fixed
 // no-alloc scratch array (noalloc.cu); allocates nothing.

@@ -570,3 +570,73 @@ class Evaluator:
         viol = C.c_double(0.0)
         _check(self._L.jc_eval_run(self._h, d, n, hz, nh, int(flags), rows, C.byref(viol)))
         return _rows_array(rows, n * nh).reshape(nh, n), float(viol.value)
+
+
+# ---- rewind round trip (jc_roundtrip_*) --------------------------------------------
+
+class JcRoundTripRow(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("corr", "amplitude_ratio", "rmse", "change_rmse")]
+
+
+ROUNDTRIP_FIELDS = [f for f, _ in JcRoundTripRow._fields_]
+EXPORTED += ["jc_roundtrip_create", "jc_roundtrip_destroy", "jc_roundtrip_run"]
+
+
+def _declare_roundtrip(L):
+    if getattr(L, "_rt_declared", False):
+        return
+    _declare_eval(L)
+    vp = C.c_void_p
+    L.jc_roundtrip_create.argtypes = [vp, vp, C.c_int32, C.c_int32, C.POINTER(vp)]
+    L.jc_roundtrip_create.restype = C.c_int
+    L.jc_roundtrip_destroy.argtypes = [vp]
+    L.jc_roundtrip_destroy.restype = None
+    L.jc_roundtrip_run.argtypes = [vp, C.POINTER(JcDrop), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint32,
+                                   C.POINTER(JcRoundTripRow)]
+    L.jc_roundtrip_run.restype = C.c_int
+    L._rt_declared = True
+
+
+class RoundTrip:
+    """Forward N ticks with `forward`, back N ticks with `reverse`, scored
+    against the start (jc_roundtrip_*)."""
+
+    def __init__(self, forward: Model, reverse: Model, max_trajectories: int, max_horizons: int = 4):
+        L = load_library()
+        _declare_roundtrip(L)
+        self._L = L
+        self.forward, self.reverse = forward, reverse
+        h = C.c_void_p()
+        _check(L.jc_roundtrip_create(forward._h, reverse._h, int(max_trajectories), int(max_horizons), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.jc_roundtrip_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, drops, horizons, flags: int = PROJECT_MASS) -> np.ndarray:
+        """drops: [(cx, cy, amp, sigma)]; returns rows [len(horizons),
+        len(drops)] structured by ROUNDTRIP_FIELDS."""
+        n, nh = len(drops), len(horizons)
+        d = (JcDrop * max(n, 1))(*[JcDrop(*map(float, dr)) for dr in drops])
+        hz = (C.c_int32 * max(nh, 1))(*[int(h) for h in horizons])
+        rows = (JcRoundTripRow * max(n * nh, 1))()
+        _check(self._L.jc_roundtrip_run(self._h, d, n, hz, nh, int(flags), rows))
+        out = np.zeros(n * nh, dtype=[(f, np.float32) for f in ROUNDTRIP_FIELDS])
+        for k in range(n * nh):
+            for f in ROUNDTRIP_FIELDS:
+                out[f][k] = getattr(rows[k], f)
+        return out.reshape(nh, n)

@@ -122,6 +122,7 @@ float orc_std_dev(const float* f, int n);
 float orc_bias(const float* model, const float* solver, int n);
 int   orc_radial_profile(const float* f, int nx, int ny, float cx, float cy, double* out, int cap);
 float orc_xcorr_lag(const double* model, const double* solver, int n, int max_lag);
+float orc_rmse(const float* a, const float* b, int n);
 void  orc_encode(const float norm_mean[3], const float norm_std[3], float norm_depth, const float* h,
                  const float* u, const float* v, int n, float* out);
 /* One eval-metrics row: corr (h,u,v), corr (h), amplitude ratio, wavefront

@@ -233,6 +233,8 @@ def _bind_eval(L):
         getattr(L, fn).restype = C.c_float
     L.orc_radial_profile.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, f64p, C.c_int]
     L.orc_radial_profile.restype = C.c_int
+    L.orc_rmse.argtypes = [f32p, f32p, C.c_int]
+    L.orc_rmse.restype = C.c_float
     L.orc_xcorr_lag.argtypes = [f64p, f64p, C.c_int, C.c_int]
     L.orc_xcorr_lag.restype = C.c_float
     fa3 = C.c_float * 3
@@ -370,6 +372,41 @@ def eval_metrics(model: "OracleModel", drops, horizons, flags: int, meta):
             t_done = hz
             rows[i, j] = eval_score(cfg, traj[hz], truth, cx, cy)
     return rows, worst
+
+
+def rmse(a, b) -> float:
+    a, b = _f32(a).ravel(), _f32(b).ravel()
+    return _elib().orc_rmse(a, b, a.size)
+
+
+def initial_state(cfg, drop) -> np.ndarray:
+    """State::flat plus one drop, encoded: the start of an eval or round-trip
+    trajectory (eval.rs:135-139)."""
+    p = sw_params(cfg)
+    truth = sw_flat(p)[0]
+    sw_add_drop(p, truth[0], *drop)
+    return encode(cfg, truth)
+
+
+def roundtrip(forward: "OracleModel", reverse: "OracleModel", drops, horizons, flags: int, meta):
+    """Forward N ticks, reverse N ticks, scored against the start: rows
+    [len(horizons), len(drops), 4] of (corr, amplitude ratio, round-trip RMSE,
+    N-tick change RMSE), with metrics.rs's correlation, peak, decode_h and
+    rmse."""
+    cfg = forward.cfg
+    n = cfg.nx * cfg.ny
+    horizons = sorted(int(h) for h in horizons)
+    rows = np.zeros((len(horizons), len(drops), 4), dtype=np.float32)
+    s0, m0 = np.float32(cfg.norm_std[0]), np.float32(cfg.norm_mean[0])
+    for j, drop in enumerate(drops):
+        x0 = initial_state(cfg, drop)
+        _, _, _, traj = forward.rollout(x0, meta, horizons[-1], flags, trajectory=True)
+        for i, hz in enumerate(horizons):
+            xn = traj[hz]
+            y, _, _ = reverse.rollout(xn, meta, hz, flags)
+            rows[i, j] = (correlation(y, x0), peak(y.ravel()[:n] * s0 + m0) / peak(x0.ravel()[:n] * s0 + m0),
+                          rmse(y, x0), rmse(xn, x0))
+    return rows
 
 
 def identity_config(n: int, g: float = 9.81, r_max: float = 1.0):

@@ -10,10 +10,10 @@
  *   crates/solvers/src/shallow_water.rs:114-124   mirror (ghost cells)
  *   crates/solvers/src/shallow_water.rs:149-238   ShallowWater::step
  *   crates/engine/src/norm.rs:27-34               Normalizer::encode
- *   crates/engine/src/metrics.rs:9-107            correlation, peak, mean,
+ *   crates/engine/src/metrics.rs:9-112            correlation, peak, mean,
  *                                                 std_dev, bias,
  *                                                 radial_profile, xcorr_lag,
- *                                                 decode_h
+ *                                                 decode_h, rmse
  *   crates/engine-cli/src/eval.rs:158-171         one scored row
  */
 #include "oracle.h"
@@ -215,6 +215,16 @@ float orc_xcorr_lag(const double* model, const double* solver, int n, int max_la
         }
     }
     return (float)best_lag;
+}
+
+/* metrics.rs:109-112 */
+float orc_rmse(const float* a, const float* b, int n) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double d = (double)(a[i] - b[i]);
+        s += d * d;
+    }
+    return (float)sqrt(s / (double)n);
 }
 
 /* norm.rs:27-34 */

@@ -244,3 +244,80 @@ def test_eval_metrics_command(tmp_path, capsys):
     out = capsys.readouterr().out
     assert "3 single-drop trajectories" in out and "| 10 |" in out
     assert "max relative energy violation" in out
+
+
+@pytest.fixture(scope="module")
+def pair64():
+    tf, cjf = synthetic_checkpoint(64, 128, 4, 0)
+    tr, cjr = synthetic_checkpoint(64, 128, 4, 1)
+    cfg = parse_config(cjf, tf)
+    f = engine.Model.from_bytes(write_safetensors_bytes(tf), cjf)
+    r = engine.Model.from_bytes(write_safetensors_bytes(tr), cjr)
+    yield f, r, cfg, O.OracleModel(cfg, tf), O.OracleModel(parse_config(cjr, tr), tr), (tf, cjf, tr, cjr)
+    f.close()
+    r.close()
+
+
+def test_roundtrip_matches_oracle(pair64):
+    f, r, cfg, of, orv, _ = pair64
+    horizons = [2, 5]
+    flags = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+    with engine.RoundTrip(f, r, 4, 2) as rt:
+        rows = rt.run(DROPS, horizons, flags)
+    want = O.roundtrip(of, orv, DROPS, horizons, O.MASS | O.ENERGY | O.SUM64, meta_of(cfg))
+    for i in range(len(horizons)):
+        for k in range(len(DROPS)):
+            g, w = rows[i, k], want[i, k]
+            assert abs(g["corr"] - w[0]) < 1e-5
+            assert abs(g["amplitude_ratio"] - w[1]) < 1e-4 * abs(w[1])
+            assert abs(g["rmse"] - w[2]) < 1e-4 * abs(w[2]) + 1e-6
+            assert abs(g["change_rmse"] - w[3]) < 1e-4 * abs(w[3]) + 1e-6
+
+
+def test_roundtrip_rows_do_not_depend_on_the_batch(pair64):
+    f, r, cfg, of, orv, _ = pair64
+    with engine.RoundTrip(f, r, 4, 3) as rt:
+        a = rt.run(DROPS, [1, 3, 6])
+        b = rt.run(DROPS, [1, 3, 6])
+        c = rt.run(DROPS[2:], [3])
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a[1, 2:], c[0])
+
+
+def test_roundtrip_bf16_close_to_fp32(pair64):
+    f, r, cfg, of, orv, (tf, cjf, tr, cjr) = pair64
+    with engine.Model.from_bytes(write_safetensors_bytes(tf), cjf, engine.BF16) as fb, \
+            engine.Model.from_bytes(write_safetensors_bytes(tr), cjr, engine.BF16) as rb:
+        with engine.RoundTrip(f, r, 4, 2) as r32, engine.RoundTrip(fb, rb, 4, 2) as r16:
+            a = r32.run(DROPS, [2, 4])
+            b = r16.run(DROPS, [2, 4])
+    assert np.abs(a["corr"] - b["corr"]).max() < 1e-2
+    assert np.abs(a["change_rmse"] - b["change_rmse"]).max() < 1e-2 * np.abs(a["change_rmse"]).max()
+
+
+def test_roundtrip_rejects_bad_arguments(pair64):
+    f, r, cfg, of, orv, _ = pair64
+    with engine.RoundTrip(f, r, 2, 2) as rt:
+        for drops, hz in [(DROPS, [3]), (DROPS[:1], [1, 2, 3]), (DROPS[:1], [2, 2]), (DROPS[:1], [0])]:
+            with pytest.raises(engine.JcError) as e:
+                rt.run(drops, hz)
+            assert e.value.name == "BAD_ARGUMENT"
+    t, cj = synthetic_checkpoint(32, 128, 4, 1)
+    with engine.Model.from_bytes(write_safetensors_bytes(t), cj) as other:
+        with pytest.raises(engine.JcError) as e:
+            engine.RoundTrip(f, other, 2, 2)
+        assert e.value.name == "BAD_SHAPE"
+
+
+def test_roundtrip_command(tmp_path, capsys):
+    from jacobi2000_gb300 import roundtrip
+
+    for name, seed in (("fwd", 0), ("rev", 1)):
+        t, cj = synthetic_checkpoint(128, 128, 4, seed)
+        (tmp_path / name).mkdir()
+        (tmp_path / name / "model.safetensors").write_bytes(write_safetensors_bytes(t))
+        (tmp_path / name / "config.json").write_text(cj)
+    assert roundtrip.main(["--forward", str(tmp_path / "fwd"), "--reverse", str(tmp_path / "rev"),
+                           "--horizons", "3,6", "--trajectories", "3"]) == 0
+    out = capsys.readouterr().out
+    assert "| 6 |" in out and "round-trip RMSE" in out
