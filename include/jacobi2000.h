@@ -70,6 +70,29 @@ jc_status jc_model_create(const uint8_t* safetensors, size_t safetensors_len,
                           const char* config_json, int32_t precision,
                           jc_model** out);
 
+/* ---- Pre-packed checkpoints ----
+ * No reference counterpart: the reference converts model.safetensors on every
+ * load (weights.rs:29-48, gpu.rs:212-283). A pre-packed checkpoint is the
+ * model's device weight image (every array in the layouts the kernels read,
+ * for the model's precision) with its config and the identity of its source,
+ * cached beside model.safetensors; the source format is unchanged.
+ *
+ * jc_model_pack writes it into `buf` (cap bytes) and sets *len; with buf null
+ * it only sets *len. */
+jc_status jc_model_pack(const jc_model* m, uint8_t* buf, size_t cap, size_t* len);
+
+/* Creates a model from a pre-packed checkpoint: one device allocation and one
+ * host->device copy of the weights, no conversion. Malformed or truncated
+ * images give JC_BAD_CHECKPOINT before any device work. */
+jc_status jc_model_create_packed(const uint8_t* packed, size_t len, jc_model** out);
+
+/* The source identity a pre-packed checkpoint records (fnv1a-64 over the
+ * safetensors bytes, then the config text), and the one it holds: a cache
+ * is current when the two agree. Host only. */
+jc_status jc_source_hash(const uint8_t* safetensors, size_t safetensors_len, const char* config_json,
+                         uint64_t* out);
+jc_status jc_packed_source_hash(const uint8_t* packed, size_t len, uint64_t* out);
+
 /* Replaces dropping a GpuModel (gpu.rs:199-209). Null is accepted. */
 void jc_model_destroy(jc_model* m);
 

@@ -165,16 +165,24 @@ constexpr int kHaloPlane = (kHaloW * kHaloH * 16 + 127) / 128 * 128;
 
 __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 
-// Token embedding and the first LayerNorm (cpu.rs:253-280, 289). One CTA per
-// 64 token rows: the embed weights [pd][D] and the 64 patches (transposed,
-// [pd][64], gathered from the state) are staged in shared memory by
-// asynchronous copies, all in flight at once. Warp w
-// owns rows 8w..8w+7 and lane l owns the CPL = D/32 consecutive outputs
-// [CPL l, CPL l + CPL): per patch element it reads 8 patch values and CPL
-// weights once and does 8 x CPL FMAs. Each output is summed in the
-// reference's order (bias, then the patch elements in order, then + pos,
-// + the meta linear); x is written f32 and LayerNorm(x) bf16.
+// Token embedding and the first LayerNorm (cpu.rs:253-280, 289). Persistent
+// CTAs walk tiles of 64 token rows: the embed weights [pd][D] are staged in
+// shared memory once per CTA, and each tile's patches arrive as 16-byte
+// asynchronous copies (one per (row, channel, patch row): 4 cells), double-
+// buffered so the next tile's patches are in flight while this one is
+// summed. Patches sit as [channel, patch row][row][4] floats. Warp w owns
+// rows 8w..8w+7 and lane l owns the CPL = D/32 consecutive outputs
+// [CPL l, CPL l + CPL): per group of 4 patch elements it reads 8 patch
+// float4s and 4 x CPL weights and does 32 x CPL FMAs. Each output is summed in
+// the reference's order (bias, then the patch elements in order, then + pos,
+// + the meta linear); x is written f32 and LayerNorm(x) bf16, with vector
+// stores.
 constexpr int kEmbedRows = 64;
+constexpr int kEmbedGroups = 12;  // 3 channels x 4 patch rows, 4 patch columns each
+
+__host__ __device__ constexpr size_t embed_smem(int D) {
+    return ((size_t)48 * D + 2 * (size_t)kEmbedGroups * kEmbedRows * 4) * sizeof(float);
+}
 
 template <int CPL>
 __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __restrict__ We,
@@ -185,106 +193,138 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
     extern __shared__ __align__(16) float esm[];
     constexpr int D = 32 * CPL;
     constexpr int P = 4, pd = 3 * P * P;  // 3 channels, patch 4 (checked when the path is built)
-    float* sW = esm;                   // [pd][D]
-    float* sP = esm + (size_t)pd * D;  // [pd][kEmbedRows]
-    __shared__ int rinst[kEmbedRows];
-    __shared__ const float* rbase[kEmbedRows];  // the row's patch origin in its state (channel 0)
-    __shared__ int rpitch[kEmbedRows];          // the state's row pitch (nx)
-    __shared__ long long rplane[kEmbedRows];    // the state's channel plane (nx * ny)
-    const int r0 = blockIdx.x * kEmbedRows;
+    float* sW = esm;                      // [pd][D]
+    float4* sP = reinterpret_cast<float4*>(esm + (size_t)pd * D);  // 2 x [groups][kEmbedRows] float4
+    __shared__ int rinst[2][kEmbedRows];
+    const int n_tiles = (R + kEmbedRows - 1) / kEmbedRows;
     for (int i = threadIdx.x; i < pd * D / 4; i += blockDim.x)
         cp_async16(reinterpret_cast<float4*>(sW) + i, reinterpret_cast<const float4*>(We) + i, true);
-    if (threadIdx.x < kEmbedRows) {
-        const int r = r0 + (int)threadIdx.x;
-        const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
-        rinst[threadIdx.x] = ii;
-        if (ii >= 0) {
-            const InstDev& I = inst[ii];
-            const int t = r - I.row0;
-            rbase[threadIdx.x] = I.state + (size_t)(t / I.tx) * P * I.nx + (size_t)(t % I.tx) * P;
-            rpitch[threadIdx.x] = I.nx;
-            rplane[threadIdx.x] = (long long)I.nx * I.ny;
+    // the patches of tile t into buffer `buf` (and each row's instance)
+    auto issue = [&](int t, int buf) {
+        for (int e = threadIdx.x; e < kEmbedRows * kEmbedGroups; e += blockDim.x) {
+            const int i = e % kEmbedRows, gq = e / kEmbedRows;  // row, (channel, patch row)
+            const int r = t * kEmbedRows + i;
+            const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
+            if (gq == 0) rinst[buf][i] = ii;
+            const float* src = We;
+            if (ii >= 0) {
+                const InstDev& I = inst[ii];
+                const int tk = r - I.row0, c = gq / P, py = gq % P;
+                src = I.state + (size_t)c * I.nx * I.ny + ((size_t)(tk / I.tx) * P + py) * I.nx +
+                      (size_t)(tk % I.tx) * P;
+            }
+            cp_async16(sP + ((size_t)buf * kEmbedGroups + gq) * kEmbedRows + i, src, ii >= 0);
         }
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < kEmbedRows * pd; e += blockDim.x) {
-        const int i = e % kEmbedRows, f = e / kEmbedRows;
-        const int c = f / (P * P), py = (f / P) % P, px = f % P;
-        const bool in = rinst[i] >= 0;
-        const float* src = in ? rbase[i] + c * rplane[i] + (size_t)py * rpitch[i] + px : We;
-        cp_async4(sP + f * kEmbedRows + i, src, in);
-    }
-    cp_async_wait_all();
-    __syncthreads();
+        cp_async_commit();
+    };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i0 = warp * 8;  // this warp's 8 rows
-    if (r0 + i0 >= R) return;
     const int o0 = CPL * lane;
-    float v[8][CPL];
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-#pragma unroll
-        for (int c = 0; c < CPL; c++) v[k][c] = be[o0 + c];
-#pragma unroll 8
-    for (int f = 0; f < pd; f++) {
-        const float4 p0 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0);
-        const float4 p1 = *reinterpret_cast<const float4*>(sP + f * kEmbedRows + i0 + 4);
-        const float pv[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-        float wv[CPL];
-        if (CPL % 4 == 0) {
-#pragma unroll
-            for (int c = 0; c < CPL; c += 4) {
-                const float4 w4 = *reinterpret_cast<const float4*>(sW + f * D + o0 + c);
-                wv[c] = w4.x; wv[c + 1] = w4.y; wv[c + 2] = w4.z; wv[c + 3] = w4.w;
-            }
+    int k = 0;
+    if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, k++) {
+        const int buf = k & 1;
+        if (t + (int)gridDim.x < n_tiles) {
+            issue(t + gridDim.x, buf ^ 1);
+            cp_async_wait_group<1>();
         } else {
-#pragma unroll
-            for (int c = 0; c < CPL; c++) wv[c] = sW[f * D + o0 + c];
+            cp_async_wait_group<0>();
         }
+        __syncthreads();
+        const int r0 = t * kEmbedRows;
+        if (r0 + i0 < R) {
+            float v[8][CPL];
 #pragma unroll
-        for (int k = 0; k < 8; k++)
+            for (int q = 0; q < 8; q++)
 #pragma unroll
-            for (int c = 0; c < CPL; c++) v[k][c] = fmaf(pv[k], wv[c], v[k][c]);
-    }
-    // the meta linear depends only on the instance: computed once for the
-    // warp's first row and again only where the instance changes
-    int m_inst = -1;
-    float m[CPL];
+                for (int c = 0; c < CPL; c++) v[q][c] = be[o0 + c];
+            const float4* pb = sP + (size_t)buf * kEmbedGroups * kEmbedRows + i0;
+#pragma unroll 2
+            for (int gq = 0; gq < kEmbedGroups; gq++) {
+                float4 p4[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int r = r0 + i0 + k;
-        if (r >= R) continue;  // warp-uniform
-        const int ii = rinst[i0 + k];
-        const InstDev& I = inst[ii];
-        if (ii != m_inst) {
-            m_inst = ii;
+                for (int q = 0; q < 8; q++) p4[q] = pb[gq * kEmbedRows + q];
 #pragma unroll
-            for (int c = 0; c < CPL; c++) {
-                m[c] = bm[o0 + c];
-                for (int f = 0; f < d.meta_dim; f++) m[c] = fmaf(I.meta[f], Wm[(size_t)f * D + o0 + c], m[c]);
+                for (int px = 0; px < 4; px++) {
+                    const int f = gq * 4 + px;
+                    float wv[CPL];
+                    if (CPL % 4 == 0) {
+#pragma unroll
+                        for (int c = 0; c < CPL; c += 4) {
+                            const float4 w4 = *reinterpret_cast<const float4*>(sW + f * D + o0 + c);
+                            wv[c] = w4.x; wv[c + 1] = w4.y; wv[c + 2] = w4.z; wv[c + 3] = w4.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < CPL; c++) wv[c] = sW[f * D + o0 + c];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const float pv = px == 0 ? p4[q].x : px == 1 ? p4[q].y : px == 2 ? p4[q].z : p4[q].w;
+#pragma unroll
+                        for (int c = 0; c < CPL; c++) v[q][c] = fmaf(pv, wv[c], v[q][c]);
+                    }
+                }
+            }
+            // the meta linear depends only on the instance: computed once for
+            // the warp's first row and again only where the instance changes
+            int m_inst = -1;
+            float m[CPL];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int r = r0 + i0 + q;
+                if (r >= R) continue;  // warp-uniform
+                const int ii = rinst[buf][i0 + q];
+                const InstDev& I = inst[ii];
+                if (ii != m_inst) {
+                    m_inst = ii;
+#pragma unroll
+                    for (int c = 0; c < CPL; c++) {
+                        m[c] = bm[o0 + c];
+                        for (int f = 0; f < d.meta_dim; f++) m[c] = fmaf(I.meta[f], Wm[(size_t)f * D + o0 + c], m[c]);
+                    }
+                }
+                const int tk = r - I.row0;
+                const float* pos = I.pos + (size_t)tk * D + o0;
+                float sum = 0.f;
+#pragma unroll
+                for (int c = 0; c < CPL; c++) {
+                    v[q][c] = (v[q][c] + pos[c]) + m[c];
+                    sum += v[q][c];
+                }
+                const float mean = warp_sum(sum) / (float)D;
+                float sq = 0.f;
+#pragma unroll
+                for (int c = 0; c < CPL; c++) sq += (v[q][c] - mean) * (v[q][c] - mean);
+                const float rstd = 1.0f / sqrtf(warp_sum(sq) / (float)D + 1e-5f);
+                float o[CPL];
+#pragma unroll
+                for (int c = 0; c < CPL; c++) o[c] = (v[q][c] - mean) * rstd * g[o0 + c] + b[o0 + c];
+                float* xr = x + (size_t)r * D + o0;
+                bf16* lr = ln + (size_t)r * D + o0;
+                if (CPL % 4 == 0) {
+#pragma unroll
+                    for (int c = 0; c < CPL; c += 4) {
+                        *reinterpret_cast<float4*>(xr + c) = make_float4(v[q][c], v[q][c + 1], v[q][c + 2], v[q][c + 3]);
+                        __nv_bfloat162 lo = __floats2bfloat162_rn(o[c], o[c + 1]);
+                        __nv_bfloat162 hi = __floats2bfloat162_rn(o[c + 2], o[c + 3]);
+                        uint2 u;
+                        u.x = *reinterpret_cast<uint32_t*>(&lo);
+                        u.y = *reinterpret_cast<uint32_t*>(&hi);
+                        *reinterpret_cast<uint2*>(lr + c) = u;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; c++) {
+                        xr[c] = v[q][c];
+                        lr[c] = __float2bfloat16(o[c]);
+                    }
+                }
             }
         }
-        const int t = r - I.row0;
-        float sum = 0.f;
-#pragma unroll
-        for (int c = 0; c < CPL; c++) {
-            v[k][c] = (v[k][c] + I.pos[(size_t)t * D + o0 + c]) + m[c];
-            sum += v[k][c];
-        }
-        const float mean = warp_sum(sum) / (float)D;
-        float q = 0.f;
-#pragma unroll
-        for (int c = 0; c < CPL; c++) q += (v[k][c] - mean) * (v[k][c] - mean);
-        const float rstd = 1.0f / sqrtf(warp_sum(q) / (float)D + 1e-5f);
-        float o[CPL];
-#pragma unroll
-        for (int c = 0; c < CPL; c++) {
-            x[(size_t)r * D + o0 + c] = v[k][c];
-            o[c] = (v[k][c] - mean) * rstd * g[o0 + c] + b[o0 + c];
-        }
-#pragma unroll
-        for (int c = 0; c < CPL; c++) ln[(size_t)r * D + o0 + c] = __float2bfloat16(o[c]);
+        __syncthreads();  // every warp is done with `buf` before it is refilled
     }
+    cp_async_wait_group<0>();
 }
 
 // Packed bf16 vectors of 1, 4 or 8 elements <-> f32.
@@ -2080,11 +2120,13 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
 // the output is bit-identical.
 constexpr int kC1PThreads = 6 * 32;
 
+constexpr int kC1PHaloStages = 3;  // halo tiles in flight per CTA
+
 struct C1PSmem {
     size_t halo, w, stage, total;
     __host__ __device__ C1PSmem(int C, int BN) {
-        halo = 0;                                                  // 2 x [C/8][18][10][8]
-        w = halo + 2 * (size_t)(C / 8) * kHaloPlane;               // 9 x [C/8][BN][8]
+        halo = 0;                                                                // stages x [C/8][18][10][8]
+        w = halo + (size_t)kC1PHaloStages * (C / 8) * kHaloPlane;                // 9 x [C/8][BN][8]
         stage = (w + (size_t)9 * C * BN * 2 + 1023) / 1024 * 1024;  // 2 x 16 KB boxes
         total = stage + 2 * 16384;
     }
@@ -2102,7 +2144,8 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
     uint8_t* sW = smem + L.w;
     uint8_t* sStage = smem + L.stage;
     const size_t halo_bytes = (size_t)(C / 8) * kHaloPlane;
-    __shared__ uint64_t w_full, h_full[2], h_empty[2], a_full[2], a_empty[2];
+    constexpr int HS = kC1PHaloStages;
+    __shared__ uint64_t w_full, h_full[HS], h_empty[HS], a_full[2], a_empty[2];
     __shared__ __align__(16) float sbias[BN];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
@@ -2110,9 +2153,11 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
     const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (threadIdx.x == 0) {
         tc::mbar_init(&w_full, 1);
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < HS; i++) {
             tc::mbar_init(&h_full[i], 1);
             tc::mbar_init(&h_empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
             tc::mbar_init(&a_full[i], 1);
             tc::mbar_init(&a_empty[i], 4 * 32);
         }
@@ -2147,15 +2192,16 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
         if (lane == 0 && !failed) {
             // halo producer
             for (int it = 0; it < my_tiles; it++) {
-                const int b = it & 1;
-                if (it >= 2 && !tc::mbar_wait(&h_empty[b], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) break;
+                const int hb = it % HS;
+                if (it >= HS && !tc::mbar_wait(&h_empty[hb], (uint32_t)((it - HS) / HS) & 1u, err, &failed)) break;
                 int ii, x0, y0;
                 locate((int)blockIdx.x + it * (int)gridDim.x, ii, x0, y0);
                 const CUtensorMap* map = maps + kMapsPerInst * ii + 1;
                 tc::tensormap_acquire(map);
-                tc::mbar_expect_tx(&h_full[b], (uint32_t)(C / 8) * (kHaloW * kHaloH * 16));
+                tc::mbar_expect_tx(&h_full[hb], (uint32_t)(C / 8) * (kHaloW * kHaloH * 16));
                 for (int kc = 0; kc < C / 8; kc++)
-                    tc::tma_load_3d(sHalo + b * halo_bytes + kc * kHaloPlane, map, kc * 8, x0 - 1, y0 - 1, &h_full[b]);
+                    tc::tma_load_3d(sHalo + hb * halo_bytes + kc * kHaloPlane, map, kc * 8, x0 - 1, y0 - 1,
+                                    &h_full[hb]);
             }
         }
         __syncwarp();
@@ -2168,12 +2214,12 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
             const uint32_t idesc = tc::idesc_f16(128, BN);  // f16 input and weights
             const uint32_t w0 = tc::smem_u32(sW);
             for (int it = 0; it < my_tiles && good; it++) {
-                const int b = it & 1;
-                good = tc::mbar_wait(&h_full[b], (uint32_t)(it >> 1) & 1u, err, &failed) &&
+                const int b = it & 1, hb = it % HS;
+                good = tc::mbar_wait(&h_full[hb], (uint32_t)(it / HS) & 1u, err, &failed) &&
                        (it < 2 || tc::mbar_wait(&a_empty[b], (uint32_t)((it - 2) >> 1) & 1u, err, &failed));
                 if (!good) break;
                 tc::tc_fence_after();
-                const uint32_t h0 = tc::smem_u32(sHalo + b * halo_bytes);
+                const uint32_t h0 = tc::smem_u32(sHalo + hb * halo_bytes);
                 const uint32_t acc = tmem + (uint32_t)b * BN;
                 for (int t = 0; t < 9; t++) {
                     const int ky = t / 3, kx = t % 3;
@@ -2184,7 +2230,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
                         tc::mma_bf16(acc, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
                     }
                 }
-                tc::mma_commit(&h_empty[b]);
+                tc::mma_commit(&h_empty[hb]);
                 tc::mma_commit(&a_full[b]);
             }
         }
@@ -2253,9 +2299,7 @@ static size_t attn_tile_smem(const Dims& d) { return (size_t)(d.D / 64) * (2 * k
 // host
 
 static const bf16* upload_bf16(DeviceArena& a, const std::vector<uint16_t>& v) {
-    void* d = a.alloc(v.size() * 2);
-    cuda_check(cudaMemcpy(d, v.data(), v.size() * 2, cudaMemcpyHostToDevice), "upload weights", JC_MAP);
-    return static_cast<const bf16*>(d);
+    return static_cast<const bf16*>(a.upload_bytes(v.data(), v.size() * 2));
 }
 
 // B[n][k] for n < N, k < K into [N/BN][K/8][BN][8].
@@ -2281,7 +2325,23 @@ static void set_smem(K kernel, size_t bytes) {
                "cudaFuncSetAttribute");
 }
 
-BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
+void BF16Path::weight_slots(std::vector<const void**>& out) const {
+    auto add = [&](const bf16* const& p) { out.push_back(reinterpret_cast<const void**>(const_cast<const bf16**>(&p))); };
+    for (int l = 0; l < dims_.L; l++) {
+        add(wqkv[l]);
+        add(wp[l]);
+    }
+    for (int v = 0; v < n_nc; v++)
+        for (int l = 0; l < dims_.L; l++) {
+            add(w1v[v][l]);
+            add(w2v[v][l]);
+        }
+    add(wtm);
+    add(wtc);
+    add(wc1);
+}
+
+BF16Path::BF16Path(const Dims& d, const TensorMap* tp, DeviceArena* ap) {
     const int D = d.D, F = d.F, HD = d.HD;
     dims_D_ = D;
     dims_F_ = F;
@@ -2304,6 +2364,20 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
     if (!mlp_fits(64, 1, 0)) def_tuning_.nc = 32;
     if (!mlp_fits(def_tuning_.nc, 1, 0)) throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
     if (attn_tile_ok(d)) def_tuning_.attn_threads = 0;  // shared-memory attention tiles
+    for (int l = 0; l < kMaxLayers; l++) {
+        wqkv[l] = wp[l] = nullptr;
+        w1v[0][l] = w1v[1][l] = w2v[0][l] = w2v[1][l] = nullptr;
+    }
+    wtm = wtc = wc1 = nullptr;
+    if (tp) upload_weights(d, *tp, *ap);
+    cache_key_ = "d" + std::to_string(D) + "_l" + std::to_string(d.L) + "_f" + std::to_string(F) + "_r" +
+                 std::to_string(d.radius) + "_k" + std::to_string(d.mask_kind) + "_g" + std::to_string(d.dilation);
+    load_cache();
+    set_kernel_attributes();
+}
+
+void BF16Path::upload_weights(const Dims& d, const TensorMap& t, DeviceArena& arena) {
+    const int D = d.D, F = d.F, HD = d.HD;
     for (int l = 0; l < d.L; l++) {
         const std::string p = "blocks." + std::to_string(l) + ".";
         const auto &q = tget(t, p + "q.weight").data, &k = tget(t, p + "k.weight").data, &v = tget(t, p + "v.weight").data;
@@ -2373,9 +2447,9 @@ BF16Path::BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena) {
                     }
         wc1 = upload_bf16(arena, o);  // f16 bits
     }
-    cache_key_ = "d" + std::to_string(D) + "_l" + std::to_string(d.L) + "_f" + std::to_string(F) + "_r" +
-                 std::to_string(d.radius) + "_k" + std::to_string(d.mask_kind) + "_g" + std::to_string(d.dilation);
-    load_cache();
+}
+
+void BF16Path::set_kernel_attributes() {
     set_smem(tc_gemm_kernel<EPI_BF16>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_F32>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
@@ -2655,12 +2729,20 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     const Tuning tu = tuning_for(R);
     {
         KScope k("bf_embed", s);
-        const unsigned blocks = (unsigned)((R + kEmbedRows - 1) / kEmbedRows);
-        const size_t smem = ((size_t)d.C * d.P * d.P * D + (size_t)kEmbedRows * d.C * d.P * d.P) * sizeof(float);
-#define JC_EMBED(CPL)                                                                                           \
-    case CPL:                                                                                                   \
-        bf_embed_kernel<CPL><<<blocks, 256, smem, s>>>(d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, \
-                                                       w.blk[0].n1b, p.inst, n, R, p.x, ln);                     \
+        const int tiles = (R + kEmbedRows - 1) / kEmbedRows;
+        const size_t smem = embed_smem(D);
+        // persistent: as many CTAs as fit on the SMs at once
+        static int occupancy[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // CTAs per SM, per D / 32
+        auto grid_for = [&](auto kernel) {
+            int& per_sm = occupancy[D / 32];
+            if (per_sm == 0)
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, smem), "occupancy");
+            return (unsigned)std::min(tiles, std::max(1, per_sm) * n_sms_);
+        };
+#define JC_EMBED(CPL)                                                                                            \
+    case CPL:                                                                                                    \
+        bf_embed_kernel<CPL><<<grid_for(bf_embed_kernel<CPL>), 256, smem, s>>>(                                  \
+            d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);     \
         break;
         switch (D / 32) {
             JC_EMBED(1) JC_EMBED(2) JC_EMBED(3) JC_EMBED(4) JC_EMBED(5) JC_EMBED(6) JC_EMBED(7) JC_EMBED(8)

@@ -33,7 +33,11 @@ extern std::atomic<int> g_autotune;
 
 class BF16Path {
    public:
-    BF16Path(const Dims& d, const TensorMap& t, DeviceArena& arena);
+    // With `t`, converts and uploads the weights through `arena`; without,
+    // leaves the weight pointers for the caller to set (pre-packed load).
+    BF16Path(const Dims& d, const TensorMap* t, DeviceArena* arena);
+    // Addresses of every weight pointer, in a fixed order.
+    void weight_slots(std::vector<const void**>& out) const;
     // Allocates this path's token- and cell-level buffers into p.bt / p.bc
     // and its per-instance tensor-map array into p.tmaps.
     void alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows, long long cells, int max_inst) const;
@@ -69,6 +73,8 @@ class BF16Path {
     mutable std::map<int, Tuning> tuned_;  // row-count bucket -> schedule
     std::string cache_key_;
     void load_cache();
+    void upload_weights(const Dims& d, const TensorMap& t, DeviceArena& arena);
+    void set_kernel_attributes();
     void save_cache(int bucket, const Tuning& t, const std::string& timings) const;
 };
 

@@ -73,6 +73,37 @@ jc_status jc_model_create(const uint8_t* st, size_t st_len, const char* config_j
     });
 }
 
+jc_status jc_model_pack(const jc_model* m, uint8_t* buf, size_t cap, size_t* len) {
+    if (!m || !len) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] {
+        std::vector<uint8_t> p = m->m->pack();
+        *len = p.size();
+        if (buf) {
+            if (cap < p.size()) throw jc::Error(JC_LIMIT, "buffer smaller than the pre-packed checkpoint");
+            std::memcpy(buf, p.data(), p.size());
+        }
+    });
+}
+
+jc_status jc_model_create_packed(const uint8_t* packed, size_t len, jc_model** out) {
+    if (!out) return fail(JC_BAD_ARGUMENT, "out is null");
+    *out = nullptr;
+    return guard([&] {
+        jc::Model* m = new jc::Model(packed, len);
+        *out = new jc_model{m};
+    });
+}
+
+jc_status jc_source_hash(const uint8_t* st, size_t st_len, const char* config_json, uint64_t* out) {
+    if (!st || !config_json || !out) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] { *out = jc::source_hash(st, st_len, config_json); });
+}
+
+jc_status jc_packed_source_hash(const uint8_t* packed, size_t len, uint64_t* out) {
+    if (!out) return fail(JC_BAD_ARGUMENT, "null argument");
+    return guard([&] { *out = jc::packed_source_hash(packed, len); });
+}
+
 void jc_model_destroy(jc_model* m) {
     if (!m) return;
     try {

@@ -318,14 +318,14 @@ __global__ void __launch_bounds__(kConv2Threads, 8) conv2_step_kernel(const floa
                 for (int ky = 0; ky < 3; ky++)
 #pragma unroll
                     for (int kx = 0; kx < 3; kx++) {
-                        const float* w = cw.w + (ci * 9 + ky * 3 + kx) * 3;
+                        const int wi = (ci * 9 + ky * 3 + kx) * 3;  // a constant after unrolling
 #pragma unroll
                         for (int i = 0; i < 2; i++) {
                             const float4 av = a[i + ky][kx];
                             const float v = c == 0 ? av.x : c == 1 ? av.y : c == 2 ? av.z : av.w;
-                            acc[i][0] = fmaf(v, w[0], acc[i][0]);
-                            acc[i][1] = fmaf(v, w[1], acc[i][1]);
-                            acc[i][2] = fmaf(v, w[2], acc[i][2]);
+                            acc[i][0] = fmaf(v, cw.w[wi], acc[i][0]);
+                            acc[i][1] = fmaf(v, cw.w[wi + 1], acc[i][1]);
+                            acc[i][2] = fmaf(v, cw.w[wi + 2], acc[i][2]);
                         }
                     }
             }

@@ -199,10 +199,54 @@ void* DeviceArena::alloc(size_t bytes) {
     return p;
 }
 
+// Provisional addresses of image arrays start here until end_image() rebases
+// them (never dereferenced: every slot is rebased, and counted, first).
+static constexpr uint64_t kImageProvisional = 1ull << 52;
+
 float* DeviceArena::upload(const std::vector<float>& v) {
-    float* d = alloc_n<float>(v.size());
-    cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice), "upload weights", JC_MAP);
+    return static_cast<float*>(const_cast<void*>(upload_bytes(v.data(), v.size() * sizeof(float))));
+}
+
+const void* DeviceArena::upload_bytes(const void* src, size_t bytes) {
+    if (imaging_) {
+        const size_t off = (image.size() + 255) / 256 * 256;
+        image.resize(off + (bytes ? bytes : 1), 0);
+        if (bytes) std::memcpy(image.data() + off, src, bytes);
+        image_arrays_++;
+        return reinterpret_cast<const void*>(kImageProvisional + off);
+    }
+    void* d = alloc(bytes);
+    cuda_check(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice), "upload weights", JC_MAP);
     return d;
+}
+
+void DeviceArena::begin_image() {
+    image.clear();
+    image_arrays_ = 0;
+    imaging_ = true;
+}
+
+std::vector<uint64_t> DeviceArena::end_image(const std::vector<const void**>& slots) {
+    imaging_ = false;
+    const uint64_t lo = kImageProvisional, hi = kImageProvisional + image.size();
+    size_t provisional = 0;
+    for (const void** sl : slots) {
+        const uint64_t a = (uint64_t)(uintptr_t)*sl;
+        if (a >= lo && a < hi) provisional++;
+    }
+    if (provisional != image_arrays_ || slots.size() != image_arrays_)
+        throw Error(JC_CUDA_ERROR, "internal: the weight slots do not match the weight image");
+    image_len = image.size();
+    image_base = alloc(image_len);
+    cuda_check(cudaMemcpy(image_base, image.data(), image_len, cudaMemcpyHostToDevice), "upload weights", JC_MAP);
+    std::vector<uint64_t> off(slots.size());
+    for (size_t i = 0; i < slots.size(); i++) {
+        off[i] = (uint64_t)(uintptr_t)*slots[i] - lo;
+        *slots[i] = static_cast<const char*>(image_base) + off[i];
+    }
+    image.clear();
+    image.shrink_to_fit();
+    return off;
 }
 
 void DeviceArena::release(void* p) {
@@ -433,6 +477,103 @@ static void upload_weights(const TensorMap& t, const Dims& dims, DeviceArena& ar
     w.shared_hash = h;
 }
 
+// Addresses of every device weight pointer of a model, in a fixed order (the
+// order of the pre-packed image's slot table).
+static std::vector<const void**> weight_slots(DeviceWeights& w, const Dims& d) {
+    std::vector<const void**> s;
+    WeightsF32& f = w.f32;
+    auto add = [&](const float* const& p) { s.push_back(reinterpret_cast<const void**>(const_cast<const float**>(&p))); };
+    add(f.embed_w);
+    add(f.embed_b);
+    add(f.meta_w);
+    add(f.meta_b);
+    add(w.pos);
+    for (int l = 0; l < d.L; l++) {
+        auto& B = f.blk[l];
+        for (const float* const* p : {&B.n1g, &B.n1b, &B.wqkv, &B.bqkv, &B.wp, &B.bp, &B.n2g, &B.n2b, &B.w1, &B.b1,
+                                      &B.w2, &B.b2})
+            add(*p);
+    }
+    for (const float* const* p : {&f.norm_g, &f.norm_b, &f.tm_w, &f.tm_b, &f.tc_w, &f.tc_b, &f.c1_w, &f.c1_b,
+                                  &f.c2_w, &f.c2_b})
+        add(*p);
+    if (w.bf16) w.bf16->weight_slots(s);
+    return s;
+}
+
+uint64_t source_hash(const uint8_t* st, size_t st_len, const char* config_json) {
+    uint64_t h = 1469598103934665603ull;
+    h = fnv1a(h, st, st_len);
+    if (config_json) h = fnv1a(h, config_json, std::strlen(config_json));
+    return h;
+}
+
+// ---------------------------------------------------------------------------
+// Pre-packed checkpoint: "JCPACK01", then little-endian u32 version (1),
+// u32 precision, u64 source hash, u64 shared-tensor hash, the jc_config
+// struct, u32 has-conv2 + the Conv2Params struct, u32 slot count + u64
+// offsets, u64 image length, the image. Host and device are little-endian
+// on every supported platform (x86-64 and aarch64).
+
+static constexpr char kPackMagic[8] = {'J', 'C', 'P', 'A', 'C', 'K', '0', '1'};
+
+namespace {
+struct PackReader {
+    const uint8_t* p;
+    size_t n, at = 0;
+    void get(void* dst, size_t k) {
+        if (k > n - at) throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint is truncated");
+        std::memcpy(dst, p + at, k);
+        at += k;
+    }
+    template <class T>
+    T get() {
+        T v;
+        get(&v, sizeof(T));
+        return v;
+    }
+};
+struct PackHeader {
+    uint32_t precision = 0;
+    uint64_t source = 0, shared = 0;
+    jc_config cfg{};
+    uint32_t has_conv2 = 0;
+    Conv2Params conv2{};
+    std::vector<uint64_t> slots;
+    uint64_t image_len = 0;
+    size_t image_at = 0;
+};
+PackHeader read_pack_header(const uint8_t* p, size_t n) {
+    if (!p) throw Error(JC_BAD_ARGUMENT, "null pre-packed checkpoint");
+    PackReader r{p, n};
+    char magic[8];
+    r.get(magic, 8);
+    if (std::memcmp(magic, kPackMagic, 8) != 0) throw Error(JC_BAD_CHECKPOINT, "not a pre-packed checkpoint");
+    if (r.get<uint32_t>() != 1) throw Error(JC_BAD_CHECKPOINT, "unsupported pre-packed checkpoint version");
+    PackHeader h;
+    h.precision = r.get<uint32_t>();
+    h.source = r.get<uint64_t>();
+    h.shared = r.get<uint64_t>();
+    h.cfg = r.get<jc_config>();
+    h.has_conv2 = r.get<uint32_t>();
+    h.conv2 = r.get<Conv2Params>();
+    const uint32_t ns = r.get<uint32_t>();
+    if (ns > 100000) throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint: bad slot count");
+    h.slots.resize(ns);
+    for (auto& o : h.slots) o = r.get<uint64_t>();
+    h.image_len = r.get<uint64_t>();
+    if (h.image_len > n - r.at) throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint is truncated");
+    h.image_at = r.at;
+    for (uint64_t o : h.slots)
+        if (o >= h.image_len || o % 256) throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint: bad slot offset");
+    if (h.precision != JC_FP32 && h.precision != JC_BF16)
+        throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint: bad precision");
+    return h;
+}
+}  // namespace
+
+uint64_t packed_source_hash(const uint8_t* packed, size_t len) { return read_pack_header(packed, len).source; }
+
 // ---------------------------------------------------------------------------
 // Model: one checkpoint, one grid, one request at a time.
 
@@ -444,9 +585,72 @@ Model::Model(const uint8_t* st, size_t st_len, const char* config_json, int prec
     require_device();
     dims = dims_of(cfg);
     cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    source_hash = jc::source_hash(st, st_len, config_json);
+    arena.begin_image();
     upload_weights(t, dims, arena, w);
-    if (precision == JC_BF16) w.bf16 = std::make_unique<BF16Path>(dims, t, arena);
+    if (precision == JC_BF16) w.bf16 = std::make_unique<BF16Path>(dims, &t, &arena);
+    slot_off_ = arena.end_image(weight_slots(w, dims));
+    finish_init();
+}
 
+Model::Model(const uint8_t* packed, size_t len) {
+    PackHeader h = read_pack_header(packed, len);
+    cfg = h.cfg;
+    precision = (int)h.precision;
+    if (cfg.nx < 1 || cfg.ny < 1 || cfg.patch < 1 || cfg.nx % cfg.patch || cfg.ny % cfg.patch || cfg.layers < 0 ||
+        cfg.layers > kMaxLayers || cfg.dim < 1 || cfg.heads < 1 || cfg.channels != 3)
+        throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint: bad config");
+    require_device();
+    dims = dims_of(cfg);
+    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    source_hash = h.source;
+    w.shared_hash = h.shared;
+    if (h.has_conv2) {
+        w.conv2.reset(new Conv2Params(h.conv2));
+        w.f32.c2p = w.conv2.get();
+    }
+    if (precision == JC_BF16) w.bf16 = std::make_unique<BF16Path>(dims, nullptr, nullptr);
+    std::vector<const void**> slots = weight_slots(w, dims);
+    if (slots.size() != h.slots.size())
+        throw Error(JC_BAD_CHECKPOINT, "pre-packed checkpoint: slot table does not match its config");
+    arena.image_len = h.image_len;
+    arena.image_base = arena.alloc(h.image_len);
+    cuda_check(cudaMemcpy(arena.image_base, packed + h.image_at, h.image_len, cudaMemcpyHostToDevice),
+               "upload weights", JC_MAP);
+    for (size_t i = 0; i < slots.size(); i++) *slots[i] = static_cast<const char*>(arena.image_base) + h.slots[i];
+    slot_off_ = h.slots;
+    finish_init();
+}
+
+std::vector<uint8_t> Model::pack() const {
+    std::vector<uint8_t> out;
+    auto put = [&](const void* p, size_t k) {
+        const uint8_t* b = static_cast<const uint8_t*>(p);
+        out.insert(out.end(), b, b + k);
+    };
+    put(kPackMagic, 8);
+    const uint32_t version = 1, prec = (uint32_t)precision, has_conv2 = w.conv2 ? 1u : 0u;
+    put(&version, 4);
+    put(&prec, 4);
+    put(&source_hash, 8);
+    put(&w.shared_hash, 8);
+    put(&cfg, sizeof(cfg));
+    put(&has_conv2, 4);
+    Conv2Params c2{};
+    if (w.conv2) c2 = *w.conv2;
+    put(&c2, sizeof(c2));
+    const uint32_t ns = (uint32_t)slot_off_.size();
+    put(&ns, 4);
+    put(slot_off_.data(), slot_off_.size() * 8);
+    const uint64_t il = arena.image_len;
+    put(&il, 8);
+    const size_t at = out.size();
+    out.resize(at + il);
+    cuda_check(cudaMemcpy(out.data() + at, arena.image_base, il, cudaMemcpyDeviceToHost), "read weights", JC_MAP);
+    return out;
+}
+
+void Model::finish_init() {
     const int tx = cfg.nx / cfg.patch, ty = cfg.ny / cfg.patch;
     const long long cells = (long long)cfg.nx * cfg.ny;
     state_len = (size_t)dims.C * cells;

@@ -37,14 +37,32 @@ TensorMap parse_safetensors(const uint8_t* p, size_t n);
 jc_config parse_config(const char* json, const TensorMap& t);
 
 // Device allocations owned by one object, freed with it.
+//
+// Weight image: between begin_image() and end_image(), upload() and
+// upload_bytes() append the arrays to one host image (256-byte aligned) and
+// return provisional addresses; end_image() makes one device allocation and
+// one host->device copy of the whole image and rebases the given pointer
+// slots (every array uploaded in between must have exactly one slot).
 struct DeviceArena {
     std::vector<void*> ptrs;
     void* alloc(size_t bytes);
     template <class T>
     T* alloc_n(size_t n) { return static_cast<T*>(alloc(n * sizeof(T))); }
     float* upload(const std::vector<float>& v);
+    const void* upload_bytes(const void* src, size_t bytes);
     void release(void* p);
     ~DeviceArena();
+
+    void begin_image();
+    // Returns the slots' offsets into the image.
+    std::vector<uint64_t> end_image(const std::vector<const void**>& slots);
+    std::vector<uint8_t> image;     // host image while building
+    void* image_base = nullptr;     // device image after end_image()
+    size_t image_len = 0;
+
+   private:
+    bool imaging_ = false;
+    size_t image_arrays_ = 0;
 };
 
 class BF16Path;  // tensor-core forward (bf16_path.cu)
@@ -84,7 +102,15 @@ struct DeviceWeights {
 class Model {
    public:
     Model(const uint8_t* st, size_t st_len, const char* config_json, int precision);
+    // From a pre-packed image written by pack(): one device allocation and
+    // one host->device copy of the weights, no conversion.
+    Model(const uint8_t* packed, size_t len);
     ~Model();
+
+    // The pre-packed checkpoint: header (config, precision, source hash,
+    // slot offsets, conv2 parameters) followed by the device weight image.
+    std::vector<uint8_t> pack() const;
+    uint64_t source_hash = 0;  // fnv1a-64 of the safetensors bytes and the config text
 
     jc_config cfg{};
     Dims dims{};
@@ -109,6 +135,8 @@ class Model {
     void forward_pack(const Pack& p, int mode, cudaStream_t s) const;
 
    private:
+    std::vector<uint64_t> slot_off_;  // weight slots' offsets into the device image
+    void finish_init();
     Workspace ws_;
     Pack pack_{};
     InstDev inst_{};
@@ -220,6 +248,12 @@ void server_destroy(jc_server* s);
 uint64_t server_submit(jc_server* s, const jc_request* r);
 void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* info, double timeout);
 void server_stats(jc_server* s, jc_server_stats* st);
+
+// fnv1a-64 of a safetensors image and its config text: the source identity a
+// pre-packed checkpoint records.
+uint64_t source_hash(const uint8_t* st, size_t st_len, const char* config_json);
+// Reads the source hash from a pre-packed image's header (no device work).
+uint64_t packed_source_hash(const uint8_t* packed, size_t len);
 
 // Evaluation path (evaluate.cu): the reference solver, the scores and the
 // evaluator behind jc_sw_*, jc_eval_score and jc_eval_*.

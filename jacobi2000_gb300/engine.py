@@ -119,6 +119,55 @@ class Model:
     def from_bytes(cls, safetensors: bytes, config_json: str, precision: int = FP32) -> "Model":
         return cls(safetensors, config_json, precision)
 
+    @classmethod
+    def from_packed(cls, packed: bytes) -> "Model":
+        """A model from a pre-packed checkpoint (jc_model_create_packed)."""
+        L = load_library()
+        _declare_pack(L)
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        _check(L.jc_model_create_packed(packed, len(packed), C.byref(h)))
+        self._h = h
+        self._L = L
+        c = JcConfig()
+        _check(L.jc_model_config(h, C.byref(c)))
+        self.config = c
+        self.precision = packed_precision(packed)
+        self.shape = (c.channels, c.ny, c.nx)
+        self.cells = c.nx * c.ny
+        return self
+
+    def pack(self) -> bytes:
+        """The pre-packed checkpoint of this model (jc_model_pack)."""
+        _declare_pack(self._L)
+        n = C.c_size_t()
+        _check(self._L.jc_model_pack(self._h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(self._L.jc_model_pack(self._h, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value]
+
+    @classmethod
+    def load_cached(cls, directory: str | Path, precision: int = FP32) -> "Model":
+        """Model.load through the pre-packed cache beside the checkpoint:
+        ``model.fp32.jcpack`` / ``model.bf16.jcpack`` is used when it records
+        the current model.safetensors and config.json, else rebuilt from them."""
+        d = Path(directory)
+        st = (d / "model.safetensors").read_bytes()
+        cj = (d / "config.json").read_text()
+        cache = d / f"model.{'bf16' if precision == BF16 else 'fp32'}.jcpack"
+        if cache.exists():
+            packed = cache.read_bytes()
+            try:
+                if packed_source_hash(packed) == source_hash(st, cj) and packed_precision(packed) == precision:
+                    return cls.from_packed(packed)
+            except JcError:
+                pass
+        m = cls(st, cj, precision)
+        tmp = cache.with_suffix(".tmp")
+        tmp.write_bytes(m.pack())
+        tmp.replace(cache)
+        return m
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._L.jc_model_destroy(self._h)
@@ -640,3 +689,46 @@ class RoundTrip:
             for f in ROUNDTRIP_FIELDS:
                 out[f][k] = getattr(rows[k], f)
         return out.reshape(nh, n)
+
+
+# ---- pre-packed checkpoints (jc_model_pack, jc_model_create_packed) ----------------
+
+EXPORTED += ["jc_model_pack", "jc_model_create_packed", "jc_source_hash", "jc_packed_source_hash"]
+
+
+def _declare_pack(L):
+    if getattr(L, "_pack_declared", False):
+        return
+    vp = C.c_void_p
+    L.jc_model_pack.argtypes = [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]
+    L.jc_model_pack.restype = C.c_int
+    L.jc_model_create_packed.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(vp)]
+    L.jc_model_create_packed.restype = C.c_int
+    L.jc_source_hash.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.POINTER(C.c_uint64)]
+    L.jc_source_hash.restype = C.c_int
+    L.jc_packed_source_hash.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_uint64)]
+    L.jc_packed_source_hash.restype = C.c_int
+    L._pack_declared = True
+
+
+def source_hash(safetensors: bytes, config_json: str) -> int:
+    L = load_library()
+    _declare_pack(L)
+    out = C.c_uint64()
+    _check(L.jc_source_hash(safetensors, len(safetensors), config_json.encode(), C.byref(out)))
+    return out.value
+
+
+def packed_source_hash(packed: bytes) -> int:
+    L = load_library()
+    _declare_pack(L)
+    out = C.c_uint64()
+    _check(L.jc_packed_source_hash(packed, len(packed), C.byref(out)))
+    return out.value
+
+
+def packed_precision(packed: bytes) -> int:
+    """The precision field of a pre-packed checkpoint's header (after the
+    8-byte magic and the u32 version)."""
+    packed_source_hash(packed)  # validates the header
+    return int.from_bytes(packed[12:16], "little")

@@ -156,3 +156,16 @@ def test_eval_drop_sampler_keeps_waves_off_the_walls():
         assert horizon_ticks(cfg, cx, cy) >= 50.0
     assert abs(float(cells_per_tick(cfg)) - np.sqrt(9.81) * 0.0903) < 1e-6
     assert draw_drops(cfg, 20, 0, 50.0) == (drops, skipped)
+
+
+def test_packed_checkpoint_header_is_checked_before_device_work(pt_tiny):
+    L = engine.load_library()
+    engine._declare_pack(L)
+    h = C.c_void_p()
+    for bad in (b"", b"JCPACK01", b"NOTAPACK" + bytes(64), b"JCPACK01" + (2).to_bytes(4, "little") + bytes(64)):
+        assert engine.STATUS[L.jc_model_create_packed(bad, len(bad), C.byref(h))] == "BAD_CHECKPOINT"
+    st, cj = pt_tiny["st_bytes"], pt_tiny["config"]
+    a = engine.source_hash(st, cj)
+    assert a == engine.source_hash(st, cj)
+    assert a != engine.source_hash(st[:-1] + bytes([st[-1] ^ 1]), cj)
+    assert a != engine.source_hash(st, cj + " ")
