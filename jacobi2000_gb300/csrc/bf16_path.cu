@@ -28,6 +28,7 @@
 #include <string>
 
 #include "bf16_path.hpp"
+#include "launch.hpp"
 #include "tc.cuh"
 
 namespace jc {
@@ -190,6 +191,7 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
                                                        const float* __restrict__ bm, const float* __restrict__ g,
                                                        const float* __restrict__ b, const InstDev* inst, int n_inst,
                                                        int R, float* __restrict__ x, bf16* __restrict__ ln) {
+    JC_PDL_ENTRY;
     extern __shared__ __align__(16) float esm[];
     constexpr int D = 32 * CPL;
     constexpr int P = 4, pd = 3 * P * P;  // 3 channels, patch 4 (checked when the path is built)
@@ -436,6 +438,7 @@ template <int HD>
 __global__ void __launch_bounds__(256) bf_attn_head_r1_kernel(Dims d, const bf16* __restrict__ qkv,
                                                               const InstDev* inst, int n_inst, int R,
                                                               bf16* __restrict__ out) {
+    JC_PDL_ENTRY;
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = gid / d.heads, h = gid - r * d.heads;
     if (r >= R) return;
@@ -476,6 +479,7 @@ __global__ void __launch_bounds__(256) bf_attn_head_r1_kernel(Dims d, const bf16
 template <int HD>
 __global__ void __launch_bounds__(256) bf_attn_head_kernel(Dims d, const bf16* __restrict__ qkv, const InstDev* inst,
                                                            int n_inst, int R, bf16* __restrict__ out) {
+    JC_PDL_ENTRY;
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = gid / d.heads, h = gid - r * d.heads;
     if (r >= R) return;
@@ -619,6 +623,7 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
         }
     }
     __syncthreads();
+    JC_PDL_ENTRY;
     if (y0 >= I.ty) return;  // the lower half of a tile that overhangs the grid (uniform per CTA)
     if (threadIdx.x == 0 && !failed) {
         tc::tensormap_acquire(mkv);
@@ -686,6 +691,7 @@ constexpr int kUpTokY = kConvTY / 4 + 1, kUpTokX = kConvTX / 4 + 1, kUpPitch = 3
 template <int HD, int C>
 __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst,
                                                           int n_inst, __half* __restrict__ zc) {
+    JC_PDL_ENTRY;
     static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh && HD + 4 <= kUpPitch, "zc layout");
     constexpr int P = 4;  // patch (the BF16 path is built for 4); (i + 1/2) / 4 is exact as a product
     __shared__ __align__(16) float win[kUpTokY * kUpTokX * kUpPitch];
@@ -951,6 +957,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
         for (int i = threadIdx.x; i < BN; i += blockDim.x) sbias[i] = ep.bias[nb * BN + i];
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     if (threadIdx.x == 0 && !failed) {
@@ -1152,6 +1159,7 @@ __global__ void __launch_bounds__(kMlpThreads, 2) tc_mlp_kernel(const __grid_con
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tO = tmem_base;
     const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
@@ -1321,6 +1329,7 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tO = tmem_base, tS = tmem_base + s_col;
     const uint32_t a0 = tc::smem_u32(sA), w1s = tc::smem_u32(sB1), w2s = tc::smem_u32(sB2), hs = tc::smem_u32(sH);
@@ -1502,6 +1511,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
@@ -1721,6 +1731,7 @@ __global__ void __launch_bounds__(kPLThreads, 1) tc_projln_persistent_kernel(
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     const size_t a_bytes = (size_t)D * 256, x_bytes = (size_t)D * 512;
@@ -1851,6 +1862,7 @@ __global__ void __launch_bounds__(kQKVPThreads, 1) tc_qkv_persistent_kernel(
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     if (warp == 0) {
@@ -2010,6 +2022,7 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     const uint32_t wtap = (uint32_t)C * BN * 2;  // bytes of one tap's B block
@@ -2172,6 +2185,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
     if (warp == 0) tc::tmem_alloc(&tmem_base, 2 * BN);
     tc::tc_fence_before();
     __syncthreads();
+    JC_PDL_ENTRY;
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
     // tile -> (instance, origin)
@@ -2483,9 +2497,9 @@ static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst
         const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
         const dim3 grid((unsigned)p->n_ttiles, 2);
         if (d.D / d.heads == 32)
-            bf_attn_tile_kernel<32><<<grid, 64 * d.heads, attn_tile_smem(d), s>>>(d, maps, 4, 5, inst, n, attn, p->err);
+            cuda_check(launch_pdl(bf_attn_tile_kernel<32>, grid, 64 * d.heads, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst, n, attn, p->err), "launch");
         else
-            bf_attn_tile_kernel<64><<<grid, 64 * d.heads, attn_tile_smem(d), s>>>(d, maps, 4, 5, inst, n, attn, p->err);
+            cuda_check(launch_pdl(bf_attn_tile_kernel<64>, grid, 64 * d.heads, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst, n, attn, p->err), "launch");
         return;
     }
     const bool r1 = d.mask_kind == 1 && d.radius == 1;
@@ -2493,8 +2507,8 @@ static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst
     const unsigned blocks = (unsigned)(((long long)R * d.heads + threads - 1) / threads);
 #define JC_ATTN_HEAD(H)                                                                          \
     if (hd == H) {                                                                               \
-        if (r1) bf_attn_head_r1_kernel<H><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn); \
-        else bf_attn_head_kernel<H><<<blocks, threads, 0, s>>>(d, qkv, inst, n, R, attn);       \
+        if (r1) cuda_check(launch_pdl(bf_attn_head_r1_kernel<H>, blocks, threads, 0, s, 1u, d, qkv, inst, n, R, attn), "launch"); \
+        else cuda_check(launch_pdl(bf_attn_head_kernel<H>, blocks, threads, 0, s, 1u, d, qkv, inst, n, R, attn), "launch");       \
         return;                                                                                  \
     }
     JC_ATTN_HEAD(8)
@@ -2547,23 +2561,23 @@ void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tunin
     const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
     const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
     if (tu.form == 0) {
-        tc_mlp_serial_kernel<<<(unsigned)((R + 127) / 128), kMlpSerialThreads, mlp_serial_smem(D, tu.nc), s>>>(
+        cuda_check(launch_pdl(tc_mlp_serial_kernel, (unsigned)((R + 127) / 128), kMlpSerialThreads, mlp_serial_smem(D, tu.nc), s, 1u, 
             m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, R, p.x, ng, nbeta,
-            reinterpret_cast<bf16*>(p.bt[0]), p.err);
+            reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
         return;
     }
     if (tu.form == 2) {
         const unsigned grid = (unsigned)std::min((R + 127) / 128, n_sms_);
         const CUtensorMap m_x = store_map(p.x, D, R, D, true);
-        tc_mlp_persistent_kernel<<<grid, kMlpPThreads, MlpPSmem(D, d.F, tu.nc, tu.ns).total, s>>>(
+        cuda_check(launch_pdl(tc_mlp_persistent_kernel, grid, kMlpPThreads, MlpPSmem(D, d.F, tu.nc, tu.ns).total, s, 1u, 
             m_ln, m_x, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
-            reinterpret_cast<bf16*>(p.bt[0]), p.err);
+            reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
         return;
     }
     const size_t smem = MlpSmem(D, d.F, tu.nc, tu.ns).total;
-    tc_mlp_kernel<<<(unsigned)((R + 127) / 128), kMlpThreads, smem, s>>>(
+    cuda_check(launch_pdl(tc_mlp_kernel, (unsigned)((R + 127) / 128), kMlpThreads, smem, s, 1u, 
         m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
-        reinterpret_cast<bf16*>(p.bt[0]), p.err);
+        reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
 }
 
 // Times `launch` with CUDA events: one warm-up, then `reps` launches.
@@ -2741,8 +2755,9 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         };
 #define JC_EMBED(CPL)                                                                                            \
     case CPL:                                                                                                    \
-        bf_embed_kernel<CPL><<<grid_for(bf_embed_kernel<CPL>), 256, smem, s>>>(                                  \
-            d, w.embed_w, w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln);     \
+        cuda_check(launch_pdl(bf_embed_kernel<CPL>, grid_for(bf_embed_kernel<CPL>), 256, smem, s, 1u, d, w.embed_w, \
+                              w.embed_b, w.meta_w, w.meta_b, w.blk[0].n1g, w.blk[0].n1b, p.inst, n, R, p.x, ln),     \
+                   "launch");                                                                                    \
         break;
         switch (D / 32) {
             JC_EMBED(1) JC_EMBED(2) JC_EMBED(3) JC_EMBED(4) JC_EMBED(5) JC_EMBED(6) JC_EMBED(7) JC_EMBED(8)
@@ -2758,13 +2773,13 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             const int BN = bn_qkv;
             if (D <= 128) {
                 const unsigned grid = (unsigned)std::min((int)gm, n_sms_);
-                tc_qkv_persistent_kernel<<<grid, kQKVPThreads, QKVPSmem(D, BN).total, s>>>(m_ln, m_qkv_out, wqkv[l],
-                                                                                         B.bqkv, D, BN, R, p.err);
+                cuda_check(launch_pdl(tc_qkv_persistent_kernel, grid, kQKVPThreads, QKVPSmem(D, BN).total, s, 1u, m_ln, m_qkv_out, wqkv[l],
+                                                                                         B.bqkv, D, BN, R, p.err), "launch");
             } else {
                 GemmEpi ep{B.bqkv, qkv, nullptr, nullptr, nullptr, nullptr, 3 * D};
                 const size_t smem = std::max((size_t)D * 256 + (size_t)D * BN * 2, (size_t)((BN + 63) / 64) * 16384);
-                tc_gemm_kernel<EPI_BF16><<<dim3(gm, 3 * D / BN), 128, smem, s>>>(m_ln, m_qkv_out, wqkv[l], D, BN, R, ep,
-                                                                             p.err);
+                cuda_check(launch_pdl(tc_gemm_kernel<EPI_BF16>, dim3(gm, 3 * D / BN), 128, smem, s, 1u, m_ln, m_qkv_out, wqkv[l], D, BN, R, ep,
+                                                                             p.err), "launch");
             }
             check_launch("tc_qkv");
         }
@@ -2777,13 +2792,13 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             KScope k("tc_proj_ln", s);
             if (D <= kLnMaxD) {
                 const unsigned grid = (unsigned)std::min((int)gm, n_sms_);
-                tc_projln_persistent_kernel<<<grid, kPLThreads, PLSmem(D).total, s>>>(m_attn, m_x, wp[l], B.bp, B.n2g,
-                                                                                    B.n2b, ln, D, R, p.err);
+                cuda_check(launch_pdl(tc_projln_persistent_kernel, grid, kPLThreads, PLSmem(D).total, s, 1u, m_attn, m_x, wp[l], B.bp, B.n2g,
+                                                                                    B.n2b, ln, D, R, p.err), "launch");
             } else {
                 GemmEpi ep{B.bp, ln, nullptr, p.x, B.n2g, B.n2b, D};
                 const size_t smem = std::max((size_t)D * 256 + (size_t)D * D * 2, (size_t)128 * D * 4);
-                tc_gemm_kernel<EPI_RESID_LN><<<dim3(gm, 1), 128, smem, s>>>(m_attn, m_attn, wp[l], D, D, R, ep,
-                                                                            p.err);
+                cuda_check(launch_pdl(tc_gemm_kernel<EPI_RESID_LN>, dim3(gm, 1), 128, smem, s, 1u, m_attn, m_attn, wp[l], D, D, R, ep,
+                                                                            p.err), "launch");
             }
             check_launch("tc_proj_ln");
         }
@@ -2797,28 +2812,28 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
         KScope k("tc_token_mix", s);
         const int BN = bn_tm;
         const int NS = conv3_smem(D, BN, 9) <= 100 * 1024 ? 9 : 2;
-        tc_conv3_kernel<CONV_TOKMIX><<<dim3(p.n_ttiles, D / BN), 128, conv3_launch_smem(D, BN, NS, 2), s>>>(
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), 0, 2, wtm, w.tm_b, D, BN, NS, p.inst, n, p.err);
+        cuda_check(launch_pdl(tc_conv3_kernel<CONV_TOKMIX>, dim3(p.n_ttiles, D / BN), 128, conv3_launch_smem(D, BN, NS, 2), s, 1u, 
+            reinterpret_cast<const CUtensorMap*>(p.tmaps), 0, 2, wtm, w.tm_b, D, BN, NS, p.inst, n, p.err), "launch");
         check_launch("tc_token_mix");
     }
     {
         KScope k("tc_to_cells", s);
         GemmEpi ep{w.tc_b, nullptr, p.z0, nullptr, nullptr, nullptr, d.HD};
         const size_t smem = std::max((size_t)D * 256 + (size_t)D * d.HD * 2, (size_t)((d.HD + 31) / 32) * 16384);
-        tc_gemm_kernel<EPI_F32><<<dim3(gm, 1), 128, smem, s>>>(m_t1, m_z0_out, wtc, D, d.HD, R, ep, p.err);
+        cuda_check(launch_pdl(tc_gemm_kernel<EPI_F32>, dim3(gm, 1), 128, smem, s, 1u, m_t1, m_z0_out, wtc, D, d.HD, R, ep, p.err), "launch");
         check_launch("tc_to_cells");
     }
     {
         KScope k("bf_upsample", s);
-        bf_upsample_kernel<32, 3><<<(unsigned)p.n_ctiles, 128, 0, s>>>(d, p.z0, p.inst, n,
-                                                                       reinterpret_cast<__half*>(p.bc[0]));
+        cuda_check(launch_pdl(bf_upsample_kernel<32, 3>, (unsigned)p.n_ctiles, 128, 0, s, 1u, d, p.z0, p.inst, n,
+                                                                       reinterpret_cast<__half*>(p.bc[0])), "launch");
         check_launch("bf_upsample");
     }
     {
         KScope k("tc_conv1", s);
         const unsigned grid = (unsigned)std::min(p.n_ctiles, 2 * n_sms_);
-        tc_conv1_persistent_kernel<<<grid, kC1PThreads, C1PSmem(kZcCh, d.HD).total, s>>>(
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n, p.err);
+        cuda_check(launch_pdl(tc_conv1_persistent_kernel, grid, kC1PThreads, C1PSmem(kZcCh, d.HD).total, s, 1u, 
+            reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n, p.err), "launch");
         check_launch("tc_conv1");
     }
     conv2_step(d, c1, w, p, mode, "bf_conv2_step", s);

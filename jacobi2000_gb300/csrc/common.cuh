@@ -107,6 +107,19 @@ __device__ __forceinline__ void cp_async_wait_group() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Programmatic dependent launch. A kernel launched with programmatic stream
+// serialization may start (be scheduled, set up shared memory, tensor memory
+// and barriers) while the previous kernel in the stream is still running.
+// JC_PDL_ENTRY lets the next kernel start early, then waits until the previous
+// kernel has completed and its writes are visible; every kernel executes it
+// before its first access to memory that other kernels write or read.
+// Without the launch attribute both instructions are no-ops.
+#define JC_PDL_ENTRY                                                      \
+    do {                                                                  \
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");  \
+        asm volatile("griddepcontrol.wait;" ::: "memory");               \
+    } while (0)
+
 // Neumaier compensated accumulator in f64.
 struct Neu {
     double s, c;

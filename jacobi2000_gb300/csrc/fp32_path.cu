@@ -12,6 +12,7 @@
 
 #include "engine.hpp"
 #include "fp32_kernels.cuh"
+#include "launch.hpp"
 
 namespace cg = cooperative_groups;
 
@@ -264,6 +265,7 @@ __global__ void __launch_bounds__(kConv2Threads, 8) conv2_step_kernel(const floa
                                                                       const __grid_constant__ Conv2Params cw,
                                                                       const InstDev* inst, int n_inst, int mode) {
     static_assert(C == 3 && HD == 32, "conv2 is built for 3 channels and a cell-head width of 32");
+    JC_PDL_ENTRY;
     constexpr int S = kConv2S, NG = HD / 8;
     extern __shared__ __align__(16) float c2smem[];
     int lo = 0, hi = n_inst - 1;
@@ -462,6 +464,7 @@ __device__ void cluster_total(cg::cluster_group& cluster, double* mine, int nv, 
 
 __global__ void __launch_bounds__(kProjThreads)
 projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int cap, int seg_cap) {
+    JC_PDL_ENTRY;
     // [3][cap] f32: this CTA's cells when they fit; then 3 x (1 + 2 seg_cap)
     // f64: per pass, the segment count and this CTA's segment totals
     extern __shared__ __align__(16) float sst[];
@@ -660,8 +663,9 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
         attr = true;
     }
     if (!w.c2p) throw std::runtime_error("conv2 weights missing");
-    f32k::conv2_step_kernel<3, 32><<<p.n_tiles, f32k::kConv2Threads, f32k::kConv2Smem, s>>>(c1, *w.c2p, p.inst,
-                                                                                          p.n_inst, mode);
+    const cudaError_t e = launch_pdl(f32k::conv2_step_kernel<3, 32>, dim3(p.n_tiles), dim3(f32k::kConv2Threads),
+                                     f32k::kConv2Smem, s, 1u, c1, *w.c2p, (const InstDev*)p.inst, p.n_inst, mode);
+    if (e != cudaSuccess) throw std::runtime_error(std::string(name) + ": " + cudaGetErrorString(e));
     check_launch(name);
 }
 
@@ -684,20 +688,8 @@ void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
     // staged in shared memory when a CTA's cells fit, else passes run in place
     const int cap = seg_cap * f32k::kProjSeg <= f32k::kProjSmemCells ? (int)(seg_cap * f32k::kProjSeg) : 1;
     const size_t smem = (size_t)3 * cap * 4 + (size_t)3 * (1 + 2 * seg_cap) * 8;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(p.n_inst * cs));
-    cfg.blockDim = dim3(f32k::kProjThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute cl[1];
-    cl[0].id = cudaLaunchAttributeClusterDimension;
-    cl[0].val.clusterDim.x = (unsigned)cs;
-    cl[0].val.clusterDim.y = 1;
-    cl[0].val.clusterDim.z = 1;
-    cfg.attrs = cl;
-    cfg.numAttrs = 1;
-    cuda_check_attr(
-        cudaLaunchKernelEx(&cfg, f32k::projection_kernel, d, (const InstDev*)p.inst, p.proj, init, cap, (int)seg_cap));
+    cuda_check_attr(launch_pdl(f32k::projection_kernel, dim3((unsigned)(p.n_inst * cs)), dim3(f32k::kProjThreads), smem,
+                               s, (unsigned)cs, d, (const InstDev*)p.inst, p.proj, init, cap, (int)seg_cap));
     check_launch("projection");
 }
 
