@@ -831,6 +831,17 @@ __device__ __forceinline__ float sqdev4(float4 v, float m) {
 __device__ __forceinline__ float ln1(float v, float m, float rstd, float g, float b) {
     return __fmaf_rn(__fmul_rn(__fsub_rn(v, m), rstd), g, b);
 }
+// warp_sum of N independent values at once: the butterfly steps of all N are
+// interleaved, so their shuffle latencies overlap; each value is added in
+// warp_sum's order and gets warp_sum's bits.
+template <int N>
+__device__ __forceinline__ void warp_sum_n(float (&v)[N]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < N; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
 // The 32 lane partials in the order warp_sum adds them.
 __device__ __forceinline__ float tree32(float* a) {
 #pragma unroll
@@ -844,7 +855,8 @@ __device__ __forceinline__ float tree32(float* a) {
 // row r at q ^ slot_swz(r, D)); x and ln are read and written coalesced, G
 // rows in flight per warp. Rows [0, nrows) of the tile (a multiple of G),
 // tile row r -> global row m0 + r. SPL = slots per lane (1: D <= 128, 2: 256).
-template <int SPL, bool FULL>  // FULL: every lane owns SPL slots (D = 128 SPL)
+// PRE: load every row group's residual rows up front (four groups at most).
+template <int SPL, bool FULL, bool PRE = false>  // FULL: every lane owns SPL slots (D = 128 SPL)
 __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
                                 float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
                                 bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
@@ -861,7 +873,28 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
         gg[j] = reinterpret_cast<const float4*>(g)[q];
         be[j] = reinterpret_cast<const float4*>(b)[q];
     }
-    for (int r0 = warp * G; r0 < nrows; r0 += nwarps * G) {
+    // at most four row groups per warp (D <= 128): every group's residual
+    // rows are loaded up front, so their latencies overlap instead of
+    // adding up group after group
+    constexpr int PF = 4;
+    float4 xpre[SPL == 1 && PRE ? PF : 1][G];
+    const bool prefetched = PRE && SPL == 1 && nrows <= PF * nwarps * G;
+    if (SPL == 1 && prefetched) {
+#pragma unroll
+        for (int i = 0; i < PF; i++) {
+            const int r0 = warp * G + i * nwarps * G;
+#pragma unroll
+            for (int k = 0; k < G; k++) {
+                const int row = m0 + r0 + k;
+                const int q = on(0) ? lane : 0;
+                xpre[SPL == 1 && PRE ? i : 0][k] = r0 < nrows && row < R
+                                                ? reinterpret_cast<const float4*>(x + (size_t)row * D)[q]
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+    }
+    int grp = 0;
+    for (int r0 = warp * G; r0 < nrows; r0 += nwarps * G, grp++) {
         float4 a[G][SPL], xv[G][SPL];
 #pragma unroll
         for (int k = 0; k < G; k++) {
@@ -870,45 +903,70 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
             for (int j = 0; j < SPL; j++) {
                 const int q = on(j) ? lane + 32 * j : 0;
                 a[k][j] = reinterpret_cast<const float4*>(tile + (size_t)r * D)[q ^ (r & swz)];
-                xv[k][j] = row < R ? reinterpret_cast<const float4*>(x + (size_t)row * D)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+                if (SPL == 1 && prefetched) {
+                    float4 t = xpre[0][k];
+#pragma unroll
+                    for (int i = 1; i < PF; i++)
+                        if (grp == i) t = xpre[SPL == 1 && PRE ? i : 0][k];
+                    xv[k][j] = t;
+                } else {
+                    xv[k][j] = row < R ? reinterpret_cast<const float4*>(x + (size_t)row * D)[q]
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             }
         }
+        // the G rows' reductions run interleaved (warp_sum_n): the same
+        // order and bits per row as one warp_sum after another
+        float4 v[G][SPL];
+        float mean[G], q2[G];
 #pragma unroll
         for (int k = 0; k < G; k++) {
-            const int row = m0 + r0 + k;
-            if (row >= R) break;
-            float4 v[SPL];
             float s = 0.f;
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
-                v[j] = resid4(xv[k][j], a[k][j], bb[j]);
-                if (on(j)) s = __fadd_rn(s, sum4(v[j]));
+                v[k][j] = resid4(xv[k][j], a[k][j], bb[j]);
+                if (on(j)) s = __fadd_rn(s, sum4(v[k][j]));
             }
-            const float mean = warp_sum(s) / (float)D;
-            float q2 = 0.f;
+            mean[k] = s;
+        }
+        warp_sum_n(mean);
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            mean[k] = mean[k] / (float)D;
+            float t = 0.f;
 #pragma unroll
             for (int j = 0; j < SPL; j++)
-                if (on(j)) q2 = __fadd_rn(q2, sqdev4(v[j], mean));
-            const float rstd = 1.0f / sqrtf(warp_sum(q2) / (float)D + 1e-5f);
+                if (on(j)) t = __fadd_rn(t, sqdev4(v[k][j], mean[k]));
+            q2[k] = t;
+        }
+        warp_sum_n(q2);
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const int row = m0 + r0 + k;
+            if (row >= R) break;  // warp-uniform
+            const float rstd = 1.0f / sqrtf(q2[k] / (float)D + 1e-5f);
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
                 if (!on(j)) continue;
                 const int q = lane + 32 * j;
-                reinterpret_cast<float4*>(x + (size_t)row * D)[q] = v[j];
-                float o[4] = {ln1(v[j].x, mean, rstd, gg[j].x, be[j].x), ln1(v[j].y, mean, rstd, gg[j].y, be[j].y),
-                              ln1(v[j].z, mean, rstd, gg[j].z, be[j].z), ln1(v[j].w, mean, rstd, gg[j].w, be[j].w)};
+                reinterpret_cast<float4*>(x + (size_t)row * D)[q] = v[k][j];
+                float o[4] = {ln1(v[k][j].x, mean[k], rstd, gg[j].x, be[j].x),
+                              ln1(v[k][j].y, mean[k], rstd, gg[j].y, be[j].y),
+                              ln1(v[k][j].z, mean[k], rstd, gg[j].z, be[j].z),
+                              ln1(v[k][j].w, mean[k], rstd, gg[j].w, be[j].w)};
                 BfVec<4>::store(ln + (size_t)row * D + 4 * q, o);
             }
         }
     }
 }
 
+template <bool PRE = false>
 __device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
                                   const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128) {
     if (D == 256) rows_resid_ln_t<2, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
-    else if (D == 128) rows_resid_ln_t<1, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else if (D == 128) rows_resid_ln_t<1, true, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
     else if (D > 128) rows_resid_ln_t<2, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
-    else rows_resid_ln_t<1, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else rows_resid_ln_t<1, false, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
 }
 
 enum { EPI_BF16 = 0, EPI_F32 = 1, EPI_RESID_LN = 2 };
@@ -1393,7 +1451,7 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
         float* tile = reinterpret_cast<float*>(smem);
         stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
         __syncthreads();
-        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpSerialThreads / 32);
+        rows_resid_ln_any<true>(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpSerialThreads / 32);
     }
     tc::tc_fence_before();
     __syncthreads();
