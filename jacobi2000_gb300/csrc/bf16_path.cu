@@ -1101,10 +1101,15 @@ __device__ __forceinline__ float4* xrow_chunk(uint8_t* sX, int r, int q) {
     return reinterpret_cast<float4*>(sX + (size_t)(q >> 3) * 16384 + (size_t)r * 128 + (((q & 7) ^ (r & 7)) << 4));
 }
 
-__device__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t* sX, const float* sbias, const float* sg,
-                             const float* sb, uint8_t* sLn, bf16* lnrow) {
+// DT > 0: the width as a compile-time constant (every loop unrolled, so the
+// shared-memory reads of a pass are all in flight at once); DT = 0: D.
+template <int DT>
+__device__ void row_resid_ln_t(uint32_t ta, int r, int D_, uint8_t* sX, const float* sbias, const float* sg,
+                               const float* sb, uint8_t* sLn, bf16* lnrow) {
+    const int D = DT > 0 ? DT : D_;
     // D <= 128: slot q is lane q's only slot, so lane partial q = 0 + sum4
     const int nq = D / 4;
+#pragma unroll
     for (int c = 0; c < D; c += 16) {
         float a[16];
         tc::tmem_ld16(ta + c, a);
@@ -1123,6 +1128,7 @@ __device__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t* sX, const float
 #pragma unroll
     for (int l = 0; l < 32; l++) part[l] = l < nq ? __fadd_rn(0.f, sqdev4(*xrow_chunk(sX, r, l), mean)) : 0.f;
     const float rstd = 1.0f / sqrtf(tree32(part) / (float)D + 1e-5f);
+#pragma unroll
     for (int c = 0; c < D; c += 8) {
         const float4 v0 = *xrow_chunk(sX, r, c >> 2), v1 = *xrow_chunk(sX, r, (c >> 2) + 1);
         const float in[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
@@ -1136,6 +1142,12 @@ __device__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t* sX, const float
             BfVec<8>::store(lnrow + c, o);
         }
     }
+}
+
+__device__ __forceinline__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t* sX, const float* sbias,
+                                             const float* sg, const float* sb, uint8_t* sLn, bf16* lnrow) {
+    if (D == 128) row_resid_ln_t<128>(ta, r, D, sX, sbias, sg, sb, sLn, lnrow);
+    else row_resid_ln_t<0>(ta, r, D, sX, sbias, sg, sb, sLn, lnrow);
 }
 
 constexpr int kLnMaxD = 128;  // widest row the row-per-thread LayerNorm serves
@@ -1705,7 +1717,7 @@ __global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
             if (!all_of(ready, 1, 128)) break;  // the four epilogue warps meet at barrier 1 below
             tc::tc_fence_after();
             const int row = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + r;
-            row_resid_ln(lane_addr(tmem + (uint32_t)(it & 1) * D), r, D, sX, sb2, sgam, sbet, nullptr,
+            row_resid_ln_t<0>(lane_addr(tmem + (uint32_t)(it & 1) * D), r, D, sX, sb2, sgam, sbet, nullptr,
                          row < R ? ln + (size_t)row * D : nullptr);
             tc::tc_fence_before();
             tc::mbar_arrive(&o_empty[it & 1]);
