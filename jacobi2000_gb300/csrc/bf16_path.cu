@@ -1984,21 +1984,26 @@ __global__ void __launch_bounds__(kQKVPThreads, 1) tc_qkv_persistent_kernel(
             asm volatile("bar.sync 1, 128;" ::: "memory");
             uint8_t* st = sStage + (size_t)(g & 1) * st_bytes;
             const uint32_t ta = lane_addr(tmem + (uint32_t)(g & 1) * BN);
-            for (int c = 0; c < BN; c += 16) {
-                float a[16];
-                tc::tmem_ld16(ta + c, a);
+            // 32 columns per TMEM round trip (BN is a multiple of 32)
+            for (int c = 0; c < BN; c += 32) {
+                float a[32];
+                tc::tmem_ld32(ta + c, a);
 #pragma unroll
-                for (int i = 0; i < 16; i += 4) {
+                for (int i = 0; i < 32; i += 4) {
                     const float4 bv = *reinterpret_cast<const float4*>(sbias + nb * BN + c + i);
                     a[i] += bv.x;
                     a[i + 1] += bv.y;
                     a[i + 2] += bv.z;
                     a[i + 3] += bv.w;
                 }
-                uint8_t* box = st + (size_t)(c / 64) * 16384 + (size_t)r * 128;
-                const int j0 = (c % 64) / 8;
-                BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
-                BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int cc = c + 16 * h;
+                    uint8_t* box = st + (size_t)(cc / 64) * 16384 + (size_t)r * 128;
+                    const int j0 = (cc % 64) / 8;
+                    BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a + 16 * h);
+                    BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 16 * h + 8);
+                }
             }
             tc::tc_fence_before();
             tc::mbar_arrive(&acc_empty[g & 1]);
