@@ -446,18 +446,32 @@ constexpr int kProjSeg = 4096;
 // Instance totals of nv (<= 2) values from this CTA's per-segment totals
 // mine[k][v] (k < nk): thread 0 reads every rank's segments through
 // distributed shared memory and adds them in segment order.
-__device__ void cluster_total(cg::cluster_group& cluster, double* mine, int nv, double* out) {
+// The cluster's totals of one pass: every CTA's segment totals, in segment
+// order. One lane per peer copies that peer's totals into `gather` (the
+// remote reads of all peers overlap), then thread 0 adds them in order.
+__device__ void cluster_total(cg::cluster_group& cluster, double* mine, int nv, double* out, double* gather,
+                              int stride) {
     const int cs = (int)cluster.num_blocks();
     cluster.sync();
-    if (threadIdx.x == 0) {
-        double t[2] = {0.0, 0.0};
-        for (int r = 0; r < cs; r++) {
+    if (threadIdx.x < 32) {
+        for (int r = threadIdx.x; r < cs; r += 32) {
             const double* peer = cs == 1 ? mine : cluster.map_shared_rank(mine, r);
             const int nk = (int)peer[0];  // slot 0 holds the segment count
-            for (int k = 0; k < nk; k++)
-                for (int v = 0; v < nv; v++) t[v] += peer[1 + 2 * k + v];
+            double* dst = gather + (size_t)r * stride;
+            dst[0] = (double)nk;
+            for (int i = 0; i < 2 * nk; i++) dst[1 + i] = peer[1 + i];
         }
-        for (int v = 0; v < nv; v++) out[v] = t[v];
+        __syncwarp();
+        if (threadIdx.x == 0) {
+            double t[2] = {0.0, 0.0};
+            for (int r = 0; r < cs; r++) {
+                const double* g = gather + (size_t)r * stride;
+                const int nk = (int)g[0];
+                for (int k = 0; k < nk; k++)
+                    for (int v = 0; v < nv; v++) t[v] += g[1 + 2 * k + v];
+            }
+            for (int v = 0; v < nv; v++) out[v] = t[v];
+        }
     }
     __syncthreads();
 }
@@ -526,7 +540,7 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
             }
         }
         __syncthreads();
-        cluster_total(cluster, mine, nv, tot);
+        cluster_total(cluster, mine, nv, tot, segs + 3 * (size_t)(1 + 2 * seg_cap), 1 + 2 * seg_cap);
     };
     const double prev = S.energy;
     // pass 1: mass
@@ -687,7 +701,7 @@ void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
     const long long seg_cap = (nseg + cs - 1) / cs;
     // staged in shared memory when a CTA's cells fit, else passes run in place
     const int cap = seg_cap * f32k::kProjSeg <= f32k::kProjSmemCells ? (int)(seg_cap * f32k::kProjSeg) : 1;
-    const size_t smem = (size_t)3 * cap * 4 + (size_t)3 * (1 + 2 * seg_cap) * 8;
+    const size_t smem = (size_t)3 * cap * 4 + (size_t)(3 + cs) * (1 + 2 * seg_cap) * 8;
     cuda_check_attr(launch_pdl(f32k::projection_kernel, dim3((unsigned)(p.n_inst * cs)), dim3(f32k::kProjThreads), smem,
                                s, (unsigned)cs, d, (const InstDev*)p.inst, p.proj, init, cap, (int)seg_cap));
     check_launch("projection");
