@@ -1410,7 +1410,7 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     uint8_t* sB2 = sB1 + (size_t)D * NC * 2;      // [NC/8][D][8]
     uint8_t* sH = sB2 + (size_t)D * NC * 2;       // [NC/8][128][8]
     __shared__ __align__(16) float sb1[1024];
-    __shared__ uint64_t bar_a, bar_w, bar_s, bar_o;
+    __shared__ uint64_t bar_a, bar_w1, bar_w2, bar_s, bar_o;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1420,7 +1420,8 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     const uint32_t s_col = D <= 128 ? 128 : 256;  // O in [0, D), S in [s_col, s_col + NC)
     if (threadIdx.x == 0) {
         tc::mbar_init(&bar_a, 1);
-        tc::mbar_init(&bar_w, 1);
+        tc::mbar_init(&bar_w1, 1);
+        tc::mbar_init(&bar_w2, 1);
         tc::mbar_init(&bar_s, 1);
         tc::mbar_init(&bar_o, 1);
         tc::fence_barrier_init();
@@ -1438,32 +1439,50 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     tc::tc_fence_after();
     const uint32_t tO = tmem_base, tS = tmem_base + s_col;
     const uint32_t a0 = tc::smem_u32(sA), w1s = tc::smem_u32(sB1), w2s = tc::smem_u32(sB2), hs = tc::smem_u32(sH);
+    const int nchunks = F / NC;
+    const uint32_t wbytes = (uint32_t)D * NC * 2;
+    auto issue_s = [&]() {  // S = A @ W1_chunk into tS
+        const uint32_t idesc = tc::idesc_bf16(128, NC);
+        for (int k = 0; k < D / 16; k++)
+            tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(w1s + k * 2 * NC * 16, NC * 16, 128), idesc,
+                         k > 0 ? 1u : 0u);
+        tc::mma_commit(&bar_s);
+    };
+    // Chunk j's critical path is GELU_j then S_{j+1}: W1_{j+1} is loaded as
+    // soon as S_j has read W1_j, W2_j once O_{j-1} has read W2_{j-1}, and
+    // S_{j+1} is issued right after GELU_j, ahead of O_j. The MMAs and their
+    // accumulation order are those of one chunk after another.
     if (threadIdx.x == 0 && !failed) {
         tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
         for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &bar_a);
+        tc::mbar_expect_tx(&bar_w1, wbytes);
+        tc::bulk_load(sB1, W1, wbytes, &bar_w1);
+        tc::mbar_expect_tx(&bar_w2, wbytes);
+        tc::bulk_load(sB2, W2, wbytes, &bar_w2);
+        if (tc::mbar_wait(&bar_a, 0, err, &failed) && tc::mbar_wait(&bar_w1, 0, err, &failed)) {
+            tc::tc_fence_after();
+            issue_s();
+        }
     }
-    const int nchunks = F / NC;
-    const uint32_t wbytes = (uint32_t)D * NC * 2;
+    __syncwarp();
     bool ok = true;
     for (int j = 0; j < nchunks && ok; j++) {
-        if (threadIdx.x == 0 && !failed) {
-            tc::mbar_expect_tx(&bar_w, 2 * wbytes);
-            tc::bulk_load(sB1, W1 + (size_t)j * D * NC, wbytes, &bar_w);
-            tc::bulk_load(sB2, W2 + (size_t)j * D * NC, wbytes, &bar_w);
-            bool good = (j > 0 || tc::mbar_wait(&bar_a, 0, err, &failed)) && tc::mbar_wait(&bar_w, j & 1, err, &failed);
-            if (good) {
-                tc::tc_fence_after();
-                const uint32_t idesc = tc::idesc_bf16(128, NC);
-                for (int k = 0; k < D / 16; k++)
-                    tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(w1s + k * 2 * NC * 16, NC * 16, 128),
-                                 idesc, k > 0 ? 1u : 0u);
-                tc::mma_commit(&bar_s);
-            }
-        }
-        __syncwarp();
         ok = __syncthreads_and(tc::mbar_wait(&bar_s, j & 1, err, &failed) ? 1 : 0) != 0;
         tc::tc_fence_after();
         if (!ok) break;
+        if (threadIdx.x == 0 && !failed && j + 1 < nchunks) {  // S_j has read W1_j
+            tc::mbar_expect_tx(&bar_w1, wbytes);
+            tc::bulk_load(sB1, W1 + (size_t)(j + 1) * D * NC, wbytes, &bar_w1);
+        }
+        if (j > 0) {  // O_{j-1} has read h_{j-1} and W2_{j-1}
+            ok = __syncthreads_and(tc::mbar_wait(&bar_o, (j - 1) & 1, err, &failed) ? 1 : 0) != 0;
+            tc::tc_fence_after();
+            if (!ok) break;
+            if (threadIdx.x == 0 && !failed) {
+                tc::mbar_expect_tx(&bar_w2, wbytes);
+                tc::bulk_load(sB2, W2 + (size_t)j * D * NC, wbytes, &bar_w2);
+            }
+        }
         {
             // h = gelu(S + b1) -> bf16 -> shared memory in the core-matrix layout
             const int r = quarter * 32 + lane;
@@ -1483,14 +1502,24 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
         __syncthreads();
         tc::tc_fence_after();
         if (threadIdx.x == 0 && !failed) {
-            const uint32_t idesc = tc::idesc_bf16(128, D);
-            for (int k = 0; k < NC / 16; k++)
-                tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(w2s + k * 2 * D * 16, D * 16, 128), idesc,
-                             (j > 0 || k > 0) ? 1u : 0u);
-            tc::mma_commit(&bar_o);
+            // S_{j+1} first (tS was read by every GELU thread), then O_j
+            if (j + 1 < nchunks && tc::mbar_wait(&bar_w1, (j + 1) & 1, err, &failed)) {
+                tc::tc_fence_after();
+                issue_s();
+            }
+            if (!failed && tc::mbar_wait(&bar_w2, j & 1, err, &failed)) {
+                tc::tc_fence_after();
+                const uint32_t idesc = tc::idesc_bf16(128, D);
+                for (int k = 0; k < NC / 16; k++)
+                    tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(w2s + k * 2 * D * 16, D * 16, 128),
+                                 idesc, (j > 0 || k > 0) ? 1u : 0u);
+                tc::mma_commit(&bar_o);
+            }
         }
         __syncwarp();
-        ok = __syncthreads_and(tc::mbar_wait(&bar_o, j & 1, err, &failed) ? 1 : 0) != 0;
+    }
+    if (ok) {  // the last O
+        ok = __syncthreads_and(tc::mbar_wait(&bar_o, (nchunks - 1) & 1, err, &failed) ? 1 : 0) != 0;
         tc::tc_fence_after();
     }
     if (ok) {
