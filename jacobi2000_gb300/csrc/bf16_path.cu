@@ -521,10 +521,11 @@ __global__ void __launch_bounds__(256) bf_attn_head_kernel(Dims d, const bf16* _
 
 // Radius-1, dilation-1 stencil attention over shared-memory tiles (cpu.rs:
 // 97-164, mask.rs:18-30). A CTA takes one 8 x 8 block of an instance's token
-// grid (half of an 8 x 16 conv tile): TMA brings the block's queries and the
-// keys and values of its 10 x 10 halo into shared memory as 128-byte
-// swizzled boxes (64 channels each; zero fill outside the grid, where the
-// mask excludes the candidates anyway). Thread (token, head) then does the
+// grid (half of an 8 x 16 conv tile) for the heads of one 64-channel box:
+// TMA brings the block's queries and the keys and values of its 10 x 10 halo
+// for those channels into shared memory as 128-byte swizzled boxes (zero fill
+// outside the grid, where the mask excludes the candidates anyway); 34 KB per
+// CTA keeps six CTAs on an SM. Thread (token, head) then does the
 // arithmetic of bf_attn_head_r1_kernel, in the same order, on shared-memory
 // operands: the eight lanes of a quarter warp are eight neighbouring tokens
 // of one head, so the swizzle spreads their 16-byte reads over all banks.
@@ -595,10 +596,12 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
                                                            int q_slot, const InstDev* inst, int n_inst,
                                                            bf16* __restrict__ out, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    const int D = d.D, nb = D / 64;  // 64-channel boxes per vector
-    uint8_t* sK = smem;                                   // nb halo boxes of the keys
-    uint8_t* sV = sK + (size_t)nb * kAttBoxKVPad;         // nb halo boxes of the values
-    uint8_t* sQ = sV + (size_t)nb * kAttBoxKVPad;         // nb query boxes
+    const int D = d.D;
+    constexpr int HPB = 64 / HD;                  // heads per 64-channel box
+    const int bx = blockIdx.z;                    // this CTA's box: heads bx HPB ..
+    uint8_t* sK = smem;                           // the halo box of the keys
+    uint8_t* sV = sK + (size_t)kAttBoxKVPad;      // the halo box of the values
+    uint8_t* sQ = sV + (size_t)kAttBoxKVPad;      // the query box
     __shared__ uint64_t bar;
     __shared__ volatile int failed;
     const int tile = blockIdx.x, half = blockIdx.y;
@@ -628,26 +631,24 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
     if (threadIdx.x == 0 && !failed) {
         tc::tensormap_acquire(mkv);
         tc::tensormap_acquire(mq);
-        tc::mbar_expect_tx(&bar, (uint32_t)nb * (2 * kAttBoxKV + kAttBoxQ));
-        for (int b = 0; b < nb; b++) {
-            tc::tma_load_3d(sK + (size_t)b * kAttBoxKVPad, mkv, D + 64 * b, x0 - 1, y0 - 1, &bar);
-            tc::tma_load_3d(sV + (size_t)b * kAttBoxKVPad, mkv, 2 * D + 64 * b, x0 - 1, y0 - 1, &bar);
-            tc::tma_load_3d(sQ + (size_t)b * kAttBoxQ, mq, 64 * b, x0, y0, &bar);
-        }
+        tc::mbar_expect_tx(&bar, (uint32_t)(2 * kAttBoxKV + kAttBoxQ));
+        tc::tma_load_3d(sK, mkv, D + 64 * bx, x0 - 1, y0 - 1, &bar);
+        tc::tma_load_3d(sV, mkv, 2 * D + 64 * bx, x0 - 1, y0 - 1, &bar);
+        tc::tma_load_3d(sQ, mq, 64 * bx, x0, y0, &bar);
     }
     const bool ok = __syncthreads_and(tc::mbar_wait(&bar, 0, err, &failed) ? 1 : 0) != 0;
     if (!ok) return;
-    const int heads = d.heads;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int h = warp % heads;
-    const int tok = (warp / heads) * 32 + lane;  // 0..63 within the block
+    const int hl = warp % HPB;                   // head within the box
+    const int h = bx * HPB + hl;
+    const int tok = (warp / HPB) * 32 + lane;    // 0..63 within the block
     if (tok >= kAttTile * kAttTile) return;
     const int lx = tok & 7, ly = tok >> 3;
     const int qx = x0 + lx, qy = y0 + ly;
     if (qx >= I.tx || qy >= I.ty) return;
     const float scale = 1.0f / sqrtf((float)HD);
     float q[HD];
-    load_head_s<HD>(sQ, kAttBoxQ, ly * kAttTile + lx, h * HD, q);
+    load_head_s<HD>(sQ, kAttBoxQ, ly * kAttTile + lx, hl * HD, q);
     float sc[9];
     bool in[9];
     float smax = -INFINITY;
@@ -657,7 +658,7 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
         const int ky = qy + dy, kx = qx + dx;
         in[j] = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
         const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
-        sc[j] = in[j] ? dot_head_s<HD>(q, sK, kAttBoxKVPad, rho, h * HD) * scale : -INFINITY;
+        sc[j] = in[j] ? dot_head_s<HD>(q, sK, kAttBoxKVPad, rho, hl * HD) * scale : -INFINITY;
         smax = fmaxf(smax, sc[j]);
     }
     float denom = 0.f;
@@ -674,7 +675,7 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
     for (int j = 0; j < 9; j++) {
         const int dy = j / 3 - 1, dx = j % 3 - 1;
         const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
-        if (in[j]) axpy_head_s<HD>(sc[j] * inv, sV, kAttBoxKVPad, rho, h * HD, acc);
+        if (in[j]) axpy_head_s<HD>(sc[j] * inv, sV, kAttBoxKVPad, rho, hl * HD, acc);
     }
     store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
 }
@@ -2448,7 +2449,7 @@ static bool attn_tile_ok(const Dims& d) {
     return d.mask_kind == 1 && d.radius == 1 && d.dilation == 1 && d.D % 64 == 0 && d.heads <= 4 &&
            (d.D / d.heads == 32 || d.D / d.heads == 64);
 }
-static size_t attn_tile_smem(const Dims& d) { return (size_t)(d.D / 64) * (2 * kAttBoxKVPad + kAttBoxQ); }
+static size_t attn_tile_smem(const Dims&) { return (size_t)2 * kAttBoxKVPad + kAttBoxQ; }
 
 // ---------------------------------------------------------------------------
 // host
@@ -2636,11 +2637,16 @@ static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst
     if (threads == 0) {
         // shared-memory tiles: grid (8 x 16 token tiles, their two 8 x 8 halves)
         const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
-        const dim3 grid((unsigned)p->n_ttiles, 2);
+        // one CTA per (token tile, 8 x 8 half, 64-channel box of heads)
+        const dim3 grid((unsigned)p->n_ttiles, 2, (unsigned)(d.D / 64));
         if (d.D / d.heads == 32)
-            cuda_check(launch_pdl(bf_attn_tile_kernel<32>, grid, 64 * d.heads, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst, n, attn, p->err), "launch");
+            cuda_check(launch_pdl(bf_attn_tile_kernel<32>, grid, 64 * 2, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst,
+                                  n, attn, p->err),
+                       "launch");
         else
-            cuda_check(launch_pdl(bf_attn_tile_kernel<64>, grid, 64 * d.heads, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst, n, attn, p->err), "launch");
+            cuda_check(launch_pdl(bf_attn_tile_kernel<64>, grid, 64, attn_tile_smem(d), s, 1u, d, maps, 4, 5, inst, n,
+                                  attn, p->err),
+                       "launch");
         return;
     }
     const bool r1 = d.mask_kind == 1 && d.radius == 1;
