@@ -494,6 +494,36 @@ def eval_bench(args, steps=3):
     t0 = time.perf_counter()
     oracle.roundtrip(om, omr, drops[:1], horizons, oracle.MASS | oracle.SUM64, meta_of(cfg))
     cpu_rt = time.perf_counter() - t0
+    # dump-dataset: 512 trajectories of the reference distribution on the 64x64
+    # solver grid, frames to host memory (files not written), against the
+    # oracle's solver on 8 of them
+    from jacobi2000_gb300 import dump_dataset as dd
+
+    dcfg = dd.DumpConfig(pool=512, seed=20)
+    drng = np.random.default_rng(20)
+    dtrajs = [dd.draw(dcfg, drng) for _ in range(dcfg.pool)]
+    dd.run_chunk(dcfg, dtrajs[:8])
+    t0 = time.perf_counter()
+    for c0 in range(0, len(dtrajs), 256):
+        dd.run_chunk(dcfg, dtrajs[c0:c0 + 256])
+    dump_s = time.perf_counter() - t0
+    frames = sum(t.ticks for t in dtrajs)
+    sp = dcfg.params()
+    q = oracle._SwParams()
+    q.nx, q.ny, q.dx, q.dt, q.g, q.depth, q.nu = sp.nx, sp.ny, sp.dx, sp.dt, sp.g, sp.depth, sp.nu
+    t0 = time.perf_counter()
+    cpu_steps = 0
+    for t in dtrajs[:8]:
+        st = oracle.sw_flat(q)[0]
+        oracle.sw_add_drop(q, st[0], t.cx, t.cy, t.amp, t.sigma)
+        oracle.sw_steps(q, st, t.ticks)
+        cpu_steps += t.ticks
+    cpu_dump_s = time.perf_counter() - t0
+    out["dump_dataset"] = {"config": "512 trajectories, 64x64, the reference distribution (60-80 and 400 ticks)",
+                           "s": dump_s, "trajectories_per_s": len(dtrajs) / dump_s,
+                           "solver_cell_steps_per_s": frames * 64 * 64 / dump_s,
+                           "cpu_baseline": {"solver_cell_steps_per_s": cpu_steps * 64 * 64 / cpu_dump_s, "cores": 1,
+                                            "kind": "port", "sample": f"8 trajectories, {cpu_dump_s:.2f} s"}}
     out["roundtrip"] = {"config": f"{ntraj} trajectories, horizons {horizons}, bf16 forward and reverse models",
                         "s_per_run": sec, "trajectories_per_s": ntraj / sec,
                         "model_cell_ticks_per_s": traj_ticks * cfg.nx * cfg.ny / sec,

@@ -327,6 +327,26 @@ jc_status jc_sw_run_device(const jc_sw_params* p, float* d_states, int32_t count
  * library's expf as the reference's f32::exp. */
 jc_status jc_sw_add_drop(const jc_sw_params* p, float* h, float cx, float cy, float amp, float sigma);
 
+/* One solver trajectory of dump-dataset (crates/engine-cli/src/dump_dataset.rs:
+ * 157-190): from its initial state, `ticks` ShallowWater::step calls, and after
+ * step t the fields of the drops landing at tick t added to h (the pending
+ * drops of apply_pending, :90-99). frames receives ticks + 1 states in the
+ * file layout of traj-NNNNN.f32: all h frames, then all u, then all v, each
+ * channel tick-major ([3][ticks + 1][ny][nx]). Host buffers. */
+typedef struct {
+    int32_t ticks;              /* >= 0 */
+    const float* x0;            /* initial state [3][ny][nx] (h, u, v) */
+    int32_t n_drops;            /* pending drops, >= 0 */
+    const int32_t* drop_ticks;  /* [n_drops], each in [1, ticks] */
+    const float* drop_fields;   /* [n_drops][ny][nx]: amp exp(-r^2 / (2 sigma^2)) as State::add_drop forms
+                                   it (jc_sw_add_drop on a zero plane gives it) */
+    float* frames;              /* [3][ticks + 1][ny][nx] */
+} jc_sw_trajectory;
+
+/* All trajectories advance together on the device (one solver launch per
+ * tick); the frames equal the reference's bit for bit. */
+jc_status jc_sw_trajectories(const jc_sw_params* p, const jc_sw_trajectory* t, int32_t n);
+
 /* One Gaussian drop: centre in cell coordinates, amplitude, radius in cells. */
 typedef struct {
     float cx, cy, amp, sigma;

@@ -275,6 +275,11 @@ jc_status jc_sw_run_device(const jc_sw_params* p, float* d_states, int32_t count
     return guard([&] { jc::sw_run_device(*p, d_states, count, steps, (cudaStream_t)stream); });
 }
 
+jc_status jc_sw_trajectories(const jc_sw_params* p, const jc_sw_trajectory* t, int32_t n) {
+    if (!p) return fail(JC_BAD_ARGUMENT, "params are null");
+    return guard([&] { jc::sw_trajectories_host(*p, t, n); });
+}
+
 jc_status jc_sw_add_drop(const jc_sw_params* p, float* h, float cx, float cy, float amp, float sigma) {
     if (!p) return fail(JC_BAD_ARGUMENT, "params are null");
     return guard([&] { jc::sw_add_drop_host(*p, h, cx, cy, amp, sigma); });

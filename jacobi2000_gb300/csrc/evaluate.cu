@@ -731,6 +731,153 @@ void sw_run_device(const jc_sw_params& p, float* d_states, int count, int steps,
     cuda_check(cudaFreeAsync(scratch, s), "cudaFreeAsync");
 }
 
+namespace ev {
+// h_k += field_f for the drops (k, f) landing at this tick; blockIdx.y = drop.
+__global__ void __launch_bounds__(256) add_fields_kernel(float* states, long long state_stride, const int* traj,
+                                                         const float* fields, long long n) {
+    const int f = blockIdx.y;
+    float* h = states + (long long)traj[f] * state_stride;
+    const float* d = fields + (long long)f * n;
+    for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256)
+        h[i] = __fadd_rn(h[i], d[i]);
+}
+
+// Frame t of trajectory k (blockIdx.y): its state's three planes to
+// frames_k + (c (T_k + 1) + t) n.
+__global__ void __launch_bounds__(256) capture_kernel(const float* states, long long state_stride, float* const* frames,
+                                                      const int* nframes, int t, long long n) {
+    const int k = blockIdx.y;
+    const float* s = states + (long long)k * state_stride;
+    float* f = frames[k];
+    const long long fc = (long long)nframes[k] * n;  // one channel's frames
+    for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < 3 * n; i += (long long)gridDim.x * 256) {
+        const long long c = i / n, j = i - c * n;
+        f[c * fc + (long long)t * n + j] = s[i];
+    }
+}
+}  // namespace ev
+
+void sw_trajectories_host(const jc_sw_params& p, const jc_sw_trajectory* tr, int n) {
+    ev::check_params(p);
+    if (n < 0 || (n > 0 && !tr)) throw Error(JC_BAD_ARGUMENT, "bad trajectory list");
+    if (n == 0) return;
+    if (n > 65535) throw Error(JC_LIMIT, "at most 65535 trajectories per call");
+    const long long cells = (long long)p.nx * p.ny, len = 3 * cells;
+    // longest first, so the trajectories still running at tick t are a prefix
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) {
+        const jc_sw_trajectory& t = tr[k];
+        if (t.ticks < 0 || !t.x0 || !t.frames || t.n_drops < 0 || (t.n_drops > 0 && (!t.drop_ticks || !t.drop_fields)))
+            throw Error(JC_BAD_ARGUMENT, "bad trajectory");
+        for (int d = 0; d < t.n_drops; d++)
+            if (t.drop_ticks[d] < 1 || t.drop_ticks[d] > t.ticks)
+                throw Error(JC_BAD_ARGUMENT, "drop tick outside [1, ticks]");
+        order[k] = k;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return tr[a].ticks > tr[b].ticks; });
+    const int tmax = tr[order[0]].ticks;
+    long long frame_floats = 0, n_fields = 0;
+    for (int k = 0; k < n; k++) {
+        frame_floats += (long long)(tr[k].ticks + 1) * len;
+        n_fields += tr[k].n_drops;
+    }
+    cudaStream_t s;
+    cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    DeviceArena a;
+    try {
+        float* st = a.alloc_n<float>(n * len);
+        float* scratch = a.alloc_n<float>(n * len);
+        float* frames = a.alloc_n<float>(frame_floats);
+        float* fields = a.alloc_n<float>(std::max(1LL, n_fields) * cells);
+        int* ftraj = a.alloc_n<int>(std::max(1LL, n_fields));
+        float** fptr = a.alloc_n<float*>(n);
+        int* nfr = a.alloc_n<int>(n);
+        // packed in `order`: slot i holds trajectory order[i]
+        std::vector<float*> hptr(n);
+        std::vector<int> hnfr(n);
+        std::vector<long long> foff(n);
+        long long off = 0;
+        for (int i = 0; i < n; i++) {
+            const jc_sw_trajectory& t = tr[order[i]];
+            cuda_check(cudaMemcpyAsync(st + i * len, t.x0, len * 4, cudaMemcpyHostToDevice, s), "H2D", JC_MAP);
+            foff[i] = off;
+            hptr[i] = frames + off;
+            hnfr[i] = t.ticks + 1;
+            off += (long long)(t.ticks + 1) * len;
+        }
+        cuda_check(cudaMemcpyAsync(fptr, hptr.data(), n * sizeof(float*), cudaMemcpyHostToDevice, s), "H2D", JC_MAP);
+        cuda_check(cudaMemcpyAsync(nfr, hnfr.data(), n * sizeof(int), cudaMemcpyHostToDevice, s), "H2D", JC_MAP);
+        // drop fields grouped into launches by landing tick; a trajectory's
+        // drops of one tick go to successive launches, in their order (the
+        // order apply_pending adds them in)
+        struct Launch {
+            int tick, first, count;
+        };
+        std::vector<std::vector<std::pair<int, const float*>>> at(tmax + 1);
+        for (int i = 0; i < n; i++) {
+            const jc_sw_trajectory& t = tr[order[i]];
+            for (int d = 0; d < t.n_drops; d++) at[t.drop_ticks[d]].push_back({i, t.drop_fields + (size_t)d * cells});
+        }
+        std::vector<Launch> launches;
+        std::vector<int> htraj;
+        long long fi = 0;
+        for (int t = 1; t <= tmax; t++) {
+            std::vector<int> rank(n, 0);  // drops of each trajectory placed so far at this tick
+            for (int rnk = 0;; rnk++) {
+                const long long first = fi;
+                std::fill(rank.begin(), rank.end(), 0);
+                for (auto& pr : at[t]) {
+                    if (rank[pr.first]++ != rnk) continue;
+                    cuda_check(cudaMemcpyAsync(fields + fi * cells, pr.second, cells * 4, cudaMemcpyHostToDevice, s),
+                               "H2D", JC_MAP);
+                    htraj.push_back(pr.first);
+                    fi++;
+                }
+                if (fi == first) break;
+                if (fi - first > 65535) throw Error(JC_LIMIT, "too many drops at one tick");
+                launches.push_back({t, (int)first, (int)(fi - first)});
+            }
+        }
+        if (!htraj.empty())
+            cuda_check(cudaMemcpyAsync(ftraj, htraj.data(), htraj.size() * sizeof(int), cudaMemcpyHostToDevice, s),
+                       "H2D", JC_MAP);
+        const ev::SwDev d = ev::sw_dev(p);
+        const unsigned gx = (unsigned)std::min<long long>((3 * cells + 255) / 256, 1024);
+        ev::capture_kernel<<<dim3(gx, n), 256, 0, s>>>(st, len, fptr, nfr, 0, cells);
+        cuda_check(cudaGetLastError(), "capture launch");
+        float* cur = st;
+        float* nxt = scratch;
+        int active = n;
+        size_t li = 0;
+        for (int t = 1; t <= tmax; t++) {
+            while (active > 0 && tr[order[active - 1]].ticks < t) active--;
+            ev::sw_step(d, cur, nxt, active, s);
+            std::swap(cur, nxt);
+            for (; li < launches.size() && launches[li].tick == t; li++) {
+                const Launch& L = launches[li];
+                const unsigned fx = (unsigned)std::min<long long>((cells + 255) / 256, 1024);
+                ev::add_fields_kernel<<<dim3(fx, L.count), 256, 0, s>>>(cur, len, ftraj + L.first,
+                                                                        fields + (long long)L.first * cells, cells);
+                cuda_check(cudaGetLastError(), "drop launch");
+            }
+            ev::capture_kernel<<<dim3(gx, active), 256, 0, s>>>(cur, len, fptr, nfr, t, cells);
+            cuda_check(cudaGetLastError(), "capture launch");
+        }
+        for (int i = 0; i < n; i++) {
+            const jc_sw_trajectory& t = tr[order[i]];
+            cuda_check(cudaMemcpyAsync(t.frames, frames + foff[i], (size_t)(t.ticks + 1) * len * 4,
+                                       cudaMemcpyDeviceToHost, s),
+                       "D2H", JC_MAP);
+        }
+        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+        throw;
+    }
+    cudaStreamDestroy(s);
+}
+
 void sw_add_drop_host(const jc_sw_params& p, float* h, float cx, float cy, float amp, float sigma) {
     ev::check_params(p);
     if (!h) throw Error(JC_BAD_ARGUMENT, "null h");

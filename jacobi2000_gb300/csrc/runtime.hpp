@@ -260,6 +260,7 @@ uint64_t packed_source_hash(const uint8_t* packed, size_t len);
 void sw_run_host(const jc_sw_params& p, float* states, int count, int steps);
 void sw_run_device(const jc_sw_params& p, float* d_states, int count, int steps, cudaStream_t s);
 void sw_add_drop_host(const jc_sw_params& p, float* h, float cx, float cy, float amp, float sigma);
+void sw_trajectories_host(const jc_sw_params& p, const jc_sw_trajectory* t, int n);
 void eval_score_host(const jc_config& c, const float* x, const float* truth, const float* centres, int count,
                      jc_eval_row* rows);
 jc_eval* eval_create(jc_model* m, int max_traj);

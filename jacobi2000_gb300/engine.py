@@ -732,3 +732,40 @@ def packed_precision(packed: bytes) -> int:
     8-byte magic and the u32 version)."""
     packed_source_hash(packed)  # validates the header
     return int.from_bytes(packed[12:16], "little")
+
+
+# ---- solver trajectories (jc_sw_trajectories) ---------------------------------------
+
+class JcSwTrajectory(C.Structure):
+    _fields_ = [("ticks", C.c_int32), ("x0", C.c_void_p), ("n_drops", C.c_int32), ("drop_ticks", C.c_void_p),
+                ("drop_fields", C.c_void_p), ("frames", C.c_void_p)]
+
+
+EXPORTED += ["jc_sw_trajectories"]
+
+
+def sw_trajectories(p: JcSwParams, trajectories):
+    """trajectories: [(x0 [3, ny, nx], ticks, [(tick, field [ny, nx]), ...])].
+    Returns frames [3, ticks + 1, ny, nx] per trajectory (the traj-NNNNN.f32
+    layout), all computed in one device batch."""
+    L = load_library()
+    _declare_eval(L)
+    if not getattr(L, "_traj_declared", False):
+        L.jc_sw_trajectories.argtypes = [C.POINTER(JcSwParams), C.POINTER(JcSwTrajectory), C.c_int32]
+        L.jc_sw_trajectories.restype = C.c_int
+        L._traj_declared = True
+    n = len(trajectories)
+    arr = (JcSwTrajectory * max(n, 1))()
+    keep, outs = [], []
+    for k, (x0, ticks, drops) in enumerate(trajectories):
+        xa = np.ascontiguousarray(x0, dtype=np.float32).reshape(3, p.ny, p.nx)
+        dt = np.ascontiguousarray([int(t) for t, _ in drops], dtype=np.int32)
+        df = np.ascontiguousarray(np.stack([np.asarray(f, np.float32).reshape(p.ny, p.nx) for _, f in drops])
+                                  if drops else np.zeros((1, p.ny, p.nx), np.float32))
+        fr = np.empty((3, int(ticks) + 1, p.ny, p.nx), dtype=np.float32)
+        keep += [xa, dt, df]
+        outs.append(fr)
+        arr[k] = JcSwTrajectory(int(ticks), xa.ctypes.data, len(drops), dt.ctypes.data if len(drops) else None,
+                                df.ctypes.data if len(drops) else None, fr.ctypes.data)
+    _check(L.jc_sw_trajectories(C.byref(p), arr, n))
+    return outs

@@ -321,3 +321,62 @@ def test_roundtrip_command(tmp_path, capsys):
                            "--horizons", "3,6", "--trajectories", "3"]) == 0
     out = capsys.readouterr().out
     assert "| 6 |" in out and "round-trip RMSE" in out
+
+
+def _oracle_trajectory(p, x0, ticks, drops):
+    """dump_dataset.rs:164-175 on the oracle: frames [3, ticks + 1, ny, nx]."""
+    q = _orc_sw(p)
+    s = np.array(x0, dtype=np.float32, copy=True)
+    frames = np.empty((3, ticks + 1, p.ny, p.nx), dtype=np.float32)
+    frames[:, 0] = s
+    for t in range(1, ticks + 1):
+        O.sw_steps(q, s, 1)
+        for tick, f in drops:  # apply_pending, in order
+            if tick == t:
+                s[0] = s[0] + f
+        frames[:, t] = s
+    return frames
+
+
+def test_solver_trajectories_match_oracle_bit_for_bit():
+    p = _sw(40, 24)
+    rng = np.random.default_rng(3)
+    items = []
+    for k, ticks in enumerate([9, 3, 14, 0]):
+        x0 = engine.sw_flat(p)[0]
+        engine.sw_add_drop(p, x0[0], rng.uniform(5, 35), rng.uniform(5, 19), 0.05, 3.0)
+        drops = []
+        for tick in ([2, 2, 7] if k == 0 else ([ticks] if ticks > 0 else [])):
+            f = np.zeros((p.ny, p.nx), np.float32)
+            engine.sw_add_drop(p, f, rng.uniform(5, 35), rng.uniform(5, 19), rng.uniform(-0.1, 0.1), 2.5)
+            drops.append((tick, f))
+        items.append((x0, ticks, drops))
+    got = engine.sw_trajectories(p, items)
+    for (x0, ticks, drops), fr in zip(items, got):
+        np.testing.assert_array_equal(fr, _oracle_trajectory(p, x0, ticks, drops))
+
+
+def test_dump_dataset_command(tmp_path, capsys):
+    import json
+    from jacobi2000_gb300 import dump_dataset as D
+
+    assert D.main(["--out", str(tmp_path), "--pool", "5", "--seed", "3", "--chunk", "2"]) == 0
+    assert "5 trajectories" in capsys.readouterr().out
+    manifest = json.loads((tmp_path / "manifest.json").read_text())
+    assert [h["index"] for h in manifest] == list(range(5))
+    cfg = D.DumpConfig(pool=5, seed=3)
+    p = cfg.params()
+    rng = np.random.default_rng(3)
+    trajs = [D.draw(cfg, rng) for _ in range(5)]
+    for h, t in zip(manifest, trajs):
+        assert json.loads((tmp_path / f"traj-{h['index']:05d}.json").read_text()) == h
+        raw = np.fromfile(tmp_path / f"traj-{h['index']:05d}.f32", dtype="<f4")
+        assert raw.size == 3 * h["ticks"] * 64 * 64 and h["ticks"] == t.ticks + 1
+        x0 = engine.sw_flat(p)[0]
+        engine.sw_add_drop(p, x0[0], t.cx, t.cy, t.amp, t.sigma)
+        drops = []
+        for (tick, cx, cy, amp, sigma) in t.pending:
+            f = np.zeros((64, 64), np.float32)
+            engine.sw_add_drop(p, f, cx, cy, amp, sigma)
+            drops.append((tick, f))
+        np.testing.assert_array_equal(raw.reshape(3, t.ticks + 1, 64, 64), _oracle_trajectory(p, x0, t.ticks, drops))

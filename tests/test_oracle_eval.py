@@ -209,3 +209,29 @@ def test_xcorr_lag_recovers_a_shift():
     lag = O.xcorr_lag(model, truth, 8)
     assert abs(lag - 2.0) < 0.05
     assert O.xcorr_lag(truth, truth, 8) == 0.0
+
+
+def test_dump_dataset_draws_follow_the_reference_distribution():
+    from jacobi2000_gb300 import dump_dataset as D
+
+    cfg = D.DumpConfig(pool=400)
+    rng = np.random.default_rng(20)
+    ts = [D.draw(cfg, rng) for _ in range(400)]
+    longs = [t for t in ts if t.ticks == 400]
+    shorts = [t for t in ts if t.ticks != 400]
+    assert 0.1 < len(longs) / 400 < 0.3 and all(60 <= t.ticks <= 80 for t in shorts)
+    cpt = 0.4 / np.sqrt(2.0)  # cells per tick at the CFL dt
+    for t in ts:
+        assert 0.02 <= abs(t.amp) < 0.3 and 2.5 <= t.sigma < 6.0
+        assert 8.0 <= t.cx < 56.0 and 8.0 <= t.cy < 56.0
+        assert len(t.pending) <= 2 and all(1 <= d[0] < t.ticks for d in t.pending)
+    # short, non-extended lives keep the pre-reflection margin
+    assert any(min(t.cx, t.cy, 64 - t.cx, 64 - t.cy) >= t.ticks * cpt - 1e-3 for t in shorts)
+    assert any(t.amp < 0 for t in ts) and any(t.pending for t in ts)
+
+
+def test_dump_dataset_header_layout():
+    from jacobi2000_gb300 import dump_dataset as D
+
+    h = {"index": 3, "ticks": 61, "nx": 64, "dx": 1.0, "dt": float(np.float32(0.09032)), "cx": float(np.float32(30.2))}
+    assert D.header_json(h) == '{"index":3,"ticks":61,"nx":64,"dx":1.0,"dt":0.09032,"cx":30.2}'
