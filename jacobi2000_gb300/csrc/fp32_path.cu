@@ -396,6 +396,56 @@ __device__ void block_sum_d2(double& a, double& b, double* red) {
     __syncthreads();
 }
 
+// Double-f32 sums for the block trees of the projection: a value hi + lo,
+// added error-free (two-sum), so a tree over 512 threads keeps about 2^-44
+// relative accuracy on the FP32 pipes; this GPU's f64 rate is a small
+// fraction of its f32 rate, and the trees would otherwise be f64 shuffles and
+// adds.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+    const float s = __fadd_rn(x.hi, y.hi);
+    const float bb = __fsub_rn(s, x.hi);
+    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+    const float t = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    const float hi = __fadd_rn(s, t);
+    return DF{hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ DF warp_sum_df(DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+    return v;
+}
+// Block sums of two per-thread values in the fixed tree of warp_sum_df:
+// warps, then warp 0 over the warp totals; the totals as f64 in every thread.
+__device__ void block_sum_df2(DF a, DF b, double& A, double& B, DF* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    a = warp_sum_df(a);
+    b = warp_sum_df(b);
+    __syncthreads();
+    if (lane == 0) {
+        red[warp] = a;
+        red[32 + warp] = b;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const DF z{0.f, 0.f};
+        DF ta = lane < nw ? red[lane] : z, tb = lane < nw ? red[32 + lane] : z;
+        ta = warp_sum_df(ta);
+        tb = warp_sum_df(tb);
+        if (lane == 0) {
+            red[0] = ta;
+            red[32] = tb;
+        }
+    }
+    __syncthreads();
+    A = (double)red[0].hi + (double)red[0].lo;
+    B = (double)red[32].hi + (double)red[32].lo;
+    __syncthreads();
+}
+
 // Mass then energy projection (eval.rs:148-153 order; project.rs:33-54). One
 // thread-block cluster of kProjCluster CTAs per instance; each CTA keeps its
 // slice of the state in shared memory (when it fits) for the three passes:
@@ -437,7 +487,8 @@ struct Kahan {
 // Reduction segments: an instance's cells are cut into segments of
 // kProjSeg cells; a segment's sums are always formed the same way (thread t
 // takes cells t, t + 512, ... with f32 Kahan compensation, then the fixed
-// block tree in f64), and the instance total adds the segment totals in
+// block tree in double-f32, converted to f64), and the instance total adds
+// the segment totals in f64 in
 // segment order. A CTA of the cluster owns a contiguous run of segments, so
 // the totals do not depend on the cluster size the launch picked, nor on the
 // other instances of the launch.
@@ -482,7 +533,7 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
     // [3][cap] f32: this CTA's cells when they fit; then 3 x (1 + 2 seg_cap)
     // f64: per pass, the segment count and this CTA's segment totals
     extern __shared__ __align__(16) float sst[];
-    __shared__ double red[64];
+    __shared__ __align__(16) double red[64];  // the block trees' DF scratch (64 pairs)
     __shared__ double tot[4];
     cg::cluster_group cluster = cg::this_cluster();
     const int cs = (int)cluster.num_blocks();
@@ -532,8 +583,8 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
                     if (nv > 1) b.add(tb);
                 }
             }
-            double A = a.val(), B = b.val();
-            block_sum_d2(A, B, red);
+            double A, B;
+            block_sum_df2(DF{a.s, -a.c}, DF{b.s, -b.c}, A, B, reinterpret_cast<DF*>(red));
             if (threadIdx.x == 0) {
                 mine[1 + 2 * (k - k0)] = A;
                 mine[2 + 2 * (k - k0)] = B;
