@@ -351,51 +351,6 @@ __global__ void __launch_bounds__(kConv2Threads, 8) conv2_step_kernel(const floa
     }
 }
 
-// Block-wide f64 sum (fixed order, deterministic). `red` holds 32 doubles.
-__device__ double block_sum_d(double v, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum_d(v);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (warp == 0) {
-        t = lane < nw ? red[lane] : 0.0;
-        t = warp_sum_d(t);
-        if (lane == 0) red[0] = t;
-    }
-    __syncthreads();
-    double r = red[0];
-    __syncthreads();
-    return r;
-}
-
-// Two block-wide f64 sums at once, each in the order of block_sum_d.
-__device__ void block_sum_d2(double& a, double& b, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    a = warp_sum_d(a);
-    b = warp_sum_d(b);
-    __syncthreads();
-    if (lane == 0) {
-        red[warp] = a;
-        red[32 + warp] = b;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        double ta = lane < nw ? red[lane] : 0.0, tb = lane < nw ? red[32 + lane] : 0.0;
-        ta = warp_sum_d(ta);
-        tb = warp_sum_d(tb);
-        if (lane == 0) {
-            red[0] = ta;
-            red[32] = tb;
-        }
-    }
-    __syncthreads();
-    a = red[0];
-    b = red[32];
-    __syncthreads();
-}
-
 // Double-f32 sums for the block trees of the projection: a value hi + lo,
 // added error-free (two-sum), so a tree over 512 threads keeps about 2^-44
 // relative accuracy on the FP32 pipes; this GPU's f64 rate is a small
@@ -481,7 +436,6 @@ struct Kahan {
         c = __fsub_rn(__fsub_rn(t, s), y);
         s = t;
     }
-    __device__ __forceinline__ double val() const { return (double)s - (double)c; }
 };
 
 // Reduction segments: an instance's cells are cut into segments of
