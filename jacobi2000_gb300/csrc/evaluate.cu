@@ -72,45 +72,59 @@ sw_step_kernel(SwDev p, const float* __restrict__ src, float* __restrict__ dst) 
     const int x0 = blockIdx.x * kSwTX, y0 = blockIdx.y * kSwTY;
     const int tid = threadIdx.x;
     // inputs on [y0-2, y0+TY+2) x [x0-2, x0+TX+2); apron positions outside
-    // the grid hold a clamped neighbour and are never read below
+    // the grid hold a clamped neighbour and are never read below. Thread t
+    // keeps column t % kSwPX and walks rows t / kSwPX, + kLoadRows, ...
+    constexpr int kLoadRows = kSwThreads / kSwPX;  // 7 rows per pass
+    if (tid < kLoadRows * kSwPX) {
+        const int lx = tid % kSwPX;
+        const int gx = min(max(x0 - 2 + lx, 0), nx - 1);
 #pragma unroll
-    for (int i = tid; i < kSwPY * kSwPX; i += kSwThreads) {
-        const int ly = i / kSwPX, lx = i - ly * kSwPX;
-        const int gx = min(max(x0 - 2 + lx, 0), nx - 1), gy = min(max(y0 - 2 + ly, 0), ny - 1);
-        const long long o = (long long)gy * nx + gx;
-        sm.h[ly][lx] = __ldg(H + o);
-        sm.u[ly][lx] = __ldg(U + o);
-        sm.v[ly][lx] = __ldg(V + o);
+        for (int ly = tid / kSwPX; ly < kSwPY; ly += kLoadRows) {
+            const int gy = min(max(y0 - 2 + ly, 0), ny - 1);
+            const long long o = (long long)gy * nx + gx;
+            sm.h[ly][lx] = __ldg(H + o);
+            sm.u[ly][lx] = __ldg(U + o);
+            sm.v[ly][lx] = __ldg(V + o);
+        }
     }
     __syncthreads();
-    // continuity on the tile and its 1-cell apron (cells inside the grid)
-#pragma unroll
-    for (int i = tid; i < kSwNY * kSwNX; i += kSwThreads) {
-        const int ly = i / kSwNX, lx = i - ly * kSwNX;
-        const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-        if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
-        const int sx = lx + 1, sy = ly + 1;
-        const float h = sm.h[sy][sx];
-        const float fxl = gx == 0 ? 0.f : face_flux(sm.h[sy][sx - 1], h, sm.u[sy][sx - 1], sm.u[sy][sx]);
-        const float fxr = gx == nx - 1 ? 0.f : face_flux(h, sm.h[sy][sx + 1], sm.u[sy][sx], sm.u[sy][sx + 1]);
-        const float fyl = gy == 0 ? 0.f : face_flux(sm.h[sy - 1][sx], h, sm.v[sy - 1][sx], sm.v[sy][sx]);
-        const float fyr = gy == ny - 1 ? 0.f : face_flux(h, sm.h[sy + 1][sx], sm.v[sy][sx], sm.v[sy + 1][sx]);
-        sm.hn[ly][lx] = __fsub_rn(h, __fmul_rn(p.r, __fadd_rn(__fsub_rn(fxr, fxl), __fsub_rn(fyr, fyl))));
+    // continuity on the tile and its 1-cell apron (cells inside the grid);
+    // thread t keeps column t % kSwNX
+    constexpr int kContRows = kSwThreads / kSwNX;  // 7 rows per pass
+    if (tid < kContRows * kSwNX) {
+        const int lx = tid % kSwNX;
+        const int gx = x0 - 1 + lx;
+        const bool xin = gx >= 0 && gx < nx;
+        const bool wl = gx == 0, wr = gx == nx - 1;
+        const int sx = lx + 1;
+        for (int ly = tid / kSwNX; ly < kSwNY; ly += kContRows) {
+            const int gy = y0 - 1 + ly;
+            if (!xin || gy < 0 || gy >= ny) continue;
+            const int sy = ly + 1;
+            const float h = sm.h[sy][sx];
+            const float fxl = wl ? 0.f : face_flux(sm.h[sy][sx - 1], h, sm.u[sy][sx - 1], sm.u[sy][sx]);
+            const float fxr = wr ? 0.f : face_flux(h, sm.h[sy][sx + 1], sm.u[sy][sx], sm.u[sy][sx + 1]);
+            const float fyl = gy == 0 ? 0.f : face_flux(sm.h[sy - 1][sx], h, sm.v[sy - 1][sx], sm.v[sy][sx]);
+            const float fyr = gy == ny - 1 ? 0.f : face_flux(h, sm.h[sy + 1][sx], sm.v[sy][sx], sm.v[sy + 1][sx]);
+            sm.hn[ly][lx] = __fsub_rn(h, __fmul_rn(p.r, __fadd_rn(__fsub_rn(fxr, fxl), __fsub_rn(fyr, fyl))));
+        }
     }
     __syncthreads();
     float* D = dst + (long long)blockIdx.z * 3 * n;
-    // momentum, centred differences on the new surface (:188-232)
+    // momentum, centred differences on the new surface (:188-232); thread t
+    // keeps column t % kSwTX and takes rows t / kSwTX, + 8, ...
+    const int tx = tid % kSwTX;
+    const int gx = x0 + tx;
+    const int sx = tx + 2, qx = tx + 1;  // in h, u, v / in hn
+    const int dxm = gx == 0 ? 0 : -1, dxp = gx == nx - 1 ? 0 : 1;
+    const float sxm = gx == 0 ? -1.f : 1.f, sxp = gx == nx - 1 ? -1.f : 1.f;
 #pragma unroll
     for (int c = 0; c < (kSwTX * kSwTY) / kSwThreads; c++) {
-        const int j = tid + c * kSwThreads;
-        const int tx = j % kSwTX, ty = j / kSwTX;
-        const int gx = x0 + tx, gy = y0 + ty;
+        const int ty = tid / kSwTX + c * (kSwThreads / kSwTX);
+        const int gy = y0 + ty;
         if (gx >= nx || gy >= ny) continue;
-        const int sx = tx + 2, sy = ty + 2;  // in h, u, v
-        const int qx = tx + 1, qy = ty + 1;  // in hn
-        const int dxm = gx == 0 ? 0 : -1, dxp = gx == nx - 1 ? 0 : 1;
+        const int sy = ty + 2, qy = ty + 1;
         const int dym = gy == 0 ? 0 : -1, dyp = gy == ny - 1 ? 0 : 1;
-        const float sxm = gx == 0 ? -1.f : 1.f, sxp = gx == nx - 1 ? -1.f : 1.f;
         const float sym = gy == 0 ? -1.f : 1.f, syp = gy == ny - 1 ? -1.f : 1.f;
         const float hl = sm.hn[qy][qx + dxm], hr = sm.hn[qy][qx + dxp];
         const float hd = sm.hn[qy + dym][qx], hu = sm.hn[qy + dyp][qx];
