@@ -588,11 +588,89 @@ __device__ __forceinline__ void axpy_head_s(float wgt, const uint8_t* boxes, int
     }
 }
 
+// lo += a.lo * b.lo, hi += a.hi * b.hi for bf16 pairs a, b with f32
+// accumulators, one rounding each (mixed-precision fma.rn.f32.bf16).
+__device__ __forceinline__ void fma2_bf16_f32(uint32_t a, uint32_t b, float& lo, float& hi) {
+    asm("{\n\t.reg .b16 al, ah, bl, bh;\n\t"
+        "mov.b32 {al, ah}, %2;\n\t"
+        "mov.b32 {bl, bh}, %3;\n\t"
+        "fma.rn.f32.bf16 %0, al, bl, %0;\n\t"
+        "fma.rn.f32.bf16 %1, ah, bh, %1;\n\t}"
+        : "+f"(lo), "+f"(hi)
+        : "r"(a), "r"(b));
+}
+
+// One (token, head) of the radius-1 stencil attention from the staged boxes:
+// query box sQ (8 x 8 tokens), key and value halo boxes sK, sV (10 x 10; the
+// positions outside the grid hold the tensor map's zero fill), token (lx, ly)
+// of the block, grid position (qx, qy) in a tx x ty token grid. The nine
+// scores are accumulated together, channel chunk outer and key inner, so a
+// thread has 18 independent FMA chains in flight; each chain adds its
+// channels in the same order as dot_head_s. Keys outside the grid get score
+// -inf and weight 0 (their zero-filled values then add exact zeros).
+template <int HD>
+__device__ __forceinline__ void attn_stencil_token(const uint8_t* sQ, const uint8_t* sK, const uint8_t* sV, int lx,
+                                                   int ly, int qx, int qy, int tx, int ty, int hl, float scale,
+                                                   float* acc) {
+    // the query stays packed (bf16 pairs); scores use the mixed-precision FMA
+    // bf16 x bf16 + f32, whose product is exact in f32, so each step rounds
+    // exactly like fmaf on the unpacked values
+    uint32_t q[HD / 2];
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const int ch = hl * HD + 8 * w;
+        const uint4 u = *swz_chunk(sQ + (size_t)(ch >> 6) * kAttBoxQ, ly * kAttTile + lx, (ch & 63) >> 3);
+        q[4 * w] = u.x;
+        q[4 * w + 1] = u.y;
+        q[4 * w + 2] = u.z;
+        q[4 * w + 3] = u.w;
+    }
+    float p0[9], p1[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) p0[j] = p1[j] = 0.f;
+#pragma unroll
+    for (int w = 0; w < HD / 8; w++) {
+        const int ch = hl * HD + 8 * w;
+#pragma unroll
+        for (int j = 0; j < 9; j++) {
+            const int rho = (ly + j / 3) * kAttHalo + (lx + j % 3);
+            const uint4 u = *swz_chunk(sK + (size_t)(ch >> 6) * kAttBoxKVPad, rho, (ch & 63) >> 3);
+            const uint32_t a[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) fma2_bf16_f32(q[4 * w + i], a[i], p0[j], p1[j]);
+        }
+    }
+    float sc[9];
+    bool in[9];
+    float smax = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int ky = qy + j / 3 - 1, kx = qx + j % 3 - 1;
+        in[j] = ky >= 0 && kx >= 0 && ky < ty && kx < tx;
+        sc[j] = in[j] ? (p0[j] + p1[j]) * scale : -INFINITY;
+        smax = fmaxf(smax, sc[j]);
+    }
+    float denom = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        sc[j] = in[j] ? __expf(sc[j] - smax) : 0.f;
+        denom += sc[j];
+    }
+    const float inv = 1.0f / denom;
+#pragma unroll
+    for (int i = 0; i < HD; i++) acc[i] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int rho = (ly + j / 3) * kAttHalo + (lx + j % 3);
+        axpy_head_s<HD>(sc[j] * inv, sV, kAttBoxKVPad, rho, hl * HD, acc);
+    }
+}
+
 // Maps of an instance used here: slot kv_slot = halo boxes (64 ch x 10 x 10)
 // over its qkv rows, slot q_slot = query boxes (64 ch x 8 x 8) over the same
 // rows. D = 64 * (boxes per vector); threads = 64 tokens x heads.
 template <int HD>
-__global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtensorMap* __restrict__ maps, int kv_slot,
+__global__ void __launch_bounds__(64 * (64 / HD), 5) bf_attn_tile_kernel(Dims d, const CUtensorMap* __restrict__ maps, int kv_slot,
                                                            int q_slot, const InstDev* inst, int n_inst,
                                                            bf16* __restrict__ out, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -647,37 +725,118 @@ __global__ void __launch_bounds__(256) bf_attn_tile_kernel(Dims d, const CUtenso
     const int qx = x0 + lx, qy = y0 + ly;
     if (qx >= I.tx || qy >= I.ty) return;
     const float scale = 1.0f / sqrtf((float)HD);
-    float q[HD];
-    load_head_s<HD>(sQ, kAttBoxQ, ly * kAttTile + lx, hl * HD, q);
-    float sc[9];
-    bool in[9];
-    float smax = -INFINITY;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        const int dy = j / 3 - 1, dx = j % 3 - 1;
-        const int ky = qy + dy, kx = qx + dx;
-        in[j] = ky >= 0 && kx >= 0 && ky < I.ty && kx < I.tx;
-        const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
-        sc[j] = in[j] ? dot_head_s<HD>(q, sK, kAttBoxKVPad, rho, hl * HD) * scale : -INFINITY;
-        smax = fmaxf(smax, sc[j]);
-    }
-    float denom = 0.f;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        sc[j] = in[j] ? __expf(sc[j] - smax) : 0.f;
-        denom += sc[j];
-    }
-    const float inv = 1.0f / denom;
     float acc[HD];
-#pragma unroll
-    for (int i = 0; i < HD; i++) acc[i] = 0.f;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        const int dy = j / 3 - 1, dx = j % 3 - 1;
-        const int rho = (ly + 1 + dy) * kAttHalo + (lx + 1 + dx);
-        if (in[j]) axpy_head_s<HD>(sc[j] * inv, sV, kAttBoxKVPad, rho, hl * HD, acc);
-    }
+    attn_stencil_token<HD>(sQ, sK, sV, lx, ly, qx, qy, I.tx, I.ty, hl, scale, acc);
     store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
+}
+
+// The same stencil attention with persistent CTAs: a CTA walks the work
+// items (token tile, 8 x 8 half, 64-channel box; item = (2 tile + half) *
+// boxes + box) with stride gridDim.x, through two stages of [key halo, value
+// halo, query] boxes in shared memory. The boxes of the item two steps ahead
+// load by TMA while this item is computed, so a CTA's loads overlap its
+// arithmetic instead of preceding it. Each output is computed exactly as in
+// bf_attn_tile_kernel (same per-thread order, same bits).
+constexpr int kAttStage = 2 * kAttBoxKVPad + kAttBoxQ;  // 34 KB, a multiple of 1024
+constexpr size_t kAttRingSmem = 2 * (size_t)kAttStage;
+
+template <int HD>
+__global__ void __launch_bounds__(128) bf_attn_ring_kernel(Dims d, const CUtensorMap* __restrict__ maps, int kv_slot,
+                                                           int q_slot, const InstDev* inst, int n_inst, int n_ttiles,
+                                                           bf16* __restrict__ out, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int D = d.D;
+    constexpr int HPB = 64 / HD;
+    const int nb = D / 64;
+    const int n_items = n_ttiles * 2 * nb;
+    __shared__ uint64_t bar[2];
+    __shared__ volatile int failed;
+    // item -> instance, token-space origin of its 8 x 8 half, box; false for
+    // the lower half of a tile that overhangs the grid (no load, no work)
+    auto decode = [&](int item, int& lo, int& x0, int& y0, int& bx) {
+        bx = item % nb;
+        const int th = item / nb, tile = th >> 1, half = th & 1;
+        lo = 0;
+        int hi = n_inst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (inst[mid].tt0 <= tile) lo = mid; else hi = mid - 1;
+        }
+        const int tiles_x = (inst[lo].tx + kConvTX - 1) / kConvTX;
+        const int tl = tile - inst[lo].tt0;
+        x0 = (tl % tiles_x) * kConvTX;
+        y0 = (tl / tiles_x) * kConvTY + half * kAttTile;
+        return y0 < inst[lo].ty;
+    };
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::fence_barrier_init();
+        failed = 0;
+        if (tc::smem_u32(smem) & 1023u) {
+            failed = 1;
+            atomicExch(err, 2);
+        }
+    }
+    __syncthreads();
+    JC_PDL_ENTRY;
+    unsigned pending = 0;  // stages with a load in flight (thread 0's view)
+    auto issue = [&](int item, int s) {
+        int lo, x0, y0, bx;
+        if (!decode(item, lo, x0, y0, bx)) return;
+        const CUtensorMap* mkv = maps + kMapsPerInst * lo + kv_slot;
+        const CUtensorMap* mq = maps + kMapsPerInst * lo + q_slot;
+        uint8_t* st = smem + (size_t)s * kAttStage;
+        tc::tensormap_acquire(mkv);
+        tc::tensormap_acquire(mq);
+        tc::mbar_expect_tx(&bar[s], (uint32_t)(2 * kAttBoxKV + kAttBoxQ));
+        tc::tma_load_3d(st, mkv, D + 64 * bx, x0 - 1, y0 - 1, &bar[s]);
+        tc::tma_load_3d(st + kAttBoxKVPad, mkv, 2 * D + 64 * bx, x0 - 1, y0 - 1, &bar[s]);
+        tc::tma_load_3d(st + 2 * kAttBoxKVPad, mq, 64 * bx, x0, y0, &bar[s]);
+        pending |= 1u << s;
+    };
+    if (threadIdx.x == 0 && !failed) {
+        if ((int)blockIdx.x < n_items) issue(blockIdx.x, 0);
+        if ((int)(blockIdx.x + gridDim.x) < n_items) issue(blockIdx.x + gridDim.x, 1);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int hl = warp % HPB;                 // head within the box
+    const int tok = (warp / HPB) * 32 + lane;  // 0..63 within the half tile
+    const int lx = tok & 7, ly = tok >> 3;
+    const float scale = 1.0f / sqrtf((float)HD);
+    unsigned phase = 0;  // parity of each stage's next completion
+    int k = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x, k++) {
+        const int s = k & 1;
+        int lo, x0, y0, bx;
+        if (decode(item, lo, x0, y0, bx)) {  // uniform per CTA
+            const bool ok =
+                __syncthreads_and(tc::mbar_wait(&bar[s], (phase >> s) & 1u, err, &failed) ? 1 : 0) != 0;
+            if (!ok) break;
+            phase ^= 1u << s;
+            if (threadIdx.x == 0) pending &= ~(1u << s);
+            const InstDev& I = inst[lo];
+            const uint8_t* sK = smem + (size_t)s * kAttStage;
+            const uint8_t* sV = sK + kAttBoxKVPad;
+            const uint8_t* sQ = sV + kAttBoxKVPad;
+            const int qx = x0 + lx, qy = y0 + ly;
+            if (qx < I.tx && qy < I.ty) {
+                float acc[HD];
+                attn_stencil_token<HD>(sQ, sK, sV, lx, ly, qx, qy, I.tx, I.ty, hl, scale, acc);
+                store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + (bx * HPB + hl) * HD, acc);
+            }
+        }
+        __syncthreads();  // stage s is free
+        if (threadIdx.x == 0 && !failed && item + 2 * (int)gridDim.x < n_items) issue(item + 2 * gridDim.x, s);
+    }
+    // after a failed wait: let this CTA's copies still in flight land (bounded)
+    if (threadIdx.x == 0 && pending) {
+        const unsigned long long t0 = tc::globaltimer();
+        for (int s = 0; s < 2; s++)
+            if (pending & (1u << s))
+                while (!tc::mbar_try_wait(&bar[s], (phase >> s) & 1u) && tc::globaltimer() - t0 < tc::kWaitNs) {
+                }
+    }
 }
 
 // to_cells' output (f32 [rows, HD]) -> the cell-head input zc (f16 [cells,
@@ -2616,6 +2775,8 @@ void BF16Path::set_kernel_attributes() {
     set_smem(tc_conv1_persistent_kernel, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
+    set_smem(bf_attn_ring_kernel<32>, kAttRingSmem);
+    set_smem(bf_attn_ring_kernel<64>, kAttRingSmem);
     set_smem(tc_mlp_persistent_kernel, kMlpSmemMax);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
@@ -2634,6 +2795,37 @@ void BF16Path::set_kernel_attributes() {
 
 static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
                              int threads, cudaStream_t s, const Pack* p = nullptr) {
+    if (threads == -1) {
+        // persistent CTAs over (token tile, half, box) items, two load stages
+        const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
+        const int items = p->n_ttiles * 2 * (d.D / 64);
+        static int per_sm[2] = {0, 0}, sms = 0;  // CTAs per SM for head width 32 / 64
+        if (sms == 0) {
+            int dev = 0;
+            cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+            cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        }
+        const bool h32 = d.D / d.heads == 32;
+        int& occ = per_sm[h32 ? 0 : 1];
+        if (occ == 0) {
+            if (h32)
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bf_attn_ring_kernel<32>, 128, kAttRingSmem),
+                           "occupancy");
+            else
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bf_attn_ring_kernel<64>, 64, kAttRingSmem),
+                           "occupancy");
+        }
+        const unsigned grid = (unsigned)std::max(1, std::min(items, std::max(1, occ) * sms));
+        if (h32)
+            cuda_check(launch_pdl(bf_attn_ring_kernel<32>, grid, 128, kAttRingSmem, s, 1u, d, maps, 4, 5, inst, n,
+                                  p->n_ttiles, attn, p->err),
+                       "launch");
+        else
+            cuda_check(launch_pdl(bf_attn_ring_kernel<64>, grid, 64, kAttRingSmem, s, 1u, d, maps, 4, 5, inst, n,
+                                  p->n_ttiles, attn, p->err),
+                       "launch");
+        return;
+    }
     if (threads == 0) {
         // shared-memory tiles: grid (8 x 16 token tiles, their two 8 x 8 halves)
         const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
@@ -2783,8 +2975,8 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
         }
     }
     best_ms = 1e30f;
-    for (int threads : {0, 64, 128, 256}) {
-        if (threads == 0 && !attn_tile_ok(d)) continue;
+    for (int threads : {-1, 0, 64, 128, 256}) {
+        if (threads <= 0 && !attn_tile_ok(d)) continue;
         const float ms =
             time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s, &p); }, 3, s);
         log += ", \"attn_" + std::to_string(threads) + "_ms\": " + std::to_string(ms);
@@ -2821,7 +3013,7 @@ void BF16Path::load_cache() {
                         key, &bucket, &form, &nc, &ns, &th) != 6)
             continue;
         if (cache_key_ == key && mlp_fits(nc, ns, form) &&
-            (th == 64 || th == 128 || th == 256 || (th == 0 && attn_tile_ok(dims_))))
+            (th == 64 || th == 128 || th == 256 || (th <= 0 && th >= -1 && attn_tile_ok(dims_))))
             tuned_[bucket] = Tuning{nc, ns, th, form};
     }
     std::fclose(f);

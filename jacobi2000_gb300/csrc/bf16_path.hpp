@@ -21,7 +21,7 @@ namespace jc {
 struct Tuning {
     int nc;            // 32 or 64 hidden columns per MLP step
     int ns;            // MLP weight-ring stages (2-4; 1 for the serial form)
-    int attn_threads;  // 64, 128 or 256 threads per attention CTA; 0 = shared-memory tiles
+    int attn_threads;  // 64, 128 or 256 threads per attention CTA; 0 = shared-memory tiles, -1 = persistent tiles
     int form;          // MLP kernel: 0 serial, 1 pipelined per tile, 2 persistent
 };
 

@@ -58,7 +58,7 @@ def test_every_schedule_gives_identical_results(tmp_path, monkeypatch, dim):
         monkeypatch.setenv("JC_AUTOTUNE_CACHE", str(cache))
         engine.autotune(True)
         mlp = [(0, 32, 1), (0, 64, 1), (1, 32, 2), (1, 32, 3), (1, 64, 2), (1, 64, 3), (2, 64, 2)]
-        scheds = [m + (256,) for m in mlp] + [(0, 64, 1, 64), (0, 64, 1, 128), (0, 64, 1, 0)]
+        scheds = [m + (256,) for m in mlp] + [(0, 64, 1, 64), (0, 64, 1, 128), (0, 64, 1, 0), (0, 64, 1, -1)]
         for form, nc, ns, threads in scheds:
             # a cache file written beforehand fixes the schedule of every row bucket
             key = _key(fam[0][2])
@@ -84,7 +84,7 @@ def test_tuning_is_recorded_and_reused(tmp_path, monkeypatch):
         assert len(rows) >= 2  # the batch's row bucket and the single forward's
         assert all(r["model"] == _key(fam[0][2]) for r in rows)
         assert all(r["mlp_form"] in (0, 1, 2) and r["nc"] in (32, 64) and r["stages"] in (1, 2, 3, 4)
-                   and r["attn_threads"] in (0, 64, 128, 256) for r in rows)
+                   and r["attn_threads"] in (-1, 0, 64, 128, 256) for r in rows)
         size = cache.stat().st_size
         again, _ = _run(fam, [(1, 2), (1, 2), (0, 2)])
         assert cache.stat().st_size == size  # read back, not tuned again
