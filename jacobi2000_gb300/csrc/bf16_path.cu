@@ -177,7 +177,9 @@ __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 // float4s and 4 x CPL weights and does 32 x CPL FMAs. Each output is summed in
 // the reference's order (bias, then the patch elements in order, then + pos,
 // + the meta linear); x is written f32 and LayerNorm(x) bf16, with vector
-// stores.
+// stores. The pos rows of a warp's 8 rows are loaded together before the
+// LayerNorms, and the meta linear is kept while the instance stays the same
+// (across tiles too).
 constexpr int kEmbedRows = 64;
 constexpr int kEmbedGroups = 12;  // 3 channels x 4 patch rows, 4 patch columns each
 
@@ -186,7 +188,7 @@ __host__ __device__ constexpr size_t embed_smem(int D) {
 }
 
 template <int CPL>
-__global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __restrict__ We,
+__global__ void __launch_bounds__(256, (CPL <= 4 ? 3 : 1)) bf_embed_kernel(Dims d, const float* __restrict__ We,
                                                        const float* __restrict__ be, const float* __restrict__ Wm,
                                                        const float* __restrict__ bm, const float* __restrict__ g,
                                                        const float* __restrict__ b, const InstDev* inst, int n_inst,
@@ -201,12 +203,15 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
     const int n_tiles = (R + kEmbedRows - 1) / kEmbedRows;
     for (int i = threadIdx.x; i < pd * D / 4; i += blockDim.x)
         cp_async16(reinterpret_cast<float4*>(sW) + i, reinterpret_cast<const float4*>(We) + i, true);
-    // the patches of tile t into buffer `buf` (and each row's instance)
+    // the patches of tile t into buffer `buf` (and each row's instance); with
+    // 256 threads, a multiple of the tile's rows, a thread copies the patches
+    // of one row (threadIdx.x % kEmbedRows), so it finds that row's instance once
+    static_assert(256 % kEmbedRows == 0, "embed copy layout");
     auto issue = [&](int t, int buf) {
+        const int i = threadIdx.x % kEmbedRows, r = t * kEmbedRows + i;
+        const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
         for (int e = threadIdx.x; e < kEmbedRows * kEmbedGroups; e += blockDim.x) {
-            const int i = e % kEmbedRows, gq = e / kEmbedRows;  // row, (channel, patch row)
-            const int r = t * kEmbedRows + i;
-            const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
+            const int gq = e / kEmbedRows;  // (channel, patch row)
             if (gq == 0) rinst[buf][i] = ii;
             const float* src = We;
             if (ii >= 0) {
@@ -223,6 +228,8 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
     const int i0 = warp * 8;  // this warp's 8 rows
     const int o0 = CPL * lane;
     int k = 0;
+    int m_inst = -1;  // the instance whose meta linear m holds
+    float m[CPL];
     if ((int)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, k++) {
         const int buf = k & 1;
@@ -268,17 +275,36 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
                     }
                 }
             }
-            // the meta linear depends only on the instance: computed once for
-            // the warp's first row and again only where the instance changes
-            int m_inst = -1;
-            float m[CPL];
+            // + pos for the warp's 8 rows, the loads of all rows in flight together
+            int rii[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int r = r0 + i0 + q;
+                rii[q] = r < R ? rinst[buf][i0 + q] : -1;
+                if (rii[q] >= 0) {
+                    const InstDev& I = inst[rii[q]];
+                    const float* pos = I.pos + (size_t)(r - I.row0) * D + o0;
+                    if (CPL % 4 == 0) {
+#pragma unroll
+                        for (int c = 0; c < CPL; c += 4) {
+                            const float4 p4 = *reinterpret_cast<const float4*>(pos + c);
+                            v[q][c] += p4.x; v[q][c + 1] += p4.y; v[q][c + 2] += p4.z; v[q][c + 3] += p4.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < CPL; c++) v[q][c] += pos[c];
+                    }
+                }
+            }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const int r = r0 + i0 + q;
                 if (r >= R) continue;  // warp-uniform
-                const int ii = rinst[buf][i0 + q];
-                const InstDev& I = inst[ii];
+                const int ii = rii[q];
                 if (ii != m_inst) {
+                    // the meta linear depends only on the instance: computed
+                    // again only where the instance changes (kept across tiles)
+                    const InstDev& I = inst[ii];
                     m_inst = ii;
 #pragma unroll
                     for (int c = 0; c < CPL; c++) {
@@ -286,12 +312,10 @@ __global__ void __launch_bounds__(256) bf_embed_kernel(Dims d, const float* __re
                         for (int f = 0; f < d.meta_dim; f++) m[c] = fmaf(I.meta[f], Wm[(size_t)f * D + o0 + c], m[c]);
                     }
                 }
-                const int tk = r - I.row0;
-                const float* pos = I.pos + (size_t)tk * D + o0;
                 float sum = 0.f;
 #pragma unroll
                 for (int c = 0; c < CPL; c++) {
-                    v[q][c] = (v[q][c] + pos[c]) + m[c];
+                    v[q][c] = v[q][c] + m[c];
                     sum += v[q][c];
                 }
                 const float mean = warp_sum(sum) / (float)D;
