@@ -565,38 +565,6 @@ __device__ __forceinline__ const uint4* swz_chunk(const uint8_t* box, int rho, i
 }
 
 template <int HD>
-__device__ __forceinline__ void load_head_s(const uint8_t* boxes, int box_stride, int rho, int ch0, float* f) {
-#pragma unroll
-    for (int w = 0; w < HD / 8; w++) {
-        const int ch = ch0 + 8 * w;
-        const uint4 u = *swz_chunk(boxes + (size_t)(ch >> 6) * box_stride, rho, (ch & 63) >> 3);
-        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            f[8 * w + 2 * i] = __uint_as_float(a[i] << 16);
-            f[8 * w + 2 * i + 1] = __uint_as_float(a[i] & 0xffff0000u);
-        }
-    }
-}
-
-template <int HD>
-__device__ __forceinline__ float dot_head_s(const float* q, const uint8_t* boxes, int box_stride, int rho, int ch0) {
-    float p0 = 0.f, p1 = 0.f;
-#pragma unroll
-    for (int w = 0; w < HD / 8; w++) {
-        const int ch = ch0 + 8 * w;
-        const uint4 u = *swz_chunk(boxes + (size_t)(ch >> 6) * box_stride, rho, (ch & 63) >> 3);
-        const uint32_t a[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            p0 = fmaf(q[8 * w + 2 * i], __uint_as_float(a[i] << 16), p0);
-            p1 = fmaf(q[8 * w + 2 * i + 1], __uint_as_float(a[i] & 0xffff0000u), p1);
-        }
-    }
-    return p0 + p1;
-}
-
-template <int HD>
 __device__ __forceinline__ void axpy_head_s(float wgt, const uint8_t* boxes, int box_stride, int rho, int ch0,
                                             float* acc) {
 #pragma unroll
@@ -630,7 +598,9 @@ __device__ __forceinline__ void fma2_bf16_f32(uint32_t a, uint32_t b, float& lo,
 // of the block, grid position (qx, qy) in a tx x ty token grid. The nine
 // scores are accumulated together, channel chunk outer and key inner, so a
 // thread has 18 independent FMA chains in flight; each chain adds its
-// channels in the same order as dot_head_s. Keys outside the grid get score
+// channels in the same order as dot_head (even channels in one, odd in the
+// other, then the two added), so every attention form gives the same bits.
+// Keys outside the grid get score
 // -inf and weight 0 (their zero-filled values then add exact zeros).
 template <int HD>
 __device__ __forceinline__ void attn_stencil_token(const uint8_t* sQ, const uint8_t* sK, const uint8_t* sV, int lx,
