@@ -374,7 +374,9 @@ __device__ __forceinline__ DF warp_sum_df(DF v) {
     return v;
 }
 // Block sums of two per-thread values in the fixed tree of warp_sum_df:
-// warps, then warp 0 over the warp totals; the totals as f64 in every thread.
+// warps, then warp 0 over the warp totals; the totals as f64 in thread 0 (the
+// only thread that uses them: f64 work in every thread would cost the FP64
+// pipe 512 times over).
 __device__ void block_sum_df2(DF a, DF b, double& A, double& B, DF* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     a = warp_sum_df(a);
@@ -391,14 +393,10 @@ __device__ void block_sum_df2(DF a, DF b, double& A, double& B, DF* red) {
         ta = warp_sum_df(ta);
         tb = warp_sum_df(tb);
         if (lane == 0) {
-            red[0] = ta;
-            red[32] = tb;
+            A = (double)ta.hi + (double)ta.lo;
+            B = (double)tb.hi + (double)tb.lo;
         }
     }
-    __syncthreads();
-    A = (double)red[0].hi + (double)red[0].lo;
-    B = (double)red[32].hi + (double)red[32].lo;
-    __syncthreads();
 }
 
 // Mass then energy projection (eval.rs:148-153 order; project.rs:33-54). One
@@ -409,11 +407,13 @@ __device__ void block_sum_df2(DF a, DF b, double& A, double& B, DF* red) {
 //   3. apply the scale; sum potential, kinetic -> energy of the stored state
 // Per-cell terms use the reference's f32 arithmetic (project.rs:9-19,
 // unfused). Each thread sums its few cells with Kahan compensation in f32;
-// the per-thread sums are combined in f64 (a fixed-order block tree, then the
-// cluster's partials in rank order through distributed shared memory), so
-// every CTA and every run sees the same totals. f64 is used only for these
-// combinations (the FP64 rate of this GPU is a small fraction of its FP32
-// rate, so per-cell f64 arithmetic would dominate the kernel).
+// the per-thread sums are combined in a fixed-order block tree in
+// double-f32, converted to f64, and the cluster's partials are added in f64
+// in segment order through distributed shared memory, so every CTA and every
+// run sees the same totals. f64 is used only for these combinations and for
+// the mass shift and energy scale, which thread 0 forms once per CTA and
+// shares (the FP64 rate of this GPU is a small fraction of its FP32 rate, so
+// f64 work per cell or per thread would dominate the kernel).
 constexpr int kProjCluster = 8;  // largest cluster (the launch picks 1..8 CTAs per instance)
 constexpr int kProjThreads = 512;
 constexpr int kProjSmemCells = 16384;  // 192 KB of state per CTA at most
@@ -489,6 +489,7 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
     extern __shared__ __align__(16) float sst[];
     __shared__ __align__(16) double red[64];  // the block trees' DF scratch (64 pairs)
     __shared__ double tot[4];
+    __shared__ float bc[2];  // the mass shift and the energy scale, formed once by thread 0
     cg::cluster_group cluster = cg::this_cluster();
     const int cs = (int)cluster.num_blocks();
     const int ii = blockIdx.x / cs, rank = (int)cluster.block_rank();
@@ -509,11 +510,22 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
     float* U = staged ? sst + cap : s + n + c0;
     float* V = staged ? sst + 2 * cap : s + 2 * n + c0;
     if (staged) {
-        // asynchronous copies: every thread's loads are in flight at once
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            cp_async4(H + i, s + c0 + i, true);
-            cp_async4(U + i, s + n + c0 + i, true);
-            cp_async4(V + i, s + 2 * n + c0 + i, true);
+        // asynchronous copies: every thread's loads are in flight at once,
+        // 16 bytes each where the state and the slice allow it
+        const bool v4 = ((reinterpret_cast<uintptr_t>(s) | (uintptr_t)n | (uintptr_t)c0 | (uintptr_t)m) & 3u) == 0 &&
+                        (reinterpret_cast<uintptr_t>(s) & 15u) == 0;
+        if (v4) {
+            for (int i = 4 * threadIdx.x; i < m; i += 4 * blockDim.x) {
+                cp_async16(H + i, s + c0 + i, true);
+                cp_async16(U + i, s + n + c0 + i, true);
+                cp_async16(V + i, s + 2 * n + c0 + i, true);
+            }
+        } else {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                cp_async4(H + i, s + c0 + i, true);
+                cp_async4(U + i, s + n + c0 + i, true);
+                cp_async4(V + i, s + 2 * n + c0 + i, true);
+            }
         }
         cp_async_wait_all();
         __syncthreads();
@@ -537,7 +549,7 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
                     if (nv > 1) b.add(tb);
                 }
             }
-            double A, B;
+            double A = 0.0, B = 0.0;
             block_sum_df2(DF{a.s, -a.c}, DF{b.s, -b.c}, A, B, reinterpret_cast<DF*>(red));
             if (threadIdx.x == 0) {
                 mine[1 + 2 * (k - k0)] = A;
@@ -558,7 +570,9 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
         M = tot[0];
     }
     // pass 2: mass shift, then potential and kinetic energy
-    const float delta = (flags & 1u) ? (float)(S.mass0 - M / (double)n) : 0.0f;
+    if (threadIdx.x == 0) bc[0] = (flags & 1u) ? (float)(S.mass0 - M / (double)n) : 0.0f;
+    __syncthreads();
+    const float delta = bc[0];
     reduce(1, 2, [&](int i, float& pot, float& kin) {
         float h = H[i];
         if (flags & 1u) {
@@ -578,12 +592,17 @@ projection_kernel(Dims d, const InstDev* inst, ProjSlot* slots, int init, int ca
     } else {
         // pass 3: energy scale of (u, v), then the energy of the stored state
         if (flags & 2u) {
-            const double bound = prev * (double)d.energy_r_max;
-            double budget = bound - P;
-            if (!(budget > 0.0)) budget = 0.0;
-            double sc = sqrt(budget / (K > 1e-12 ? K : 1e-12));
-            sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
-            const float s32 = (float)sc;
+            double sc = 1.0;
+            if (threadIdx.x == 0) {
+                const double bound = prev * (double)d.energy_r_max;
+                double budget = bound - P;
+                if (!(budget > 0.0)) budget = 0.0;
+                sc = sqrt(budget / (K > 1e-12 ? K : 1e-12));
+                sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc);
+                bc[1] = (float)sc;
+            }
+            __syncthreads();
+            const float s32 = bc[1];
             reduce(2, 2, [&](int i, float& pot, float& kin) {
                 float u = __fadd_rn(__fmul_rn(U[i], d.norm_std[1]), d.norm_mean[1]);
                 float v = __fadd_rn(__fmul_rn(V[i], d.norm_std[2]), d.norm_mean[2]);
