@@ -29,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -613,8 +614,10 @@ def main():
     for _ in range(args.warmup):
         batch.rollout(dev_items, device=True, stream=sptr)
     barrier()
-    clocks = Clocks(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv")
-    (ROOT / "gpurun_out").mkdir(exist_ok=True)
+    # the raw nvidia-smi samples go to $JC_BENCH_OUT (default: the system's temp folder)
+    out_dir = Path(os.environ.get("JC_BENCH_OUT") or tempfile.gettempdir())
+    out_dir.mkdir(parents=True, exist_ok=True)
+    clocks = Clocks(out_dir / f"clocks_rank{rank}.csv")
     with clocks:
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
