@@ -548,6 +548,25 @@ def cpu_sample(cfg, t, x0, meta, ticks: int):
     return cfg.nx * cfg.ny * ticks / dt, oracle.get_threads(), dt
 
 
+def max_over_ranks(v: float, world: int, device: str) -> float:
+    """The largest of the ranks' values (a step time: the job ends with its
+    slowest rank), by an all-reduce over the default process group."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, ms: float) -> float:
+    """Units per second of the whole job: every rank processes the same
+    number of units (replicas, weak scaling) in at most `ms` per step."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -625,13 +644,8 @@ def main():
             batch.rollout(dev_items, device=True, stream=sptr)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    work = B * cells * H * world
-    value = work / (ms / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, "cuda")
+    value = whole_job_rate(B * cells * H, world, ms)
 
     # end to end through the C ABI with host buffers
     for _ in range(2):
@@ -641,11 +655,7 @@ def main():
     for _ in range(args.steps):
         batch.rollout(host_items)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, "cuda")
     h2d = B * (x0s[0].nbytes + meta.nbytes)
     d2h = B * (x0s[0].nbytes + 32)
 
@@ -711,7 +721,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32" if prec == engine.FP32 else "bf16", "data": "synthetic",
                 "config": config_dict(args, cfg),
-                "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "e2e": {"value": whole_job_rate(B * cells * H, world, 1e3 * e2e_s), "unit": UNIT,
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
                                "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,

@@ -1,7 +1,8 @@
 """The bench's JSON line contract, checked through its CPU reference arm (the
 oracle's f32 rollout on the host cores): one line with the metric, the
 timing keys, the configuration and the CPU baseline; ranks other than 0 of a
-multi-process launch print nothing."""
+multi-process launch print nothing. The multi-rank timing (the slowest rank's
+step, whole-job units) runs on two gloo processes."""
 
 import json
 import os
@@ -40,3 +41,39 @@ def test_reference_arm_prints_one_contract_line():
 
 def test_reference_arm_other_ranks_print_nothing():
     assert _run({"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def _ranks_worker(rank, world, port, q):
+    import importlib.util
+
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    spec = importlib.util.spec_from_file_location("bench_mod", ROOT / "bench.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    ms = b.max_over_ranks(10.0 + 5.0 * rank, world, "cpu")  # rank 1 is the slower one
+    q.put((rank, ms, b.whole_job_rate(1000.0, world, ms)))
+    dist.destroy_process_group()
+
+
+def test_two_ranks_take_the_slowest_step_and_count_every_rank():
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_ranks_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    # both ranks see the slowest rank's 15 ms; 2 x 1000 units in 15 ms
+    assert got == [(0, 15.0, 2000.0 / 0.015), (1, 15.0, 2000.0 / 0.015)]
