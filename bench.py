@@ -359,8 +359,9 @@ def accuracy_c3(ticks=(10, 25, 50)):
     """Config: 256x256 checkpoints at dim 128 / 4 layers (seed 0) and dim 256 /
     6 layers (seed 1), 8 drops, mass + energy projection each tick. Per-field
     normwise error (max|a - b| / max|b|) of the BF16 and the FP32 path against
-    the f64 oracle for one forward and along a 50-tick rollout, and the largest
-    relative energy violation of each."""
+    the f64 oracle for one forward and along a 50-tick rollout, the largest
+    relative energy violation of each, and |E - E_oracle| / E_oracle at the
+    reported ticks."""
     from jacobi2000_gb300 import engine
     from jacobi2000_gb300.checkpoint import parse_config, synthetic_checkpoint, write_safetensors_bytes, meta_of
     from jacobi2000_gb300.ic import random_drops
@@ -393,9 +394,11 @@ def accuracy_c3(ticks=(10, 25, 50)):
                 fwd = m.forward(x0, meta)
                 final, e, traj = m.rollout(x0, meta, H, me, trajectory=True)
             viol = float(np.max(np.maximum((e[1:] - e[:-1] * cfg.energy_r_max) / e[:-1], 0.0)))
+            e, e64a = np.asarray(e, np.float64), np.asarray(e64, np.float64)
             row["paths"][name] = {"forward": max(err(fwd, want_fwd)),
                                   "rollout": {str(k): max(err(traj[k], traj64[k])) for k in ticks},
-                                  "max_energy_violation": viol}
+                                  "max_energy_violation": viol,
+                                  "energy_rel_diff": {str(k): float(abs(e[k] - e64a[k]) / abs(e64a[k])) for k in ticks}}
         out.append(row)
     return {"measure": "max over fields of max|a - b| / max|b| against the f64 oracle", "ticks": list(ticks),
             "cases": out}
