@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--layers", type=int, default=4)
     ap.add_argument("--cpu-sample-ticks", type=int, default=300,
                     help="ticks of one instance timed on the host cores for cpu_baseline (about 10 s)")
+    ap.add_argument("--cpu-sample-ticks-1t", type=int, default=20,
+                    help="ticks of the same instance timed on one host thread (about 10 s); 0 to skip")
     ap.add_argument("--ref-step-ticks", type=int, default=50,
                     help="ticks of one instance per step of the --impl reference arm")
     ap.add_argument("--served-rates", default="100,400,1600",
@@ -537,12 +539,13 @@ def eval_bench(args, steps=3):
     return out
 
 
-def cpu_sample(cfg, t, x0, meta, ticks: int):
+def cpu_sample(cfg, t, x0, meta, ticks: int, threads: int = 0):
     """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
-    masked scan) on all host cores, over `ticks` ticks of one instance."""
+    masked scan) over `ticks` ticks of one instance, on `threads` host
+    threads (0: all host cores)."""
     from oracle import oracle
 
-    oracle.set_threads(os.cpu_count() or 1)
+    oracle.set_threads(threads or os.cpu_count() or 1)
     oracle.set_attention_mode("scan")
     m = oracle.OracleModel(cfg, t)
     t0 = time.perf_counter()
@@ -718,6 +721,10 @@ def main():
         v, cores, dt = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"1 instance x {args.cpu_sample_ticks} tick(s), {dt:.1f} s"}
+        if args.cpu_sample_ticks_1t > 0:
+            v1, _, dt1 = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks_1t, threads=1)
+            cpu["one_thread"] = {"value": v1, "unit": UNIT, "cores": 1,
+                                 "sample": f"1 instance x {args.cpu_sample_ticks_1t} tick(s), {dt1:.1f} s"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
