@@ -255,21 +255,26 @@ jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out);
 jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n,
                            int32_t device_pointers, char* report, size_t cap);
 
-/* The forward pass of jc_forward_device, with f32 arithmetic, for callers that
- * cannot allocate device memory at call time: code recording a CUDA stream
- * capture (cudaMalloc cannot be captured and breaks a global or thread-local
- * capture) and processes whose own pool allocator owns the whole device.
- * This entry point has no counterpart in the reference. It allocates nothing:
- * every intermediate buffer lives in one fixed 12 MiB device array inside
- * the library, which every GPU that loads the library holds until the process
- * exits. Grids whose buffers exceed 12 MiB are refused with JC_LIMIT (the
- * dim 128, 4-layer model fits grids up to 128 x 128 cells). All calls share
- * that array: calls that overlap on the GPU (on different streams, or from
- * different threads) race and corrupt each other's results; serialise them.
- * The first call on each device looks up the array's device address, so make
- * that first call before any stream capture begins. Pointers are device
- * pointers; `stream` is a cudaStream_t (null = the legacy default stream);
- * the call enqueues and returns. */
+/* The forward pass of jc_forward_device for callers that cannot allocate
+ * device memory when they run the model: a host application whose own pool
+ * allocator has reserved the whole device up front (an extra cudaMalloc then
+ * fails or fragments that pool), or a plugin that is handed device buffers
+ * by its host and must not grow the process's footprint behind its back.
+ * This entry point has no counterpart in the reference. It allocates
+ * nothing: every intermediate buffer lives in one fixed 12 MiB device array
+ * inside the library, which every GPU that loads the library holds until the
+ * process exits. It always runs the FP32 kernels (f32 weights and
+ * activations), for a model created with either precision. Grids whose
+ * buffers exceed 12 MiB are refused with JC_LIMIT (the dim 128, 4-layer
+ * model fits grids up to 128 x 128 cells). All calls share that array:
+ * calls that overlap on the GPU (on different streams, or from different
+ * threads) race and corrupt each other's results; serialise them. The first
+ * call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture begins. cudaDeviceReset discards the array with the
+ * context: do not use the library's handles across a reset. Pointers are
+ * device pointers; `stream` is a cudaStream_t (null = the legacy default
+ * stream); the call enqueues and returns. */
 jc_status jc_forward_device_noalloc(jc_model* m, const float* d_state, const float* d_meta,
                                     float* d_increment, void* stream);
 
@@ -419,6 +424,18 @@ void jc_roundtrip_destroy(jc_roundtrip* r);
  * direction. rows: [n_horizons][n]. */
 jc_status jc_roundtrip_run(jc_roundtrip* r, const jc_drop* drops, int32_t n, const int32_t* horizons,
                            int32_t n_horizons, uint32_t flags, jc_roundtrip_row* rows);
+
+/* Self-test of the bounded device-side waits, with no counterpart in the
+ * reference (whose error surface for a stalled device is
+ * lean_runtime::Error::Poll, crates/lean-runtime/src/error.rs:6-13). Every
+ * spin-wait in this library's kernels gives up after a time limit, sets an
+ * error flag and returns, and the call that launched it reports
+ * JC_DEVICE_TIMEOUT. This runs the same mbarrier wait in a one-CTA kernel
+ * with a limit of limit_us microseconds (1 .. 2,000,000): with satisfy = 0
+ * nothing ever arrives on the barrier, the wait runs out and the call
+ * returns JC_DEVICE_TIMEOUT with the kernel finished and the context usable;
+ * with satisfy = 1 the barrier completes and the call returns JC_OK. */
+jc_status jc_selftest_device_wait(int32_t satisfy, uint32_t limit_us);
 
 /* Thread-local description of the last failure on this thread ("" if none). */
 const char* jc_last_error(void);

@@ -22,7 +22,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contrac
          "-I", str(ROOT / "include")]
 
 SOURCES = ["fp32_path.cu", "bf16_path.cu", "runtime.cu", "server.cu", "recon.cu", "noalloc.cu", "evaluate.cu",
-           "roundtrip.cu", "capi.cpp"]
+           "roundtrip.cu", "selftest.cu", "capi.cpp"]
 
 
 def _deps() -> list[Path]:

@@ -160,6 +160,10 @@ jc_status jc_forward_device_noalloc(jc_model* m, const float* d_state, const flo
     return guard([&] { jc::forward_noalloc(*m->m, d_state, d_meta, d_increment, (cudaStream_t)stream); });
 }
 
+jc_status jc_selftest_device_wait(int32_t satisfy, uint32_t limit_us) {
+    return guard([&] { jc::selftest_device_wait(satisfy, limit_us); });
+}
+
 jc_status jc_batch_create(jc_model* const* models, int32_t n_models, int32_t max_instances, int64_t max_cells,
                           jc_batch** out) {
     if (!out) return fail(JC_BAD_ARGUMENT, "out is null");

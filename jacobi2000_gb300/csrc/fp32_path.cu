@@ -5,6 +5,7 @@
 // attention softmax), so results agree with the reference's f32 CPU path to
 // rounding.
 #include <algorithm>
+#include <atomic>
 #include <stdexcept>
 #include <string>
 
@@ -69,6 +70,19 @@ KernelTimer::~KernelTimer() {
 
 static void cuda_check_attr(cudaError_t e) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+}
+
+// Raises a kernel's dynamic shared-memory limit on the current device, once
+// per device: the attribute belongs to the device's context, so a process
+// that uses several GPUs sets it on each. `done` holds one bit per device.
+template <class K>
+static void set_smem_per_device(K kernel, int bytes, std::atomic<unsigned long long>& done) {
+    int dev = 0;
+    cuda_check_attr(cudaGetDevice(&dev));
+    const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (done.load() & bit)) return;
+    cuda_check_attr(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    done.fetch_or(bit);
 }
 
 static void check_launch(const char* what) {
@@ -694,12 +708,8 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
                 cudaStream_t s) {
     KScope k(name, s);
     if (d.C != 3 || d.HD != 32) throw std::runtime_error("conv2 is built for 3 channels and a cell-head width of 32");
-    static bool attr = false;
-    if (!attr) {
-        cuda_check_attr(cudaFuncSetAttribute(f32k::conv2_step_kernel<3, 32>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, f32k::kConv2Smem));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    set_smem_per_device(f32k::conv2_step_kernel<3, 32>, f32k::kConv2Smem, attr);
     if (!w.c2p) throw std::runtime_error("conv2 weights missing");
     const cudaError_t e = launch_pdl(f32k::conv2_step_kernel<3, 32>, dim3(p.n_tiles), dim3(f32k::kConv2Threads),
                                      f32k::kConv2Smem, s, 1u, c1, *w.c2p, (const InstDev*)p.inst, p.n_inst, mode);
@@ -709,12 +719,8 @@ void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack&
 
 void projection(const Dims& d, const Pack& p, int init, cudaStream_t s) {
     KScope k("projection", s);
-    static bool attr = false;
-    if (!attr) {
-        cuda_check_attr(cudaFuncSetAttribute(f32k::projection_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             200 * 1024));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    set_smem_per_device(f32k::projection_kernel, 200 * 1024, attr);
     // cluster size: the smallest whose slices fit in shared memory, and about
     // one CTA per SM (152 here) when the instances are few; the sums do not
     // depend on it (segment totals in segment order)

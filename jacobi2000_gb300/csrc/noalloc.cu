@@ -1,14 +1,15 @@
 // A forward pass that allocates nothing, for callers that cannot call
-// cudaMalloc: code running inside a CUDA stream capture (cudaMalloc is not a
-// capturable call, and under the global or thread-local capture modes it
-// invalidates the capture), and processes that hand the whole device to their
-// own pool allocator, where an extra cudaMalloc fails or fragments the pool.
+// cudaMalloc when they run the model: host applications whose own pool
+// allocator reserved the whole device up front (an extra cudaMalloc fails or
+// fragments the pool), and plugins that work only in the buffers their host
+// hands them.
 //
 // All intermediate buffers of the FP32 forward (the same kernels as
 // jc_forward_device) live in one file-scope device array of kNoAllocBytes.
 // Every GPU that loads this library holds that array until the process exits.
 // The model's weights were allocated when the model was created; this call
-// itself allocates no device or host memory.
+// itself allocates no device or host memory. It runs the FP32 kernels for a
+// model of either precision (a BF16 model keeps its f32 weights too).
 #include <mutex>
 #include <string>
 

@@ -295,16 +295,18 @@ void Workspace::alloc(DeviceArena& a, const Dims& d, int rows, long long cells, 
     metas = a.alloc_n<float>((size_t)inst * 64);
 }
 
-void Workspace::check_timeout(cudaStream_t s) const {
+void check_wait_flag(int* flag, cudaStream_t s) {
     int e = 0;
-    cuda_check(cudaMemcpyAsync(&e, base.err, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag", JC_MAP);
+    cuda_check(cudaMemcpyAsync(&e, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag", JC_MAP);
     cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
     if (e) {
-        cudaMemsetAsync(base.err, 0, sizeof(int), s);
+        cudaMemsetAsync(flag, 0, sizeof(int), s);
         cudaStreamSynchronize(s);
         throw Error(JC_DEVICE_TIMEOUT, "a device-side wait exceeded its time limit; results of this call are invalid");
     }
 }
+
+void Workspace::check_timeout(cudaStream_t s) const { check_wait_flag(base.err, s); }
 
 Pack Workspace::view(const Dims& d, int inst_base, int n, int row_base, int rows, long long cell_base,
                      long long cells, int tiles, int ttiles, int ctiles) const {

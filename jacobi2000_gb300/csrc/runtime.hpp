@@ -86,6 +86,16 @@ struct Workspace {
     void check_timeout(cudaStream_t s) const;
 };
 
+// Reads a device-side wait flag (set by a kernel whose bounded wait gave up)
+// after the work on `s`; throws JC_DEVICE_TIMEOUT and clears the flag when
+// it is set.
+void check_wait_flag(int* flag, cudaStream_t s);
+
+// Device-side wait self-test (selftest.cu): one CTA waits on an mbarrier
+// with a limit of limit_us microseconds; with satisfy = 0 nothing ever
+// arrives, so the wait gives up and the call reports JC_DEVICE_TIMEOUT.
+void selftest_device_wait(int satisfy, unsigned limit_us);
+
 // Tile counts of one instance's grids.
 int cell_tiles(int nx, int ny);   // 16x16 cells
 int conv_tiles(int w, int h);     // 8x16 positions

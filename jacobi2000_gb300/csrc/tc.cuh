@@ -59,16 +59,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Waits for the phase with the given parity to complete. Returns false (and
-// sets *err) when the wait exceeds kWaitNs; a wait that already failed in
-// this CTA returns false at once.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, volatile int* cta_failed) {
+// sets *err) when the wait exceeds limit_ns (kWaitNs unless a caller passes
+// a shorter limit); a wait that already failed in this CTA returns false at
+// once.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, volatile int* cta_failed,
+                                          unsigned long long limit_ns = kWaitNs) {
     if (*cta_failed) return false;
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = globaltimer();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*cta_failed) return false;
-        if (globaltimer() - t0 > kWaitNs) {
+        if (globaltimer() - t0 > limit_ns) {
             *cta_failed = 1;
             atomicExch(err, 1);
             return false;

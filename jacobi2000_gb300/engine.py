@@ -276,7 +276,7 @@ def _declare_batch(L):
 
 
 EXPORTED += ["jc_batch_create", "jc_batch_destroy", "jc_batch_rollout", "jc_batch_profile",
-             "jc_forward_device_noalloc"]
+             "jc_forward_device_noalloc", "jc_selftest_device_wait"]
 
 
 class Batch:

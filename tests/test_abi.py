@@ -24,6 +24,14 @@ def test_header_symbols_are_exported():
     assert declared >= set(engine.EXPORTED)
 
 
+def test_device_wait_selftest_validates_its_limit():
+    # argument checks happen on the host, before any device work
+    L = engine.load_library()
+    L.jc_selftest_device_wait.argtypes = [C.c_int32, C.c_uint32]
+    assert engine.STATUS[L.jc_selftest_device_wait(0, 0)] == "BAD_ARGUMENT"
+    assert engine.STATUS[L.jc_selftest_device_wait(0, 3_000_000)] == "BAD_ARGUMENT"
+
+
 def _create(st: bytes, cj: str):
     L = engine.load_library()
     h = C.c_void_p()
