@@ -1,24 +1,37 @@
-"""Throughput of the shallow-water transformer rollout on GB300.
+"""Throughput of the shallow-water transformer on GB300, served.
 
-Workload (default): B instances of a 128x128 grid, model20-shaped checkpoint
-(dim 128, 4 layers, 4 heads, stencil r1 d1, random init seed 0), 8 seeded
-Gaussian drops per instance (amplitude U[0.02, 0.15], sigma U[2, 6] cells,
-periodic images), a 50-tick rollout with mass and energy projection per
-instance. One step = one batched rollout of all B instances. Metric:
-cell-ticks/s = sum over instances of nx * ny * ticks / seconds.
+Workload (the metric's configuration): a request loop with continuous
+batching on one GPU. Requests arrive as a Poisson stream (rates swept over
+10-2000 req/s); grid side log-uniform in [32, 256] rounded to a multiple of 4
+(one checkpoint per side, dim 128, 4 layers, random init: a forward family,
+seed 0, and a reverse family, seed 1); horizon U[10, 50] ticks; 1/3 forward,
+1/3 rewind, 1/3 reconstruct (2% of the space-time cells known, 4 Jacobi
+sweeps); mass and energy projection each tick; admission at 80% of HBM.
+Metric: useful cell-ticks/s = sum over requests of nx * ny * horizon /
+seconds. One step = one served run of N requests arriving at 2000 req/s (the
+saturating rate).
 
-* ``value``: device-resident inputs (x0/meta already in HBM), timed with CUDA
-  events on the launching stream.
-* ``e2e``: the same rollouts through the C ABI with host buffers; host->device
-  copies of x0/meta and device->host copies of the final states and energies
-  are inside the timed region.
-* ``fp32_plain``: the FP32 single-request path, one rollout at a time.
-* ``--impl reference``: the reference's CPU forward pass and projections
-  (the C restatement of crates/engine/src/cpu.rs and project.rs, with the
-  reference's own O(T^2) masked attention scan) on the host cores.
+* ``value``: the BF16 served form with inputs already in device memory
+  (requests carry device pointers), timed on the device: CUDA events on the
+  server's stream from the start of its first iteration to the end of its
+  last, summed over the timed steps.
+* ``e2e``: the same runs through the C ABI with host buffers
+  (jc_server_submit / jc_server_wait): wall clock from the first arrival to
+  the last result in host memory, host->device and device->host copies
+  inside.
+* ``served.rates``: throughput and p50/p99 latency per arrival rate (host
+  buffers).
+* ``fp32_plain``: the plain FP32 kernel path, one request at a time; and
+  ``served_vs_plain`` = value / its throughput.
+* ``batched``: 64 instances of a 128x128 grid x 50 ticks in one batch call;
+  the per-kernel table and the roofline of the dominant kernel come from it.
+* ``--impl reference``: the reference's CPU forward pass and projections (the
+  C restatement of crates/engine/src/cpu.rs and project.rs, with the
+  reference's own O(T^2) masked attention scan) on a bounded sample of the
+  same requests, on the host cores.
 
-Under torchrun each rank runs its own B instances (no exchange step):
-weak scaling, barrier + max over ranks.
+Under torchrun each rank serves its own requests (no exchange step): weak
+scaling, barrier + max over ranks.
 """
 
 from __future__ import annotations
@@ -49,22 +62,25 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
+    ap.add_argument("--dim", type=int, default=128)
+    ap.add_argument("--layers", type=int, default=4)
+    ap.add_argument("--requests", type=int, default=400,
+                    help="served requests per step at the saturating rate")
+    ap.add_argument("--sweep-seconds", type=float, default=3.0,
+                    help="arrival time per rate of the 10-2000 req/s sweep (at least 40 requests per rate)")
+    ap.add_argument("--plain-requests", type=int, default=120,
+                    help="requests of the FP32 one-request-at-a-time run")
+    ap.add_argument("--cpu-requests", type=int, default=12,
+                    help="requests of the served workload in the CPU sample (each at most 5 ticks)")
+    ap.add_argument("--ref-requests", type=int, default=4,
+                    help="requests of the served workload per step of the --impl reference arm")
+    ap.add_argument("--ref-horizon", type=int, default=5,
+                    help="ticks of each request run by the CPU sample (the rest of its horizon is not run)")
+    # the batched extra: B instances of one grid, one rollout per step
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--side", type=int, default=128)
     ap.add_argument("--ticks", type=int, default=50)
-    ap.add_argument("--dim", type=int, default=128)
-    ap.add_argument("--layers", type=int, default=4)
-    ap.add_argument("--cpu-sample-ticks", type=int, default=300,
-                    help="ticks of one instance timed on the host cores for cpu_baseline (about 10 s)")
-    ap.add_argument("--cpu-sample-ticks-1t", type=int, default=20,
-                    help="ticks of the same instance timed on one host thread (about 10 s); 0 to skip")
-    ap.add_argument("--ref-step-ticks", type=int, default=50,
-                    help="ticks of one instance per step of the --impl reference arm")
-    ap.add_argument("--served-rates", default="100,400,1600",
-                    help="request arrival rates (req/s) of the served-form run; empty to skip")
-    ap.add_argument("--served-requests", type=int, default=240)
-    ap.add_argument("--served-fp32-requests", type=int, default=24)
+    ap.add_argument("--no-sweep", action="store_true", help="skip the arrival-rate sweep")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-task batch measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 256x256 error report against the f64 oracle")
     ap.add_argument("--no-eval", action="store_true", help="skip the eval-metrics measurement")
@@ -80,14 +96,6 @@ def workload(args):
     rank = int(os.environ.get("RANK", "0"))
     x0s = [random_drops(cfg, seed=rank * 100_000 + i) for i in range(args.instances)]
     return t, cj, cfg, x0s, meta_of(cfg)
-
-
-def config_dict(args, cfg):
-    return {"workload": f"rollout {args.instances}x {args.side}x{args.side} grids, {args.ticks} ticks, "
-                        f"mass+energy projection, 8 drops/instance",
-            "model": f"jacobi2000 dim {args.dim}, {args.layers} layers, 4 heads, stencil r1 d1, seed 0",
-            "grid": [args.side, args.side], "instances_per_step": args.instances, "ticks": args.ticks,
-            "l2": "per-tick working set > 129 MB L2 (no flush needed)", "parallelism": "replicas"}
 
 
 class Clocks:
@@ -178,121 +186,217 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
     return None, None
 
 
-SERVED_SIDES = [32, 64, 96, 128, 160, 192, 224, 256]
+# ---- the served workload (the metric's configuration) ------------------------------------
+
+C5_SIDES = list(range(32, 257, 4))  # grid sides: log-uniform in [32, 256], rounded to a multiple of 4
+C5_RATES = [10.0, 30.0, 100.0, 300.0, 1000.0, 2000.0]
+C5_SWEEPS = 4         # reconstruct: Jacobi sweeps (tolerance 0: every sweep runs)
+C5_KNOWN = 0.02       # reconstruct: fraction of space-time cells known
+C5_MAX_CELLS = 8 << 20
+C5_HBM = 0.8
 
 
-def served_requests(rng, n, rate, cfgs, volumes, masks):
-    """Poisson arrivals at `rate`; grid side log-uniform in [32, 256] rounded
-    to a multiple of 32; horizon U[10, 50]; tasks 1/3 forward (initial state
-    known), 1/3 rewind (final state known), 1/3 reconstruct (2% of the
-    space-time cells known). Returns (arrival_s, task, grid, ticks, x, known)."""
+class C5:
+    """Requests of the serving configuration: Poisson arrivals at `rate`;
+    grid side log-uniform in [32, 256] rounded to a multiple of 4; horizon
+    U[10, 50] ticks; tasks 1/3 forward (initial state known), 1/3 rewind
+    (final state known), 1/3 reconstruct (2% of the space-time cells known as
+    sensor readings of a drop field, the rest blank). Inputs are made from the
+    request's own seed, so a request list is reproducible."""
+
+    def __init__(self, cfgs):
+        self.cfgs = cfgs
+        self._states = {}
+
+    @staticmethod
+    def draw(seed: int, n: int, rate: float):
+        rng = np.random.default_rng(seed)
+        out, t = [], 0.0
+        for _ in range(n):
+            t += rng.exponential(1.0 / rate)
+            side = float(np.exp(rng.uniform(np.log(32.0), np.log(256.0))))
+            g = int(np.clip(round(side / 4.0) * 4, 32, 256) - 32) // 4
+            out.append({"arrival": t, "task": int(rng.integers(0, 3)), "g": g, "ticks": int(rng.integers(10, 51)),
+                        "seed": int(rng.integers(1 << 30))})
+        return out
+
+    def side(self, r):
+        return C5_SIDES[r["g"]]
+
+    def state(self, g: int, k: int):
+        from jacobi2000_gb300.ic import random_drops
+
+        key = (g, k % 2)
+        if key not in self._states:
+            self._states[key] = random_drops(self.cfgs[g], seed=1000 * g + k % 2)
+        return self._states[key]
+
+    def inputs(self, r):
+        """(x, known): x is [3, n, n] (forward / rewind) or the values [H+1, 3,
+        n, n] (reconstruct, zero where unknown) with its mask known [H+1, n, n]."""
+        from jacobi2000_gb300 import engine
+
+        if r["task"] != engine.TASK_RECONSTRUCT:
+            return self.state(r["g"], r["seed"]), None
+        n, H = self.side(r), r["ticks"]
+        known = (np.random.default_rng(r["seed"]).random((H + 1, n, n)) < C5_KNOWN).astype(np.uint8)
+        vals = np.where(known[:, None], self.state(r["g"], r["seed"])[None], np.float32(0.0)).astype(np.float32)
+        return vals, known
+
+    def useful(self, reqs):
+        return sum(self.side(r) ** 2 * r["ticks"] for r in reqs)
+
+    def work(self, reqs):
+        """Forward cell-ticks the requests cost (a reconstruct sweep steps 2H slices)."""
+        from jacobi2000_gb300 import engine
+
+        return sum(self.side(r) ** 2 * r["ticks"] * (2 * C5_SWEEPS if r["task"] == engine.TASK_RECONSTRUCT else 1)
+                   for r in reqs)
+
+
+def c5_models(args, precision):
+    """The forward and the reverse checkpoint family (seeds 0 and 1; one model
+    per grid side, every tensor but `pos` shared) at `precision`."""
     from jacobi2000_gb300 import engine
-    from jacobi2000_gb300.ic import random_drops
+    from jacobi2000_gb300.checkpoint import synthetic_family, write_safetensors_bytes
 
-    out, t = [], 0.0
-    for k in range(n):
-        t += rng.exponential(1.0 / rate)
-        side = float(np.exp(rng.uniform(np.log(32), np.log(256))))
-        g = int(np.argmin([abs(side - s) for s in SERVED_SIDES]))
-        ticks = int(rng.integers(10, 51))
-        task = int(rng.integers(0, 3))
-        if task == engine.TASK_RECONSTRUCT:
-            x, known = volumes[g][: ticks + 1], masks[g][: ticks + 1]
-        else:
-            x, known = random_drops(cfgs[g], seed=int(rng.integers(1 << 30))), None
-        out.append((t, task, g, ticks, x, known))
-    return out
+    fams = [synthetic_family(args.dim, args.layers, seed, C5_SIDES) for seed in (0, 1)]
+    return [[engine.Model.from_bytes(write_safetensors_bytes(f[(s, s)][0]), f[(s, s)][1], precision)
+             for s in C5_SIDES] for f in fams]
 
 
-def run_served(srv, reqs, metas, sweeps, concurrent=True):
-    """Submits at the arrival times (concurrent) or one request at a time
-    after the previous result (sequential). Returns throughput and latency
-    percentiles, latency measured from the scheduled arrival."""
+def c5_configs(args):
+    from jacobi2000_gb300.checkpoint import parse_config, synthetic_family
+
+    fam = synthetic_family(args.dim, args.layers, 0, C5_SIDES)
+    return [parse_config(fam[(s, s)][1], fam[(s, s)][0]) for s in C5_SIDES]
+
+
+def run_served(srv, wl, reqs, metas, device=False, concurrent=True):
+    """Submits `reqs` at their arrival times (concurrent) or one after the
+    previous result (sequential) and collects every result. Host mode: host
+    buffers in and out through jc_server_submit / jc_server_wait. Device mode:
+    inputs already in device memory, results copied to device memory
+    (JC_REQUEST_DEVICE_BUFFERS). Latency per request is the server's submit to
+    completion time plus how late the submission was."""
     import threading
 
     from jacobi2000_gb300 import engine
 
+    ins = [wl.inputs(r) for r in reqs]
+    h2d = sum(x.nbytes + (k.nbytes if k is not None else 0) + metas[r["g"]].nbytes for r, (x, k) in zip(reqs, ins))
+    d2h = sum(x.nbytes for x, _ in ins)
+    dev = None
+    if device:
+        import torch
+
+        dev = [(torch.from_numpy(x).cuda(), torch.from_numpy(k).cuda() if k is not None else None,
+                torch.from_numpy(metas[r["g"]]).cuda(), torch.empty(x.shape, device="cuda"))
+               for r, (x, k) in zip(reqs, ins)]
+        torch.cuda.synchronize()
+    srv.reset_stats()
     lat = [None] * len(reqs)
-    cell_ticks = sum(SERVED_SIDES[g] ** 2 * ticks for _, _, g, ticks, _, _ in reqs)
-    t0 = time.perf_counter()
     ids = [None] * len(reqs)
+    late = [0.0] * len(reqs)
 
-    def collect():
-        for k, (arr, task, g, ticks, _, _) in enumerate(reqs):
-            while ids[k] is None:
-                time.sleep(0.0002)
-            srv.wait(ids[k], task, g, ticks, timeout=600)
-            lat[k] = time.perf_counter() - (t0 + arr)
+    def submit(k, r):
+        x, known = ins[k]
+        if device:
+            dx, dk, dm, _ = dev[k]
+            return srv.submit_device(r["task"], r["g"], dx.data_ptr(), dm.data_ptr(), r["ticks"],
+                                     known_ptr=dk.data_ptr() if dk is not None else None, max_sweeps=C5_SWEEPS,
+                                     tol=0.0)
+        return srv.submit(r["task"], r["g"], x, metas[r["g"]], r["ticks"], known=known, max_sweeps=C5_SWEEPS, tol=0.0)
 
+    def collect(k, r):
+        if device:
+            o = dev[k][3]
+            info = srv.wait_device(ids[k], o.data_ptr(), o.numel(), timeout=600)
+        else:
+            _, info = srv.wait(ids[k], r["task"], r["g"], r["ticks"], timeout=600)
+        lat[k] = info["latency_s"] + late[k]
+
+    t0 = time.perf_counter()
     if concurrent:
-        th = threading.Thread(target=collect)
+        def collector():
+            for k, r in enumerate(reqs):
+                while ids[k] is None:
+                    time.sleep(0.0002)
+                collect(k, r)
+
+        th = threading.Thread(target=collector)
         th.start()
-        for k, (arr, task, g, ticks, x, known) in enumerate(reqs):
-            delay = t0 + arr - time.perf_counter()
+        for k, r in enumerate(reqs):
+            delay = t0 + r["arrival"] - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
-            ids[k] = srv.submit(task, g, x, metas[g], ticks, known=known, max_sweeps=sweeps, tol=0.0)
+            late[k] = max(0.0, time.perf_counter() - (t0 + r["arrival"]))
+            ids[k] = submit(k, r)
         th.join()
     else:
-        for k, (arr, task, g, ticks, x, known) in enumerate(reqs):
-            delay = t0 + arr - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            rid = srv.submit(task, g, x, metas[g], ticks, known=known, max_sweeps=sweeps, tol=0.0)
-            srv.wait(rid, task, g, ticks, timeout=600)
-            lat[k] = time.perf_counter() - (t0 + arr)
-    span = time.perf_counter() - t0
+        for k, r in enumerate(reqs):
+            ids[k] = submit(k, r)
+            collect(k, r)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    useful = wl.useful(reqs)
     lat_ms = np.array(lat) * 1e3
-    return {"requests": len(reqs), "cell_ticks_per_s": cell_ticks / span, "span_s": span,
-            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99))}
+    return {"requests": len(reqs), "useful_cell_ticks": useful, "work_cell_ticks": wl.work(reqs),
+            "wall_s": wall, "device_span_s": st["device_span_s"], "cell_ticks_per_s_wall": useful / wall,
+            "cell_ticks_per_s_device": useful / st["device_span_s"] if st["device_span_s"] > 0 else None,
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "iterations": st["iterations"], "launches": st["launches"], "h2d_bytes": h2d, "d2h_bytes": d2h}
 
 
-def served_bench(args):
-    """Config: Poisson arrivals, three task types, sides 32-256, BF16 served
-    form with continuous batching vs the FP32 one-request-at-a-time path."""
+def cpu_served_sample(args, n_requests: int, seed: int, threads: int = 0, horizon_cap: int = 5):
+    """The reference's CPU forward (the oracle's f32 restatement with the
+    reference's O(T^2) masked attention scan) on a bounded sample of the
+    served workload, one request at a time on `threads` host threads (0: all
+    cores). Each request runs at most `horizon_cap` ticks of its horizon (a
+    reconstruct: one of its sweeps over that window) and is credited with the
+    useful cell-ticks that part of it is worth (a reconstruct sweep 1/4 of its
+    window's cell-ticks), so the rate is the full workload's rate."""
     from jacobi2000_gb300 import engine
-    from jacobi2000_gb300.checkpoint import parse_config, synthetic_family, write_safetensors_bytes, meta_of
+    from jacobi2000_gb300.checkpoint import meta_of, parse_config, synthetic_family
+    from oracle import oracle
 
-    rates = [float(r) for r in args.served_rates.split(",") if r.strip()]
-    if not rates:
-        return None
-    fam_f = synthetic_family(args.dim, args.layers, 0, SERVED_SIDES)
-    fam_r = synthetic_family(args.dim, args.layers, 1, SERVED_SIDES)
-    cfgs = [parse_config(fam_f[(s, s)][1], fam_f[(s, s)][0]) for s in SERVED_SIDES]
-    metas = [meta_of(c) for c in cfgs]
-    rng = np.random.default_rng(1234)
-    volumes, masks = [], []
-    for s in SERVED_SIDES:
-        volumes.append((0.3 * rng.standard_normal((51, 3, s, s))).astype(np.float32))
-        masks.append((rng.random((51, s, s)) < 0.02).astype(np.uint8))
-    sweeps = 4
-    out = {"task_mix": "1/3 forward, 1/3 rewind, 1/3 reconstruct (2% known, 4 Jacobi sweeps)",
-           "sides": "log-uniform 32-256, rounded to a multiple of 32", "horizon": "U[10,50] ticks",
-           "admission": "0.8 x HBM, 8M cells per tick", "bf16": []}
-    for prec, key in ((engine.BF16, "bf16"), (engine.FP32, "fp32_one_at_a_time")):
-        fm = [engine.Model.from_bytes(write_safetensors_bytes(fam_f[(s, s)][0]), fam_f[(s, s)][1], prec)
-              for s in SERVED_SIDES]
-        rm = [engine.Model.from_bytes(write_safetensors_bytes(fam_r[(s, s)][0]), fam_r[(s, s)][1], prec)
-              for s in SERVED_SIDES]
-        with engine.Server(fm, rm, max_active_cells=8 << 20, hbm_fraction=0.8) as srv:
-            warm = served_requests(np.random.default_rng(99), 12, 1000.0, cfgs, volumes, masks)
-            run_served(srv, warm, metas, sweeps)
-            if prec == engine.BF16:
-                for rate in rates:
-                    reqs = served_requests(np.random.default_rng(int(rate)), args.served_requests, rate, cfgs,
-                                           volumes, masks)
-                    r = run_served(srv, reqs, metas, sweeps)
-                    r["rate_req_s"] = rate
-                    out["bf16"].append(r)
-            else:
-                reqs = served_requests(np.random.default_rng(int(rates[0])), args.served_fp32_requests, rates[0],
-                                       cfgs, volumes, masks)
-                r = run_served(srv, reqs, metas, sweeps, concurrent=False)
-                r["rate_req_s"] = rates[0]
-                out[key] = r
-        for m in fm + rm:
-            m.close()
-    return out
+    oracle.set_threads(threads or os.cpu_count() or 1)
+    oracle.set_attention_mode("scan")
+    reqs = C5.draw(seed, n_requests, 1000.0)
+    sides = sorted({C5_SIDES[r["g"]] for r in reqs})
+    fams = [synthetic_family(args.dim, args.layers, s, sides) for s in (0, 1)]
+    cfgs = {sd: parse_config(fams[0][(sd, sd)][1], fams[0][(sd, sd)][0]) for sd in sides}
+    wl = C5([cfgs.get(sd) for sd in C5_SIDES])
+    credited, elapsed = 0.0, 0.0
+    for r in reqs:
+        sd, H = C5_SIDES[r["g"]], min(r["ticks"], horizon_cap)
+        fo = oracle.OracleModel(cfgs[sd], fams[0][(sd, sd)][0])
+        ro = oracle.OracleModel(cfgs[sd], fams[1][(sd, sd)][0])
+        meta = meta_of(cfgs[sd])
+        x, known = wl.inputs(dict(r, ticks=H))
+        t0 = time.perf_counter()
+        if r["task"] == engine.TASK_RECONSTRUCT:
+            oracle.reconstruct(fo, ro, x, known, meta, 1)
+            credited += sd * sd * H / C5_SWEEPS
+        else:
+            (fo if r["task"] == engine.TASK_FORWARD else ro).rollout(x, meta, H, oracle.MASS | oracle.ENERGY)
+            credited += sd * sd * H
+        elapsed += time.perf_counter() - t0
+    return credited / elapsed, oracle.get_threads(), elapsed, len(reqs)
+
+
+def served_config(n_requests: int):
+    return {"workload": f"served: Poisson arrivals at {C5_RATES[-1]:.0f} req/s (the saturating rate of the 10-2000 "
+                        f"req/s sweep), {n_requests} requests per step; grid side log-uniform 32-256 rounded to a "
+                        f"multiple of 4, horizon U[10,50] ticks; 1/3 forward, 1/3 rewind, 1/3 reconstruct "
+                        f"({C5_KNOWN:.0%} of space-time cells known, {C5_SWEEPS} Jacobi sweeps); mass+energy "
+                        f"projection; continuous batching, admission at {C5_HBM:.0%} of HBM and "
+                        f"{C5_MAX_CELLS >> 20}M cells per tick",
+            "model": "jacobi2000 dim 128, 4 layers, 4 heads, stencil r1 d1; forward family seed 0, reverse family "
+                     "seed 1 (one checkpoint per side, every tensor but pos shared)",
+            "sides": [C5_SIDES[0], C5_SIDES[-1], 4], "requests_per_step": n_requests,
+            "l2": "per-tick working set of the active requests > 129 MB L2 (no flush needed)",
+            "parallelism": "replicas"}
 
 
 MIXED_SIDES = [32, 64, 96, 128, 192]
@@ -539,21 +643,6 @@ def eval_bench(args, steps=3):
     return out
 
 
-def cpu_sample(cfg, t, x0, meta, ticks: int, threads: int = 0):
-    """The oracle's f32 rollout (the reference's CPU arithmetic and O(T^2)
-    masked scan) over `ticks` ticks of one instance, on `threads` host
-    threads (0: all host cores)."""
-    from oracle import oracle
-
-    oracle.set_threads(threads or os.cpu_count() or 1)
-    oracle.set_attention_mode("scan")
-    m = oracle.OracleModel(cfg, t)
-    t0 = time.perf_counter()
-    m.rollout(x0, meta, ticks, oracle.MASS | oracle.ENERGY)
-    dt = time.perf_counter() - t0
-    return cfg.nx * cfg.ny * ticks / dt, oracle.get_threads(), dt
-
-
 def max_over_ranks(v: float, world: int, device: str) -> float:
     """The largest of the ranks' values (a step time: the job ends with its
     slowest rank), by an all-reduce over the default process group."""
@@ -574,27 +663,112 @@ def whole_job_rate(units_per_rank: float, world: int, ms: float) -> float:
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU forward (the oracle's f32
+    restatement, O(T^2) masked attention scan) on a bounded sample of the
+    served workload per step, on every host core; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    t, cj, cfg, x0s, meta = workload(args)
     from oracle import oracle
 
     oracle.build()
-    vals = []
+    vals, cores, secs = [], 1, 0.0
     for i in range(args.warmup + args.steps):
-        v, cores, dt = cpu_sample(cfg, t, x0s[i % len(x0s)], meta, args.ref_step_ticks)
+        v, cores, dt, n = cpu_served_sample(args, args.ref_requests, seed=500 + i, horizon_cap=args.ref_horizon)
         if i >= args.warmup:
             vals.append(v)
+            secs += dt
     value = statistics.median(vals)
-    sample = f"1 instance x {args.ref_step_ticks} tick(s) of the {args.side}x{args.side} workload per step"
+    sample = (f"{args.ref_requests} requests of the served workload per step, one at a time, each at most "
+              f"{args.ref_horizon} ticks "
+              f"(a reconstruct: one sweep of that window, credited 1/4 of its cell-ticks)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * cfg.nx * cfg.ny * args.ref_step_ticks / value,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(args, cfg), "impl": "reference",
+            "config": served_config(args.requests), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batched_bench(args, world, barrier):
+    """The batched extra: B instances of one grid (side x side), `ticks`
+    ticks with mass+energy projection, one batch call per step, device
+    buffers (CUDA events) and host buffers (wall clock); the per-kernel table
+    and the roofline of the dominant kernel."""
+    import torch
+
+    from jacobi2000_gb300 import engine
+    from jacobi2000_gb300.checkpoint import write_safetensors_bytes
+
+    t, cj, cfg, x0s, meta = workload(args)
+    model = engine.Model.from_bytes(write_safetensors_bytes(t), cj, engine.BF16)
+    cells = cfg.nx * cfg.ny
+    B, H = args.instances, args.ticks
+    batch = engine.Batch([model], max_instances=B, max_cells=B * cells)
+    me = engine.PROJECT_MASS | engine.PROJECT_ENERGY
+    host_items = [(0, x, meta, H, me) for x in x0s]
+    dx0 = [torch.from_numpy(x).cuda() for x in x0s]
+    dmeta = torch.from_numpy(meta).cuda()
+    dout = [torch.empty_like(x) for x in dx0]
+    dev_items = [(0, x.data_ptr(), dmeta.data_ptr(), H, me, o.data_ptr()) for x, o in zip(dx0, dout)]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    for _ in range(2):
+        batch.rollout(dev_items, device=True, stream=sptr)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = 5
+    ev0.record(stream)
+    for _ in range(steps):
+        batch.rollout(dev_items, device=True, stream=sptr)
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1) / steps
+    batch.rollout(host_items)
+    t0 = time.perf_counter()
+    for _ in range(2):
+        batch.rollout(host_items)
+    e2e_s = (time.perf_counter() - t0) / 2
+    prof = batch.profile(dev_items, device=True)
+    pk, pk_kind = peaks()
+    total_ms = sum(v[1] for v in prof.values())
+    table = {}
+    for kname, (nl, tot) in prof.items():
+        kind, amount = kernel_work(kname, B, cells, args.dim, 4 * args.dim)
+        avg_s = tot / nl / 1e3
+        if kind == "flop":
+            table[kname] = {"tflops": amount / avg_s / 1e12, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
+        elif kind == "byte":
+            table[kname] = {"gbs": amount / avg_s / 1e9, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
+    name, (nl, tot_ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    kind, amount = kernel_work(name, B, cells, args.dim, 4 * args.dim)
+    avg_s = tot_ms / nl / 1e3
+    traffic = ncu_traffic().get(name)
+    if kind == "flop":
+        peak = pk["bf16_tflops"]
+        roof = {"bound": "tensor", "kernel": name, "achieved": amount / avg_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": amount / avg_s / 1e12 / peak, "traffic": traffic,
+                "peak_kind": f"{pk_kind} bf16 dense burst", "flop_per_launch": amount}
+    else:
+        peak = pk["hbm_gbs"]
+        roof = {"bound": "hbm", "kernel": name, "achieved": amount / avg_s / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": amount / avg_s / 1e9 / peak, "traffic": traffic, "peak_kind": f"{pk_kind} copy bandwidth",
+                "bytes_per_launch": amount}
+    roof.update({"avg_launch_ms": avg_s * 1e3, "share": tot_ms / total_ms,
+                 "measured_on": f"the batched extra ({B} x {args.side}x{args.side}, one tick's launches timed with "
+                                f"CUDA events on the launching stream)"})
+    rate = B * cells * H / (ms / 1e3)
+    flop = FLOP_PER_CELL_TICK.get((args.dim, args.layers))
+    out = {"workload": f"rollout {B}x {args.side}x{args.side} grids, {H} ticks, mass+energy projection, "
+                       f"8 drops/instance, one batch call per step",
+           "value": rate, "ms_per_step": ms, "e2e": B * cells * H / e2e_s,
+           "tick_tflops": rate * flop / 1e12 if flop else None,
+           "tick_frac_of_bf16_peak": rate * flop / 1e12 / pk["bf16_tflops"] if flop else None,
+           "launches_per_step": sum(n for n, _ in prof.values())}
+    batch.close()
+    model.close()
+    return out, roof, table
 
 
 def main():
@@ -612,137 +786,125 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     from jacobi2000_gb300 import engine
-    from jacobi2000_gb300.checkpoint import write_safetensors_bytes
-
-    t, cj, cfg, x0s, meta = workload(args)
-    prec = engine.BF16 if args.precision == "bf16" else engine.FP32
-    model = engine.Model.from_bytes(write_safetensors_bytes(t), cj, prec)
-    cells = cfg.nx * cfg.ny
-    B, H = args.instances, args.ticks
-    batch = engine.Batch([model], max_instances=B, max_cells=B * cells)
-    me = engine.PROJECT_MASS | engine.PROJECT_ENERGY
-    host_items = [(0, x, meta, H, me) for x in x0s]
-
-    # device-resident inputs
-    dx0 = [torch.from_numpy(x).cuda() for x in x0s]
-    dmeta = torch.from_numpy(meta).cuda()
-    dout = [torch.empty_like(x) for x in dx0]
-    dev_items = [(0, x.data_ptr(), dmeta.data_ptr(), H, me, o.data_ptr()) for x, o in zip(dx0, dout)]
-    stream = torch.cuda.current_stream()
-    sptr = stream.cuda_stream
+    from jacobi2000_gb300.checkpoint import meta_of
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
+    pk, pk_kind = peaks()
+    cfgs = c5_configs(args)
+    metas = [meta_of(c) for c in cfgs]
+    wl = C5(cfgs)
+    fm, rm = c5_models(args, engine.BF16)
+    srv = engine.Server(fm, rm, max_active_cells=C5_MAX_CELLS, hbm_fraction=C5_HBM)
+    rate = C5_RATES[-1]
+    step_reqs = C5.draw(7 + 1000 * rank, args.requests, rate)
+    # warm-up: the same requests (tunes and allocates outside the timed steps)
     for _ in range(args.warmup):
-        batch.rollout(dev_items, device=True, stream=sptr)
+        run_served(srv, wl, step_reqs, metas, device=True)
     barrier()
-    # the raw nvidia-smi samples go to $JC_BENCH_OUT (default: the system's temp folder)
     out_dir = Path(os.environ.get("JC_BENCH_OUT") or tempfile.gettempdir())
     out_dir.mkdir(parents=True, exist_ok=True)
     clocks = Clocks(out_dir / f"clocks_rank{rank}.csv")
+    runs = []
     with clocks:
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
         for _ in range(args.steps):
-            batch.rollout(dev_items, device=True, stream=sptr)
-        ev1.record(stream)
+            runs.append(run_served(srv, wl, step_reqs, metas, device=True))
         barrier()
-    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, "cuda")
-    value = whole_job_rate(B * cells * H, world, ms)
+    dev_s = sum(r["device_span_s"] for r in runs)
+    ms = max_over_ranks(1e3 * dev_s / args.steps, world, "cuda")
+    useful = wl.useful(step_reqs)
+    value = whole_job_rate(useful, world, ms)
+    launches = sum(r["launches"] for r in runs)
+    # end to end with host buffers through the C ABI
+    e2e_runs = [run_served(srv, wl, step_reqs, metas, device=False) for _ in range(2)]
+    e2e_ms = max_over_ranks(1e3 * statistics.mean(r["wall_s"] for r in e2e_runs), world, "cuda")
 
-    # end to end through the C ABI with host buffers
-    for _ in range(2):
-        batch.rollout(host_items)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        batch.rollout(host_items)
-    barrier()
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, "cuda")
-    h2d = B * (x0s[0].nbytes + meta.nbytes)
-    d2h = B * (x0s[0].nbytes + 32)
+    served = None
+    if rank == 0:
+        served = {"saturating_rate_req_s": rate,
+                  "device_buffers": {"p50_ms": statistics.median(r["p50_ms"] for r in runs),
+                                     "p99_ms": statistics.median(r["p99_ms"] for r in runs),
+                                     "iterations_per_step": statistics.mean(r["iterations"] for r in runs),
+                                     "work_cell_ticks_per_s": wl.work(step_reqs) / (dev_s / args.steps)},
+                  "host_buffers": {k: e2e_runs[-1][k] for k in ("cell_ticks_per_s_wall", "p50_ms", "p99_ms",
+                                                                  "wall_s")},
+                  "rates": []}
+        if not args.no_sweep:
+            for r_ in C5_RATES:
+                n = max(40, int(r_ * args.sweep_seconds))
+                n = min(n, args.requests)
+                res = run_served(srv, wl, C5.draw(int(r_) + 17, n, r_), metas)
+                res["rate_req_s"] = r_
+                served["rates"].append({k: res[k] for k in ("rate_req_s", "requests", "cell_ticks_per_s_wall",
+                                                             "cell_ticks_per_s_device", "p50_ms", "p99_ms",
+                                                             "wall_s")})
+        served["work_per_useful"] = wl.work(step_reqs) / useful
+    srv.close()
+    for m in fm + rm:
+        m.close()
 
-    # the plain FP32 single-request path, one rollout at a time
-    plain = engine.Model.from_bytes(write_safetensors_bytes(t), cj, engine.FP32)
-    plain.rollout(x0s[0], meta, H, me)
-    n_plain = min(B, 8)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(n_plain):
-        plain.rollout(x0s[i], meta, H, me)
-    plain_s = (time.perf_counter() - t0) / n_plain
-    plain_value = cells * H / plain_s
+    plain = None
+    if rank == 0:
+        fm32, rm32 = c5_models(args, engine.FP32)
+        with engine.Server(fm32, rm32, max_active_cells=C5_MAX_CELLS, hbm_fraction=C5_HBM) as s32:
+            preqs = C5.draw(99, args.plain_requests, rate)
+            run_served(s32, wl, preqs[:6], metas, concurrent=False)
+            r32 = run_served(s32, wl, preqs, metas, concurrent=False)
+        for m in fm32 + rm32:
+            m.close()
+        flop = FLOP_PER_CELL_TICK.get((args.dim, args.layers))
+        fp32_peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        work_rate = r32["work_cell_ticks"] / r32["wall_s"]
+        plain = {"value": r32["cell_ticks_per_s_wall"], "unit": UNIT, "requests": r32["requests"],
+                 "p50_ms": r32["p50_ms"], "p99_ms": r32["p99_ms"],
+                 "note": "FP32 kernels, one request at a time (each submitted after the previous result), "
+                         "same request distribution, host buffers",
+                 "roofline": {"bound": "fp32-simt", "achieved": work_rate * flop / 1e12 if flop else None,
+                              "peak": fp32_peak, "unit": "TFLOP/s",
+                              "frac": work_rate * flop / 1e12 / fp32_peak if flop else None,
+                              "peak_kind": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x max SM clock)",
+                              "flop_per_cell_tick": flop}}
+    batched, roof, table = batched_bench(args, world, barrier)
 
-    # per-kernel device times (events on the launching stream, outside graphs)
-    prof = batch.profile(dev_items, device=True)
-    launches_per_step = sum(n for n, _ in prof.values())
-    pk, pk_kind = peaks()
-    total_ms = sum(v[1] for v in prof.values())
-    table = {}
-    for kname, (nl, tot) in prof.items():
-        kind, amount = kernel_work(kname, B, cells, args.dim, 4 * args.dim)
-        avg_s = tot / nl / 1e3
-        if kind == "flop":
-            table[kname] = {"tflops": amount / avg_s / 1e12, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
-        elif kind == "byte":
-            table[kname] = {"gbs": amount / avg_s / 1e9, "avg_ms": avg_s * 1e3, "share": tot / total_ms}
-    name, (nl, tot_ms) = max(prof.items(), key=lambda kv: kv[1][1])
-    kind, amount = kernel_work(name, B, cells, args.dim, 4 * args.dim)
-    avg_s = tot_ms / nl / 1e3
-    traffic = ncu_traffic().get(name)
-    if kind == "flop" and name.startswith("tc_"):
-        peak = pk["bf16_tflops"]
-        roof = {"bound": "tensor", "kernel": name, "achieved": amount / avg_s / 1e12, "peak": peak,
-                "unit": "TFLOP/s", "frac": amount / avg_s / 1e12 / peak, "traffic": traffic,
-                "peak_kind": f"{pk_kind} bf16 dense burst", "flop_per_launch": amount}
-    elif kind == "flop":
-        peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-        roof = {"bound": "fp32-simt", "kernel": name, "achieved": amount / avg_s / 1e12, "peak": peak,
-                "unit": "TFLOP/s", "frac": amount / avg_s / 1e12 / peak, "traffic": traffic,
-                "peak_kind": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x max SM clock)",
-                "flop_per_launch": amount}
-    else:
-        peak = pk["hbm_gbs"]
-        roof = {"bound": "hbm", "kernel": name, "achieved": amount / avg_s / 1e9, "peak": peak, "unit": "GB/s",
-                "frac": amount / avg_s / 1e9 / peak, "traffic": traffic, "peak_kind": f"{pk_kind} copy bandwidth",
-                "bytes_per_launch": amount}
-    roof.update({"avg_launch_ms": avg_s * 1e3, "share": tot_ms / total_ms})
-
-    served = served_bench(args) if rank == 0 else None
     mixed = mixed_batch_bench(args) if rank == 0 and not args.no_mixed else None
     accuracy = accuracy_c3() if rank == 0 and not args.no_accuracy else None
     evalm = eval_bench(args) if rank == 0 and not args.no_eval else None
 
     cpu = None
     if rank == 0:
-        v, cores, dt = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks)
+        v, cores, dt, n = cpu_served_sample(args, args.cpu_requests, seed=31)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"1 instance x {args.cpu_sample_ticks} tick(s), {dt:.1f} s"}
-        if args.cpu_sample_ticks_1t > 0:
-            v1, _, dt1 = cpu_sample(cfg, t, x0s[0], meta, args.cpu_sample_ticks_1t, threads=1)
-            cpu["one_thread"] = {"value": v1, "unit": UNIT, "cores": 1,
-                                 "sample": f"1 instance x {args.cpu_sample_ticks_1t} tick(s), {dt1:.1f} s"}
+               "sample": f"{n} requests of the served workload, one at a time, each at most 5 ticks (a "
+                         f"reconstruct: one sweep of that window, credited 1/4 of its cell-ticks), {dt:.1f} s"}
+        v1, _, dt1, n1 = cpu_served_sample(args, 3, seed=32, threads=1, horizon_cap=2)
+        cpu["one_thread"] = {"value": v1, "unit": UNIT, "cores": 1,
+                             "sample": f"{n1} requests, each at most 2 ticks, {dt1:.1f} s"}
 
     if rank == 0:
+        flop = FLOP_PER_CELL_TICK.get((args.dim, args.layers))
+        h2d = e2e_runs[-1]["h2d_bytes"]
+        d2h = e2e_runs[-1]["d2h_bytes"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32" if prec == engine.FP32 else "bf16", "data": "synthetic",
-                "config": config_dict(args, cfg),
-                "e2e": {"value": whole_job_rate(B * cells * H, world, 1e3 * e2e_s), "unit": UNIT,
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded drops and sensor masks, "
+                "random-init checkpoints)", "config": served_config(args.requests),
+                "e2e": {"value": whole_job_rate(useful, world, e2e_ms), "unit": UNIT,
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-                "fp32_plain": {"value": plain_value, "unit": UNIT, "ms_per_rollout": plain_s * 1e3,
-                               "note": f"one {args.side}x{args.side} rollout of {H} ticks at a time"},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local), "served": served,
-                "mixed_batch": mixed, "accuracy": accuracy, "eval_metrics": evalm,
-                "gpu_launches": launches_per_step * args.steps,
-                "kernels": table, "peaks": pk_kind}
+                "served_vs_plain": value / plain["value"] if plain else None,
+                "fp32_plain": plain, "served": served,
+                "served_roofline": {"bound": "tensor", "achieved": served["device_buffers"]["work_cell_ticks_per_s"]
+                                    * flop / 1e12 if flop else None, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                                    "frac": served["device_buffers"]["work_cell_ticks_per_s"] * flop / 1e12
+                                    / pk["bf16_tflops"] if flop else None,
+                                    "note": "every forward the served steps ran (reconstruct sweeps included) "
+                                            "x useful FLOP per cell-tick, over the device span"},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(local),
+                "batched": batched, "kernels": table, "mixed_batch": mixed, "accuracy": accuracy,
+                "eval_metrics": evalm, "gpu_launches": launches, "peaks": pk_kind}
         print(json.dumps(line), flush=True)
-    batch.close()
-    model.close()
-    plain.close()
     if world > 1:
         dist.destroy_process_group()
 

@@ -181,9 +181,13 @@ jc_status jc_batch_rollout(jc_batch* b, const jc_instance* instances, int32_t n,
 
 /* ---- Serving ----
  * A request loop with continuous batching: requests of different grid sizes
- * and tasks that arrive while others run are admitted at the next tick as the
- * workspace and the device memory budget allow, and share the same launches;
- * their states stay on the device until they finish. Tasks:
+ * and tasks that arrive while others run are admitted as the workspace and
+ * the device memory budget allow, and share the same launches; their states
+ * stay on the device until they finish. The loop runs chunks of ticks with
+ * no host round trip inside a chunk; a chunk ends when a waiting request
+ * could be admitted, or after a few milliseconds of device time when none
+ * waits. Results do not depend on the other requests in the mix or on how
+ * a request's ticks fall into chunks. Tasks:
  *   FORWARD:     ticks steps of the forward model from x = X_0, projected
  *                (the eval.rs:144-157 loop);
  *   REWIND:      ticks steps of the reverse model from x = X_H, projected
@@ -198,14 +202,21 @@ typedef struct jc_server jc_server;
 
 enum { JC_TASK_FORWARD = 0, JC_TASK_REWIND = 1, JC_TASK_RECONSTRUCT = 2 };
 
+/* Request flag: x, known and meta are device pointers that stay valid until
+ * the request is done, and jc_server_wait's `out` is a device pointer. The
+ * result stays in the server's device memory (counted against its budget)
+ * until jc_server_wait copies it out. Without it, inputs and results are
+ * host memory and jc_server_submit copies the inputs. */
+#define JC_REQUEST_DEVICE_BUFFERS 0x100u
+
 typedef struct {
     int32_t task;         /* JC_TASK_* */
     int32_t grid;         /* index into the server's model lists */
     int32_t ticks;        /* horizon H >= 1 */
-    uint32_t flags;       /* JC_PROJECT_* (forward and rewind) */
-    const float* x;       /* see above; copied by jc_server_submit */
-    const uint8_t* known; /* reconstruct only; copied */
-    const float* meta;    /* [meta_dim]; copied */
+    uint32_t flags;       /* JC_PROJECT_* (forward and rewind), JC_REQUEST_DEVICE_BUFFERS */
+    const float* x;       /* see above; host memory is copied by jc_server_submit */
+    const uint8_t* known; /* reconstruct only */
+    const float* meta;    /* [meta_dim] */
     int32_t max_sweeps;   /* reconstruct */
     float tol;            /* reconstruct: stop when max |change| < tol */
 } jc_request;
@@ -224,8 +235,11 @@ typedef struct {
     int64_t completed;
     double cell_ticks;    /* sum of nx * ny * ticks of completed requests */
     double busy_s;        /* time the loop spent in iterations */
-    double span_s;        /* first submit to last completion */
+    double span_s;        /* first submit to last completion (host clock) */
     int32_t iterations, active, pending;
+    double device_span_s; /* device time (CUDA events on the server's stream) from the start
+                             of the first iteration to the end of the latest one */
+    int64_t launches;     /* kernel launches the loop made (forward, projection, reconstruct) */
 } jc_server_stats;
 
 /* forward_models[i] and reverse_models[i] (reverse may be null: forward only)
@@ -246,6 +260,8 @@ jc_status jc_server_submit(jc_server* s, const jc_request* r, uint64_t* id);
 jc_status jc_server_wait(jc_server* s, uint64_t id, float* out, size_t out_len, jc_result* info,
                          double timeout_s);
 jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out);
+/* Zeroes the statistics; the next iteration starts a new device span. */
+jc_status jc_server_reset_stats(jc_server* s);
 
 /* Instrumentation, with no counterpart in the reference: runs the instances
  * once, outside any graph, with CUDA events around every kernel launch, and

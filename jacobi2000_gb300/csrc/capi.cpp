@@ -219,6 +219,11 @@ jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out) {
     return guard([&] { jc::server_stats(s, out); });
 }
 
+jc_status jc_server_reset_stats(jc_server* s) {
+    if (!s) return fail(JC_BAD_ARGUMENT, "server is null");
+    return guard([&] { jc::server_reset_stats(s); });
+}
+
 jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n, int32_t device_pointers,
                            char* report, size_t cap) {
     if (!b || !report || cap == 0) return fail(JC_BAD_ARGUMENT, "null argument");

@@ -134,9 +134,13 @@ struct KernelTimer {
     ~KernelTimer();
 };
 extern thread_local KernelTimer* g_ktimer;
+// Kernel launches of the forward, projection and reconstruct paths made by
+// the calling thread (every such launch is wrapped in one KScope).
+extern thread_local long long g_launches;
 
 struct KScope {
     KScope(const char* name, cudaStream_t s) {
+        g_launches++;
         if (g_ktimer) g_ktimer->begin(name, s);
     }
     ~KScope() {

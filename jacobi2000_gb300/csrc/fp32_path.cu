@@ -20,6 +20,7 @@ namespace cg = cooperative_groups;
 namespace jc {
 
 thread_local KernelTimer* g_ktimer = nullptr;
+thread_local long long g_launches = 0;
 
 void KernelTimer::begin(const char* name, cudaStream_t s) {
     stream = s;

@@ -1,9 +1,11 @@
 // Serving loop: continuous batching of forward, rewind and reconstruct
 // requests of different grid sizes on one GPU.
 //
-// A server thread runs iterations; each iteration is one tick for every active
-// request. All instances that use the forward weights go into one packed launch
-// sequence, all that use the reverse weights into another:
+// A server thread runs iterations. An iteration admits waiting requests, then
+// runs a chunk of K ticks for every active request without returning to the
+// host in between, then collects the requests that finished. Per tick, all
+// instances that use the forward weights go into one packed launch sequence
+// and all that use the reverse weights into another:
 //   forward     request: its state (one instance, forward model), projected;
 //   rewind      request: its state (one instance, reverse model), projected
 //               (the web demo's rewind, crates/web/src/lib.rs:383-409);
@@ -15,11 +17,19 @@
 //               or `max_sweeps` sweeps ran, without projection. This task has no
 //               counterpart in the reference (its tests pin it against the
 //               oracle restated with the same rule).
-// Requests that arrive while others run are admitted at the next iteration,
+// Within a chunk each group's instances are ordered by the ticks (sweeps) they
+// have left, longest first, so the instances still running at chunk tick t
+// are a prefix: a request that finishes inside the chunk simply drops out of
+// the later ticks' launches. A reconstruct request that converges inside the
+// chunk is frozen on the device (its volume no longer changes). The chunk
+// ends early when a waiting request could be admitted, or after about
+// kChunkTargetS of device time when nothing waits.
+// Requests that arrive while a chunk runs are admitted at the next iteration,
 // while their instances fit the workspace and their buffers fit the device
 // memory budget; each request's state stays on the device until it is done.
 // A request's result does not depend on which other requests share its
-// launches (no kernel's arithmetic for one instance reads another's data).
+// launches (no kernel's arithmetic for one instance reads another's data),
+// nor on how its ticks are cut into chunks.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -41,42 +51,12 @@ double now_s() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
-// X_t <- known_t ? value : mean of the available step results; records the
-// largest change of an unknown value (as the bits of a non-negative float).
-__global__ void recon_update_kernel(float* __restrict__ vol, const float* __restrict__ F,
-                                    const float* __restrict__ Rv, const float* __restrict__ vals,
-                                    const uint8_t* __restrict__ known, int H, long long cells,
-                                    unsigned* __restrict__ residual) {
-    __shared__ float red[32];
-    const long long per = 3 * cells, total = (long long)(H + 1) * per;
-    float local = 0.f;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int t = (int)(i / per);
-        const long long rem = i - (long long)t * per, cell = rem % cells;
-        float v;
-        if (known[(long long)t * cells + cell]) {
-            v = vals[i];
-        } else {
-            if (t == 0) v = Rv[rem];
-            else if (t == H) v = F[(long long)(H - 1) * per + rem];
-            else v = 0.5f * (F[(long long)(t - 1) * per + rem] + Rv[(long long)t * per + rem]);
-            local = fmaxf(local, fabsf(v - vol[i]));
-        }
-        vol[i] = v;
-    }
-    local = warp_max(local);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
-        v = warp_max(v);
-        if (threadIdx.x == 0) atomicMax(residual, __float_as_uint(v));
-    }
-}
+// Longest chunk when nothing waits: about this much device time.
+constexpr double kChunkTargetS = 4e-3;
+constexpr int kMaxChunk = 64;
 
 // X_t <- known_t ? value : 0 (the normalized mean state) for every t.
-__global__ void recon_init_kernel(float* __restrict__ vol, const float* __restrict__ vals,
+__global__ void recon_fill_kernel(float* __restrict__ vol, const float* __restrict__ vals,
                                   const uint8_t* __restrict__ known, int H, long long cells) {
     const long long per = 3 * cells, total = (long long)(H + 1) * per;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -89,6 +69,10 @@ __global__ void recon_init_kernel(float* __restrict__ vol, const float* __restri
 
 }  // namespace
 
+// Request flag: x, known and meta are device pointers (valid until the request
+// is done), and jc_server_wait's `out` is a device pointer.
+constexpr uint32_t kDeviceBuffers = JC_REQUEST_DEVICE_BUFFERS;
+
 struct Request {
     uint64_t id = 0;
     jc_request r{};
@@ -96,14 +80,20 @@ struct Request {
     std::string error;
     bool done = false, admitted = false, fresh = false;
     bool finished = false;  // set by the server thread; published as `done` under the lock
+    bool device_io = false;
     double t_submit = 0, t_admit = 0, t_done = 0;
-    int ticks_done = 0, sweeps = 0;
+    int ticks_done = 0;                  // forward / rewind
+    int sweeps = 0, frozen = 0;          // reconstruct: host copy of the device bookkeeping
     float residual = 0.f;
     size_t cells = 0, bytes = 0;
-    // host copies of the inputs, and the result
+    // host copies of the inputs (host buffers), and the result
     std::vector<float> x, out;
     std::vector<uint8_t> known;
     std::vector<float> meta;
+    // caller's device inputs (device buffers)
+    const float* dev_x = nullptr;
+    const uint8_t* dev_known = nullptr;
+    const float* dev_meta = nullptr;
     // device buffers
     float* d_state = nullptr;   // forward / rewind: [3, cells]; reconstruct: the volume [H+1][3][cells]
     float* d_F = nullptr;       // reconstruct: [H][3][cells]
@@ -112,11 +102,12 @@ struct Request {
     uint8_t* d_known = nullptr; // reconstruct: [H+1][cells]
     float* d_meta = nullptr;
     ProjSlot* d_slot = nullptr;
-    unsigned* d_resid = nullptr;
     double energy = 0, max_viol = 0;
-    int inst_cells() const {
-        return r.task == JC_TASK_RECONSTRUCT ? (int)(2 * (size_t)r.ticks * cells) : (int)cells;
-    }
+    bool recon() const { return r.task == JC_TASK_RECONSTRUCT; }
+    long long inst_cells() const { return recon() ? 2 * (long long)r.ticks * (long long)cells : (long long)cells; }
+    int n_inst() const { return recon() ? 2 * r.ticks : 2; }  // sub-instances; forward/rewind: init + tick
+    int remaining() const { return recon() ? (frozen ? 0 : r.max_sweeps - sweeps) : r.ticks - ticks_done; }
+    size_t out_floats() const { return (recon() ? (size_t)(r.ticks + 1) : 1) * 3 * cells; }
 };
 
 class Server {
@@ -126,6 +117,7 @@ class Server {
     uint64_t submit(const jc_request& r);
     void wait(uint64_t id, float* out, size_t out_len, jc_result* info, double timeout_s);
     void stats(jc_server_stats* s);
+    void reset_stats();
 
    private:
     std::vector<Model*> fwd_, rev_;
@@ -134,8 +126,12 @@ class Server {
     DeviceArena arena_;
     Workspace ws_;
     cudaStream_t stream_ = nullptr;
-    InstDev* h_inst_ = nullptr;  // pinned mirror of the descriptor array
-    int max_inst_ = 0;
+    cudaStream_t wait_stream_ = nullptr;  // result copies of device-buffer requests in wait()
+    InstDev* h_inst_ = nullptr;    // pinned mirror of the descriptor array
+    ReconDev* h_recon_ = nullptr;  // pinned mirror of the reconstruct bookkeeping
+    ReconDev* d_recon_ = nullptr;
+    ProjSlot* h_slots_ = nullptr;  // pinned: slots of the requests finishing in a chunk
+    int max_inst_ = 0, max_recon_ = 0;
     long long max_cells_ = 0;
     size_t budget_bytes_ = 0, used_bytes_ = 0;
     std::mutex mu_;
@@ -146,16 +142,24 @@ class Server {
     uint64_t next_id_ = 1;
     bool stop_ = false;
     std::thread thread_;
+    // chunk timing: device events around each chunk, and the measured time
+    // of one tick per active cell (for the chunk length when nothing waits)
+    cudaEvent_t ev_first_ = nullptr, ev_a_ = nullptr, ev_b_ = nullptr;
+    bool span_open_ = false;
+    double s_per_cell_tick_ = 0.0;
     // statistics
     long long completed_ = 0;
-    double cell_ticks_ = 0, busy_s_ = 0, first_submit_ = 0, last_done_ = 0;
+    double cell_ticks_ = 0, busy_s_ = 0, first_submit_ = 0, last_done_ = 0, device_span_s_ = 0;
     int iterations_ = 0;
+    long long launches_ = 0;
 
     void loop();
-    void iteration(std::vector<Request*>& act);
+    int chunk_length(const std::vector<Request*>& act, long long head_cells, int head_inst) const;
+    void iteration(std::vector<Request*>& act, int K);
     void admit_locked();
     void allocate(Request& q);
     void release(Request& q);
+    void release_on(Request& q, cudaStream_t st);
     void fail_locked(Request& q, int status, const std::string& msg);
 };
 
@@ -196,10 +200,16 @@ Server::Server(jc_model* const* fwd, jc_model* const* rev, int n_grids, long lon
             throw Error(JC_BAD_ARGUMENT, "reverse model i must have forward model i's grid");
     max_cells_ = max_active_cells;
     max_inst_ = (int)std::min<long long>(max_active_cells / 16 + 64, 1 << 20);
+    max_recon_ = max_inst_ / 2 + 1;
     cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&wait_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&ev_first_, &ev_a_, &ev_b_}) cuda_check(cudaEventCreate(e), "cudaEventCreate");
     const int pp = dims_.P * dims_.P;
     ws_.alloc(arena_, dims_, (int)(max_cells_ / pp) + 1, max_cells_, max_inst_, fwd_[0]->w.bf16.get());
+    d_recon_ = arena_.alloc_n<ReconDev>(max_recon_);
     cuda_check(cudaMallocHost(&h_inst_, (size_t)max_inst_ * sizeof(InstDev)), "cudaMallocHost", JC_OVER_BUDGET);
+    cuda_check(cudaMallocHost(&h_recon_, (size_t)max_recon_ * sizeof(ReconDev)), "cudaMallocHost", JC_OVER_BUDGET);
+    cuda_check(cudaMallocHost(&h_slots_, (size_t)max_inst_ * sizeof(ProjSlot)), "cudaMallocHost", JC_OVER_BUDGET);
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
     const double cap = hbm_fraction * (double)total_b - (double)(total_b - free_b);
@@ -219,7 +229,15 @@ Server::~Server() {
         cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
     }
+    if (wait_stream_) {
+        cudaStreamSynchronize(wait_stream_);
+        cudaStreamDestroy(wait_stream_);
+    }
+    for (cudaEvent_t e : {ev_first_, ev_a_, ev_b_})
+        if (e) cudaEventDestroy(e);
     if (h_inst_) cudaFreeHost(h_inst_);
+    if (h_recon_) cudaFreeHost(h_recon_);
+    if (h_slots_) cudaFreeHost(h_slots_);
 }
 
 uint64_t Server::submit(const jc_request& r) {
@@ -229,27 +247,38 @@ uint64_t Server::submit(const jc_request& r) {
     if ((r.task != JC_TASK_FORWARD) && rev_.empty())
         throw Error(JC_BAD_ARGUMENT, "rewind and reconstruct need reverse models");
     if (r.ticks < 1) throw Error(JC_BAD_ARGUMENT, "ticks must be >= 1");
-    if (r.flags & ~3u) throw Error(JC_BAD_ARGUMENT, "unknown projection flag");
+    if (r.flags & ~(3u | kDeviceBuffers)) throw Error(JC_BAD_ARGUMENT, "unknown request flag");
     if (!r.x || !r.meta) throw Error(JC_BAD_ARGUMENT, "null input");
     if (r.task == JC_TASK_RECONSTRUCT && (!r.known || r.max_sweeps < 1))
         throw Error(JC_BAD_ARGUMENT, "reconstruct needs a known mask and max_sweeps >= 1");
     const Model& m = *fwd_[r.grid];
     Request q;
     q.r = r;
+    q.r.flags &= 3u;
+    q.device_io = (r.flags & kDeviceBuffers) != 0;
     q.cells = (size_t)m.cfg.nx * m.cfg.ny;
     if (q.inst_cells() > max_cells_)
         throw Error(JC_OVER_BUDGET, "this request needs more cells per tick than the server's workspace holds");
+    if (q.n_inst() > max_inst_)
+        throw Error(JC_OVER_BUDGET, "this request needs more instances than the server's descriptor array holds");
     const size_t len = 3 * q.cells;
     if (r.task == JC_TASK_RECONSTRUCT) {
         const size_t vol = (size_t)(r.ticks + 1);
-        q.x.assign(r.x, r.x + vol * len);
-        q.known.assign(r.known, r.known + vol * q.cells);
+        if (q.device_io) {
+            q.dev_x = r.x;
+            q.dev_known = r.known;
+        } else {
+            q.x.assign(r.x, r.x + vol * len);
+            q.known.assign(r.known, r.known + vol * q.cells);
+        }
         q.bytes = vol * len * 4 * 2 + 2 * (size_t)r.ticks * len * 4 + vol * q.cells + 4096;
     } else {
-        q.x.assign(r.x, r.x + len);
+        if (q.device_io) q.dev_x = r.x;
+        else q.x.assign(r.x, r.x + len);
         q.bytes = len * 4 + 4096;
     }
-    q.meta.assign(r.meta, r.meta + m.cfg.meta_dim);
+    if (q.device_io) q.dev_meta = r.meta;
+    else q.meta.assign(r.meta, r.meta + m.cfg.meta_dim);
     q.r.x = nullptr;
     q.r.known = nullptr;
     q.r.meta = nullptr;
@@ -276,15 +305,36 @@ void Server::wait(uint64_t id, float* out, size_t out_len, jc_result* info, doub
         if (timeout_s < 0) cv_done_.wait(lk);
         it = reqs_.find(id);
     }
-    Request& q = it->second;
-    if (q.status != JC_OK) {
-        Error e((jc_status)q.status, q.error);
-        reqs_.erase(it);
-        throw e;
-    }
-    if (out) {
-        if (out_len < q.out.size()) throw Error(JC_BAD_ARGUMENT, "output buffer too small");
-        std::memcpy(out, q.out.data(), q.out.size() * 4);
+    // a done request is no longer referenced by the server thread
+    Request q = std::move(it->second);
+    reqs_.erase(it);
+    lk.unlock();
+    if (q.status != JC_OK) throw Error((jc_status)q.status, q.error);
+    const size_t n = q.out_floats();
+    struct Settle {  // device results: free the buffers and the budget even on errors
+        Server* s;
+        Request* q;
+        ~Settle() {
+            if (!q->device_io) return;
+            s->release_on(*q, s->wait_stream_);
+            cudaStreamSynchronize(s->wait_stream_);
+            {
+                std::lock_guard<std::mutex> g(s->mu_);
+                s->used_bytes_ -= q->bytes;
+            }
+            s->cv_work_.notify_one();  // the freed memory may admit a waiting request
+        }
+    } settle{this, &q};
+    if (out && out_len < n) throw Error(JC_BAD_ARGUMENT, "output buffer too small");
+    if (q.device_io) {
+        // the result is in the request's device buffer, written by work that
+        // has completed (the chunk that finished it was synchronized)
+        if (out) {
+            cuda_check(cudaMemcpyAsync(out, q.d_state, n * 4, cudaMemcpyDeviceToDevice, wait_stream_), "D2D", JC_MAP);
+            cuda_check(cudaStreamSynchronize(wait_stream_), "cudaStreamSynchronize", JC_POLL);
+        }
+    } else if (out) {
+        std::memcpy(out, q.out.data(), n * 4);
     }
     if (info) {
         info->latency_s = q.t_done - q.t_submit;
@@ -293,9 +343,8 @@ void Server::wait(uint64_t id, float* out, size_t out_len, jc_result* info, doub
         info->residual = q.residual;
         info->energy = q.energy;
         info->max_violation = q.max_viol;
-        info->out_len = (int64_t)q.out.size();
+        info->out_len = (int64_t)n;
     }
-    reqs_.erase(it);
 }
 
 void Server::stats(jc_server_stats* s) {
@@ -307,6 +356,18 @@ void Server::stats(jc_server_stats* s) {
     s->iterations = iterations_;
     s->active = (int32_t)active_.size();
     s->pending = (int32_t)pending_.size();
+    s->device_span_s = device_span_s_;
+    s->launches = launches_;
+}
+
+void Server::reset_stats() {
+    std::lock_guard<std::mutex> lk(mu_);
+    completed_ = 0;
+    cell_ticks_ = busy_s_ = device_span_s_ = 0.0;
+    first_submit_ = last_done_ = 0.0;
+    iterations_ = 0;
+    launches_ = 0;
+    span_open_ = false;
 }
 
 void Server::fail_locked(Request& q, int status, const std::string& msg) {
@@ -323,57 +384,61 @@ void Server::allocate(Request& q) {
         cuda_check(cudaMallocAsync(&p, bytes, stream_), "cudaMallocAsync", JC_OVER_BUDGET);
         return p;
     };
+    const cudaMemcpyKind in_kind = q.device_io ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     q.d_meta = static_cast<float*>(get(64 * 4));
     q.d_slot = static_cast<ProjSlot*>(get(sizeof(ProjSlot)));
-    q.d_resid = static_cast<unsigned*>(get(16));
-    cuda_check(cudaMemcpyAsync(q.d_meta, q.meta.data(), q.meta.size() * 4, cudaMemcpyHostToDevice, stream_), "H2D",
-               JC_MAP);
-    if (q.r.task == JC_TASK_RECONSTRUCT) {
+    cuda_check(cudaMemcpyAsync(q.d_meta, q.device_io ? q.dev_meta : q.meta.data(), dims_.meta_dim * 4, in_kind,
+                               stream_),
+               "meta", JC_MAP);
+    if (q.recon()) {
         const size_t H = (size_t)q.r.ticks;
         q.d_state = static_cast<float*>(get((H + 1) * len * 4));
         q.d_vals = static_cast<float*>(get((H + 1) * len * 4));
         q.d_F = static_cast<float*>(get(H * len * 4));
         q.d_R = static_cast<float*>(get(H * len * 4));
         q.d_known = static_cast<uint8_t*>(get((H + 1) * q.cells));
-        cuda_check(cudaMemcpyAsync(q.d_vals, q.x.data(), (H + 1) * len * 4, cudaMemcpyHostToDevice, stream_), "H2D",
-                   JC_MAP);
-        cuda_check(cudaMemcpyAsync(q.d_known, q.known.data(), (H + 1) * q.cells, cudaMemcpyHostToDevice, stream_),
-                   "H2D", JC_MAP);
-        recon_init_kernel<<<1024, 256, 0, stream_>>>(q.d_state, q.d_vals, q.d_known, (int)H, (long long)q.cells);
-        cuda_check(cudaGetLastError(), "recon init");
+        cuda_check(cudaMemcpyAsync(q.d_vals, q.device_io ? q.dev_x : q.x.data(), (H + 1) * len * 4, in_kind, stream_),
+                   "reconstruct values", JC_MAP);
+        cuda_check(cudaMemcpyAsync(q.d_known, q.device_io ? q.dev_known : q.known.data(), (H + 1) * q.cells, in_kind,
+                                   stream_),
+                   "reconstruct mask", JC_MAP);
+        g_launches++;
+        recon_fill_kernel<<<1024, 256, 0, stream_>>>(q.d_state, q.d_vals, q.d_known, (int)H, (long long)q.cells);
+        cuda_check(cudaGetLastError(), "reconstruct fill");
     } else {
         q.d_state = static_cast<float*>(get(len * 4));
-        cuda_check(cudaMemcpyAsync(q.d_state, q.x.data(), len * 4, cudaMemcpyHostToDevice, stream_), "H2D", JC_MAP);
+        cuda_check(cudaMemcpyAsync(q.d_state, q.device_io ? q.dev_x : q.x.data(), len * 4, in_kind, stream_), "state",
+                   JC_MAP);
     }
 }
 
-void Server::release(Request& q) {
+void Server::release(Request& q) { release_on(q, stream_); }
+
+void Server::release_on(Request& q, cudaStream_t st) {
     for (void* p : {(void*)q.d_state, (void*)q.d_F, (void*)q.d_R, (void*)q.d_vals, (void*)q.d_known,
-                    (void*)q.d_meta, (void*)q.d_slot, (void*)q.d_resid})
-        if (p) cudaFreeAsync(p, stream_);
+                    (void*)q.d_meta, (void*)q.d_slot})
+        if (p) cudaFreeAsync(p, st);
     q.d_state = q.d_F = q.d_R = q.d_vals = nullptr;
     q.d_known = nullptr;
     q.d_meta = nullptr;
     q.d_slot = nullptr;
-    q.d_resid = nullptr;
 }
 
 void Server::admit_locked() {
     long long cells = 0;
-    for (uint64_t id : active_) cells += reqs_[id].inst_cells();
     int inst = 0;
     for (uint64_t id : active_) {
         const Request& q = reqs_[id];
-        inst += q.r.task == JC_TASK_RECONSTRUCT ? 2 * q.r.ticks : 2;
+        cells += q.inst_cells();
+        inst += q.n_inst();
     }
     while (!pending_.empty()) {
         Request& q = reqs_[pending_.front()];
-        const int qi = q.r.task == JC_TASK_RECONSTRUCT ? 2 * q.r.ticks : 2;
-        if (cells + q.inst_cells() > max_cells_ || inst + qi > max_inst_ || used_bytes_ + q.bytes > budget_bytes_)
+        if (cells + q.inst_cells() > max_cells_ || inst + q.n_inst() > max_inst_ || used_bytes_ + q.bytes > budget_bytes_)
             break;  // first in, first admitted: later requests wait behind it
         pending_.pop_front();
         cells += q.inst_cells();
-        inst += qi;
+        inst += q.n_inst();
         used_bytes_ += q.bytes;
         q.admitted = true;
         q.fresh = true;
@@ -382,9 +447,44 @@ void Server::admit_locked() {
     }
 }
 
+// Ticks of the next chunk. Nothing waits: the longest remaining request, at
+// most about kChunkTargetS of device time (measured per active cell-tick).
+// A request waits for room: up to the first tick after which enough of the
+// active requests have finished to admit it.
+int Server::chunk_length(const std::vector<Request*>& act, long long head_cells, int head_inst) const {
+    int most = 1;
+    long long cells = 0;
+    int inst = 0;
+    std::vector<std::pair<int, Request*>> ends;
+    for (Request* q : act) {
+        const int rem = q->remaining();
+        most = std::max(most, rem);
+        cells += q->inst_cells();
+        inst += q->n_inst();
+        ends.push_back({rem, q});
+    }
+    int K = std::min(most, kMaxChunk);
+    if (head_cells < 0) {
+        if (s_per_cell_tick_ > 0.0 && cells > 0) {
+            const double tick_s = s_per_cell_tick_ * (double)cells;
+            K = std::min(K, std::max(1, (int)(kChunkTargetS / tick_s)));
+        }
+        return K;
+    }
+    std::sort(ends.begin(), ends.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    for (const auto& e : ends) {
+        cells -= e.second->inst_cells();
+        inst -= e.second->n_inst();
+        if (cells + head_cells <= max_cells_ && inst + head_inst <= max_inst_) return std::max(1, std::min(K, e.first));
+    }
+    return K;
+}
+
 void Server::loop() {
     std::vector<Request*> act;
     while (true) {
+        long long head_cells = -1;
+        int head_inst = 0;
         {
             std::unique_lock<std::mutex> lk(mu_);
             admit_locked();
@@ -395,10 +495,17 @@ void Server::loop() {
             if (stop_) return;
             act.clear();
             for (uint64_t id : active_) act.push_back(&reqs_[id]);
+            if (!pending_.empty()) {
+                const Request& h = reqs_[pending_.front()];
+                head_cells = h.inst_cells();
+                head_inst = h.n_inst();
+            }
         }
+        const int K = chunk_length(act, head_cells, head_inst);
         const double t0 = now_s();
+        const long long l0 = g_launches;
         try {
-            iteration(act);
+            iteration(act, K);
         } catch (const std::exception& e) {
             const Error* je = dynamic_cast<const Error*>(&e);
             cudaStreamSynchronize(stream_);
@@ -410,12 +517,14 @@ void Server::loop() {
                 fail_locked(*q, je ? je->code : JC_CUDA_ERROR, e.what());
             }
             active_.clear();
+            span_open_ = false;
             cv_done_.notify_all();
             continue;
         }
         std::lock_guard<std::mutex> lk(mu_);
         busy_s_ += now_s() - t0;
         iterations_++;
+        launches_ += g_launches - l0;
         std::vector<uint64_t> still;
         for (Request* q : act) {
             if (q->finished) {
@@ -423,7 +532,7 @@ void Server::loop() {
                 completed_++;
                 cell_ticks_ += (double)q->cells * q->r.ticks;
                 last_done_ = q->t_done;
-                used_bytes_ -= q->bytes;
+                if (!q->device_io) used_bytes_ -= q->bytes;  // device results free their memory in wait()
             } else {
                 still.push_back(q->id);
             }
@@ -433,14 +542,58 @@ void Server::loop() {
     }
 }
 
-void Server::iteration(std::vector<Request*>& act) {
+namespace {
+
+// The instances of one weight group in a chunk, ordered by the ticks their
+// request has left (longest first), with cumulative sizes so that the
+// instances still running at chunk tick t form a prefix view.
+struct GroupPlan {
+    std::vector<InstDev> inst;
+    std::vector<int> rem;  // per instance: ticks (sweeps) its request has left
+    std::vector<int> rows, tiles, ttiles, ctiles;
+    std::vector<long long> cells, maxc;
+    int inst_base = 0, row_base = 0;
+    long long cell_base = 0;
+    void add(InstDev d, int r) {
+        const int r0 = rows.empty() ? 0 : rows.back();
+        const long long c0 = cells.empty() ? 0 : cells.back();
+        const int t0 = tiles.empty() ? 0 : tiles.back(), tt0 = ttiles.empty() ? 0 : ttiles.back(),
+                  ct0 = ctiles.empty() ? 0 : ctiles.back();
+        d.row0 = r0;
+        d.cell0 = c0;
+        d.tile0 = t0;
+        d.tt0 = tt0;
+        d.ct0 = ct0;
+        inst.push_back(d);
+        rem.push_back(r);
+        rows.push_back(r0 + d.tx * d.ty);
+        cells.push_back(c0 + (long long)d.nx * d.ny);
+        tiles.push_back(t0 + cell_tiles(d.nx, d.ny));
+        ttiles.push_back(tt0 + conv_tiles(d.tx, d.ty));
+        ctiles.push_back(ct0 + conv_tiles(d.nx, d.ny));
+        maxc.push_back(std::max(maxc.empty() ? 0LL : maxc.back(), (long long)d.nx * d.ny));
+    }
+    // instances still running at chunk tick t (rem >= t)
+    int running(int t) const {
+        int n = 0;
+        while (n < (int)rem.size() && rem[n] >= t) n++;
+        return n;
+    }
+    Pack view(const Workspace& ws, const Dims& d, int n) const {
+        Pack v = ws.view(d, inst_base, n, row_base, rows[n - 1], cell_base, cells[n - 1], tiles[n - 1],
+                         ttiles[n - 1], ctiles[n - 1]);
+        v.max_inst_cells = maxc[n - 1];
+        return v;
+    }
+};
+
+}  // namespace
+
+void Server::iteration(std::vector<Request*>& act, int K) {
     cudaStream_t s = stream_;
     // new requests: buffers and inputs on the device
     for (Request* q : act)
         if (q->fresh && !q->d_state) allocate(*q);
-    // descriptor lists: [init (new forward/rewind)] [forward group] [reverse group]
-    std::vector<InstDev> init, fg, rg;
-    std::vector<const Model*> fmod, rmod;
     auto base_inst = [&](const Model& m) {
         InstDev d{};
         d.tx = m.cfg.nx / m.cfg.patch;
@@ -450,9 +603,19 @@ void Server::iteration(std::vector<Request*>& act) {
         d.pos = m.w.pos;
         return d;
     };
-    for (Request* q : act) {
-        const int g = q->r.grid;
-        if (q->r.task == JC_TASK_RECONSTRUCT) {
+    // requests of each group, longest remaining first (stable: admission order)
+    std::vector<Request*> order(act.begin(), act.end());
+    std::stable_sort(order.begin(), order.end(),
+                     [](const Request* a, const Request* b) { return a->remaining() > b->remaining(); });
+    std::vector<InstDev> init, proj;
+    std::vector<int> proj_rem;
+    std::vector<long long> proj_maxc;
+    GroupPlan fg, rg;
+    std::vector<Request*> recon;
+    for (Request* q : order) {
+        const int g = q->r.grid, rem = q->remaining();
+        if (q->recon()) {
+            if (rem <= 0) continue;
             const size_t len = 3 * q->cells;
             for (int t = 1; t <= q->r.ticks; t++) {  // F_t = step_F(X_{t-1})
                 InstDev d = base_inst(*fwd_[g]);
@@ -460,7 +623,7 @@ void Server::iteration(std::vector<Request*>& act) {
                 d.out = q->d_F + (size_t)(t - 1) * len;
                 d.meta = q->d_meta;
                 d.flags = 4u;
-                fg.push_back(d);
+                fg.add(d, rem);
             }
             for (int t = 0; t < q->r.ticks; t++) {  // R_t = step_R(X_{t+1})
                 InstDev d = base_inst(*rev_[g]);
@@ -468,8 +631,9 @@ void Server::iteration(std::vector<Request*>& act) {
                 d.out = q->d_R + (size_t)t * len;
                 d.meta = q->d_meta;
                 d.flags = 4u;
-                rg.push_back(d);
+                rg.add(d, rem);
             }
+            recon.push_back(q);
         } else {
             const Model& m = q->r.task == JC_TASK_FORWARD ? *fwd_[g] : *rev_[g];
             InstDev d = base_inst(m);
@@ -479,132 +643,176 @@ void Server::iteration(std::vector<Request*>& act) {
             d.flags = q->r.flags;
             d.slot = q->d_slot;
             if (q->fresh) init.push_back(d);
-            (q->r.task == JC_TASK_FORWARD ? fg : rg).push_back(d);
+            (q->r.task == JC_TASK_FORWARD ? fg : rg).add(d, rem);
+            proj.push_back(d);
+            proj_rem.push_back(rem);
+            proj_maxc.push_back(std::max(proj_maxc.empty() ? 0LL : proj_maxc.back(), (long long)d.nx * d.ny));
         }
     }
-    // pack offsets per group
-    auto layout = [&](std::vector<InstDev>& v, int& rows, long long& cells, int& tiles, int& tt, int& ct,
-                      long long& maxc) {
-        rows = 0;
-        cells = 0;
-        tiles = tt = ct = 0;
-        maxc = 0;
-        for (InstDev& d : v) {
-            d.row0 = rows;
-            d.cell0 = cells;
-            d.tile0 = tiles;
-            d.tt0 = tt;
-            d.ct0 = ct;
-            rows += d.tx * d.ty;
-            cells += (long long)d.nx * d.ny;
-            tiles += cell_tiles(d.nx, d.ny);
-            tt += conv_tiles(d.tx, d.ty);
-            ct += conv_tiles(d.nx, d.ny);
-            maxc = std::max(maxc, (long long)d.nx * d.ny);
-        }
-    };
-    int fr, ft, ftt, fct, rr, rt, rtt, rct, ir, it_, itt, ict;
-    long long fc, rc, fmax, rmax, ic, imax;
-    layout(fg, fr, fc, ft, ftt, fct, fmax);
-    layout(rg, rr, rc, rt, rtt, rct, rmax);
-    layout(init, ir, ic, it_, itt, ict, imax);
-    const int n_all = (int)(init.size() + fg.size() + rg.size());
+    // descriptor array: [init projections] [forward group] [reverse group]
+    // [tick projections: forward and rewind requests, longest remaining first]
+    fg.inst_base = (int)init.size();
+    rg.inst_base = fg.inst_base + (int)fg.inst.size();
+    rg.row_base = fg.rows.empty() ? 0 : fg.rows.back();
+    rg.cell_base = fg.cells.empty() ? 0 : fg.cells.back();
+    const int proj_base = rg.inst_base + (int)rg.inst.size();
+    const int n_all = proj_base + (int)proj.size();
     if (n_all > max_inst_) throw Error(JC_OVER_BUDGET, "too many instances for the server's descriptor array");
+    if ((long long)rg.row_base + (rg.rows.empty() ? 0 : rg.rows.back()) > ws_.max_rows ||
+        rg.cell_base + (rg.cells.empty() ? 0 : rg.cells.back()) > ws_.max_cells)
+        throw Error(JC_OVER_BUDGET, "the active requests need more cells than the server's workspace holds");
     std::memcpy(h_inst_, init.data(), init.size() * sizeof(InstDev));
-    std::memcpy(h_inst_ + init.size(), fg.data(), fg.size() * sizeof(InstDev));
-    std::memcpy(h_inst_ + init.size() + fg.size(), rg.data(), rg.size() * sizeof(InstDev));
+    std::memcpy(h_inst_ + fg.inst_base, fg.inst.data(), fg.inst.size() * sizeof(InstDev));
+    std::memcpy(h_inst_ + rg.inst_base, rg.inst.data(), rg.inst.size() * sizeof(InstDev));
+    std::memcpy(h_inst_ + proj_base, proj.data(), proj.size() * sizeof(InstDev));
     cuda_check(cudaMemcpyAsync(ws_.base.inst, h_inst_, (size_t)n_all * sizeof(InstDev), cudaMemcpyHostToDevice, s),
                "descriptors", JC_MAP);
-    const int fi = (int)init.size(), ri = fi + (int)fg.size();
-    Pack pf = ws_.view(dims_, fi, (int)fg.size(), 0, fr, 0, fc, ft, ftt, fct);
-    pf.max_inst_cells = fmax;
-    Pack pr = ws_.view(dims_, ri, (int)rg.size(), fr, rr, fc, rc, rt, rtt, rct);
-    pr.max_inst_cells = rmax;
+    // reconstruct bookkeeping, in the same (longest remaining first) order
+    for (size_t i = 0; i < recon.size(); i++) {
+        const Request* q = recon[i];
+        ReconDev& R = h_recon_[i];
+        R = ReconDev{};
+        R.vol = q->d_state;
+        R.F = q->d_F;
+        R.R = q->d_R;
+        R.vals = q->d_vals;
+        R.known = q->d_known;
+        R.cells = (long long)q->cells;
+        R.H = q->r.ticks;
+        R.max_sweeps = q->r.max_sweeps;
+        R.tol = q->r.tol;
+        R.sweeps = q->sweeps;
+        R.frozen = q->frozen;
+        R.last_resid = q->residual;
+    }
+    if (!recon.empty())
+        cuda_check(cudaMemcpyAsync(d_recon_, h_recon_, recon.size() * sizeof(ReconDev), cudaMemcpyHostToDevice, s),
+                   "reconstruct bookkeeping", JC_MAP);
     const BF16Path* bf = fwd_[0]->w.bf16.get();
     if (bf) {
-        if (!fg.empty()) {
-            bf->prepare(dims_, pf, h_inst_ + fi, s);
-            bf->tune(dims_, fwd_[0]->w.f32, pf, s);
+        if (!fg.inst.empty()) {
+            Pack v = fg.view(ws_, dims_, (int)fg.inst.size());
+            bf->prepare(dims_, v, h_inst_ + fg.inst_base, s);
+            bf->tune(dims_, fwd_[0]->w.f32, v, s);
         }
-        if (!rg.empty()) {
-            bf->prepare(dims_, pr, h_inst_ + ri, s);
-            rev_[0]->w.bf16->tune(dims_, rev_[0]->w.f32, pr, s);
-        }
-    }
-    if (!init.empty()) {
-        Pack pi = ws_.view(dims_, 0, (int)init.size(), 0, ir, 0, ic, it_, itt, ict);
-        pi.max_inst_cells = imax;
-        projection(dims_, pi, 1, s);
-    }
-    if (!fg.empty()) {
-        fwd_[0]->forward_pack(pf, kWriteNextState, s);
-        projection(dims_, pf, 0, s);
-    }
-    if (!rg.empty()) {
-        rev_[0]->forward_pack(pr, kWriteNextState, s);
-        projection(dims_, pr, 0, s);
-    }
-    std::vector<Request*> recon;
-    for (Request* q : act) {
-        q->fresh = false;
-        if (q->r.task == JC_TASK_RECONSTRUCT) {
-            cuda_check(cudaMemsetAsync(q->d_resid, 0, 4, s), "memset");
-            recon_update_kernel<<<1024, 256, 0, s>>>(q->d_state, q->d_F, q->d_R, q->d_vals, q->d_known, q->r.ticks,
-                                                     (long long)q->cells, q->d_resid);
-            cuda_check(cudaGetLastError(), "recon update");
-            recon.push_back(q);
+        if (!rg.inst.empty()) {
+            Pack v = rg.view(ws_, dims_, (int)rg.inst.size());
+            bf->prepare(dims_, v, h_inst_ + rg.inst_base, s);
+            rev_[0]->w.bf16->tune(dims_, rev_[0]->w.f32, v, s);
         }
     }
-    // results of forward/rewind requests that finish with this tick
+    // the chunk: K ticks with no host round trip
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!span_open_) {
+            cuda_check(cudaEventRecord(ev_first_, s), "cudaEventRecord");
+            span_open_ = true;
+        }
+    }
+    cuda_check(cudaEventRecord(ev_a_, s), "cudaEventRecord");
+    long long cell_ticks = 0;
+    for (int t = 1; t <= K; t++) {
+        if (t == 1 && !init.empty()) {
+            Pack pi = ws_.view(dims_, 0, (int)init.size(), 0, 0, 0, 0, 0, 0, 0);
+            long long mx = 0;
+            for (const InstDev& d : init) mx = std::max(mx, (long long)d.nx * d.ny);
+            pi.max_inst_cells = mx;
+            projection(dims_, pi, 1, s);
+        }
+        const int nf = fg.running(t), nr = rg.running(t);
+        if (nf) {
+            Pack v = fg.view(ws_, dims_, nf);
+            fwd_[0]->forward_pack(v, kWriteNextState, s);
+            cell_ticks += v.NC;
+        }
+        if (nr) {
+            Pack v = rg.view(ws_, dims_, nr);
+            rev_[0]->forward_pack(v, kWriteNextState, s);
+            cell_ticks += v.NC;
+        }
+        int np = 0;
+        while (np < (int)proj.size() && proj_rem[np] >= t) np++;
+        if (np) {
+            Pack pv = ws_.view(dims_, proj_base, np, 0, 0, 0, 0, 0, 0, 0);
+            pv.max_inst_cells = proj_maxc[np - 1];
+            projection(dims_, pv, 0, s);
+        }
+        int nrec = 0;
+        while (nrec < (int)recon.size() && recon[nrec]->remaining() >= t) nrec++;
+        if (nrec) {
+            recon_update(d_recon_, nrec, s);
+            recon_finalize(d_recon_, nrec, 0ull, 0, s);
+        }
+    }
+    cuda_check(cudaEventRecord(ev_b_, s), "cudaEventRecord");
+    // results of forward/rewind requests that finish in this chunk
     std::vector<Request*> finishing;
     for (Request* q : act) {
-        if (q->r.task == JC_TASK_RECONSTRUCT) continue;
-        if (q->ticks_done + 1 == q->r.ticks) {
+        if (q->recon() || q->remaining() > K) continue;
+        if (!q->device_io) {
             q->out.resize(3 * q->cells);
-            cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s), "D2H",
-                       JC_MAP);
-            finishing.push_back(q);
+            cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s),
+                       "D2H", JC_MAP);
         }
+        cuda_check(cudaMemcpyAsync(&h_slots_[finishing.size()], q->d_slot, sizeof(ProjSlot), cudaMemcpyDeviceToHost, s),
+                   "D2H", JC_MAP);
+        finishing.push_back(q);
     }
-    std::vector<unsigned> resid(recon.size());
-    std::vector<ProjSlot> slots(finishing.size());
-    for (size_t i = 0; i < recon.size(); i++)
-        cuda_check(cudaMemcpyAsync(&resid[i], recon[i]->d_resid, 4, cudaMemcpyDeviceToHost, s), "D2H", JC_MAP);
-    for (size_t i = 0; i < finishing.size(); i++)
-        cuda_check(cudaMemcpyAsync(&slots[i], finishing[i]->d_slot, sizeof(ProjSlot), cudaMemcpyDeviceToHost, s),
+    if (!recon.empty())
+        cuda_check(cudaMemcpyAsync(h_recon_, d_recon_, recon.size() * sizeof(ReconDev), cudaMemcpyDeviceToHost, s),
                    "D2H", JC_MAP);
     cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
     ws_.check_timeout(s);
+    {
+        float ms = 0.f, span = 0.f;
+        cudaEventElapsedTime(&ms, ev_a_, ev_b_);
+        cudaEventElapsedTime(&span, ev_first_, ev_b_);
+        if (cell_ticks > 0 && ms > 0.f) {
+            const double v = ms * 1e-3 / (double)cell_ticks;
+            s_per_cell_tick_ = s_per_cell_tick_ > 0.0 ? 0.5 * (s_per_cell_tick_ + v) : v;
+        }
+        std::lock_guard<std::mutex> lk(mu_);
+        device_span_s_ = span * 1e-3;
+    }
     const double t = now_s();
     for (size_t i = 0; i < finishing.size(); i++) {
         Request* q = finishing[i];
-        q->energy = slots[i].energy;
-        q->max_viol = slots[i].max_viol;
+        q->energy = h_slots_[i].energy;
+        q->max_viol = h_slots_[i].max_viol;
     }
     for (Request* q : act) {
-        if (q->r.task != JC_TASK_RECONSTRUCT) {
-            q->ticks_done++;
-            if (q->ticks_done == q->r.ticks) {
-                release(*q);
-                q->finished = true;
-                q->t_done = t;
-            }
+        q->fresh = false;
+        if (q->recon()) continue;
+        const int rem = q->remaining();
+        q->ticks_done += std::min(rem, K);
+        if (q->ticks_done == q->r.ticks) {
+            if (!q->device_io) release(*q);
+            q->finished = true;
+            q->t_done = t;
         }
     }
+    std::vector<Request*> recon_done;
     for (size_t i = 0; i < recon.size(); i++) {
         Request* q = recon[i];
-        q->sweeps++;
-        float r;
-        std::memcpy(&r, &resid[i], 4);
-        q->residual = r;
-        if (r < q->r.tol || q->sweeps >= q->r.max_sweeps) {
-            q->out.resize((size_t)(q->r.ticks + 1) * 3 * q->cells);
-            cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s), "D2H",
-                       JC_MAP);
-            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
-            release(*q);
+        q->sweeps = h_recon_[i].sweeps;
+        q->frozen = h_recon_[i].frozen;
+        q->residual = h_recon_[i].last_resid;
+        if (q->frozen) {
+            if (!q->device_io) {
+                q->out.resize(q->out_floats());
+                cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s),
+                           "D2H", JC_MAP);
+            }
+            recon_done.push_back(q);
+        }
+    }
+    if (!recon_done.empty()) {
+        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
+        const double t2 = now_s();
+        for (Request* q : recon_done) {
+            if (!q->device_io) release(*q);
             q->finished = true;
-            q->t_done = now_s();
+            q->t_done = t2;
         }
     }
 }
@@ -630,4 +838,5 @@ void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* inf
     s->s->wait(id, out, n, info, timeout);
 }
 void server_stats(jc_server* s, jc_server_stats* st) { s->s->stats(st); }
+void server_reset_stats(jc_server* s) { s->s->reset_stats(); }
 }  // namespace jc

@@ -389,10 +389,14 @@ class JcResult(C.Structure):
 
 class JcServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("cell_ticks", C.c_double), ("busy_s", C.c_double), ("span_s", C.c_double),
-                ("iterations", C.c_int32), ("active", C.c_int32), ("pending", C.c_int32)]
+                ("iterations", C.c_int32), ("active", C.c_int32), ("pending", C.c_int32),
+                ("device_span_s", C.c_double), ("launches", C.c_int64)]
 
 
-EXPORTED += ["jc_server_create", "jc_server_destroy", "jc_server_submit", "jc_server_wait", "jc_server_get_stats"]
+REQUEST_DEVICE_BUFFERS = 0x100
+
+EXPORTED += ["jc_server_create", "jc_server_destroy", "jc_server_submit", "jc_server_wait", "jc_server_get_stats",
+             "jc_server_reset_stats"]
 
 
 def _declare_server(L):
@@ -409,6 +413,8 @@ def _declare_server(L):
     L.jc_server_wait.restype = C.c_int
     L.jc_server_get_stats.argtypes = [vp, C.POINTER(JcServerStats)]
     L.jc_server_get_stats.restype = C.c_int
+    L.jc_server_reset_stats.argtypes = [vp]
+    L.jc_server_reset_stats.restype = C.c_int
     L._server_declared = True
 
 
@@ -461,6 +467,26 @@ class Server:
         req = JcRequest(int(task), int(grid), int(ticks), int(flags), xa.ctypes.data,
                         ka.ctypes.data if ka is not None else None, ma.ctypes.data, int(max_sweeps), float(tol))
         return self._submit(req)  # inputs are copied by the call
+
+    def submit_device(self, task: int, grid: int, x_ptr: int, meta_ptr: int, ticks: int,
+                      flags: int = PROJECT_MASS | PROJECT_ENERGY, known_ptr: int | None = None, max_sweeps: int = 4,
+                      tol: float = 1e-3) -> int:
+        """submit() with device-resident inputs (device pointers that must stay
+        valid until the request is done); collect with wait_device()."""
+        req = JcRequest(int(task), int(grid), int(ticks), int(flags) | REQUEST_DEVICE_BUFFERS, int(x_ptr),
+                        int(known_ptr) if known_ptr else None, int(meta_ptr), int(max_sweeps), float(tol))
+        return self._submit(req)
+
+    def wait_device(self, rid: int, out_ptr: int | None, out_len: int, timeout: float = -1.0) -> dict:
+        """Waits for a request submitted with submit_device and copies its
+        result to the device pointer `out_ptr` (out_len floats; None: drop it)."""
+        info = JcResult()
+        _check(self._L.jc_server_wait(self._h, int(rid), int(out_ptr) if out_ptr else None, int(out_len),
+                                      C.byref(info), float(timeout)))
+        return {f: getattr(info, f) for f, _ in JcResult._fields_}
+
+    def reset_stats(self) -> None:
+        _check(self._L.jc_server_reset_stats(self._h))
 
     def out_shape(self, task: int, grid: int, ticks: int):
         c = self.forward_models[grid].config

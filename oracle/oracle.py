@@ -409,6 +409,38 @@ def roundtrip(forward: "OracleModel", reverse: "OracleModel", drops, horizons, f
     return rows
 
 
+def reconstruct(forward: "OracleModel", reverse: "OracleModel", vals, known, meta, sweeps: int, tol: float = 0.0):
+    """The reconstruct rule on the f32 oracle (no reference counterpart; the
+    library's JC_TASK_RECONSTRUCT): from X = known ? value : 0, each sweep
+    sets X_t <- known_t ? value : mean of step_F(X_{t-1}) and step_R(X_{t+1})
+    where they exist (one-sided at t = 0 and t = H), until the largest change
+    of an unknown value is below tol or `sweeps` sweeps ran. Returns (X,
+    sweeps run, last largest change)."""
+    vals = np.asarray(vals, dtype=np.float32)
+    known = np.asarray(known).astype(bool)
+    H = vals.shape[0] - 1
+    X = np.where(known[:, None], vals, np.float32(0.0)).astype(np.float32)
+    resid, k = 0.0, 0
+    for k in range(1, sweeps + 1):
+        F = [forward.step(X[t - 1], meta) for t in range(1, H + 1)]
+        R = [reverse.step(X[t + 1], meta) for t in range(0, H)]
+        new = np.empty_like(X)
+        for t in range(H + 1):
+            if t == 0:
+                v = R[0]
+            elif t == H:
+                v = F[H - 1]
+            else:
+                v = np.float32(0.5) * (F[t - 1] + R[t])
+            new[t] = np.where(known[t][None], vals[t], v)
+        unknown = ~np.broadcast_to(known[:, None], X.shape)
+        resid = float(np.abs(new - X)[unknown].max()) if unknown.any() else 0.0
+        X = new
+        if resid < tol:
+            break
+    return X, k, resid
+
+
 def identity_config(n: int, g: float = 9.81, r_max: float = 1.0):
     """A config with identity normalization over an n-cell strip, for the
     projection unit cases of crates/engine/src/project.rs:64-102."""

@@ -17,7 +17,7 @@ def _run(extra_env=None, *args):
     env = dict(os.environ)
     env.update(extra_env or {})
     cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-           "--side", "32", "--ref-step-ticks", "1", *args]
+           "--ref-requests", "2", "--ref-horizon", "1", *args]
     r = subprocess.run(cmd, capture_output=True, text=True, env=env, cwd=ROOT, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     return [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -32,7 +32,7 @@ def test_reference_arm_prints_one_contract_line():
         assert key in line, key
     assert line["impl"] == "reference" and line["unit"] == "cell-ticks/s" and line["higher_is_better"] is True
     assert line["value"] > 0 and line["steps"] == 1 and line["n_gpus"] == 1
-    assert line["config"]["workload"] and line["config"]["grid"] == [32, 32]
+    assert line["config"]["workload"] and line["config"]["sides"] == [32, 256, 4]
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,

@@ -169,3 +169,92 @@ def test_submissions_from_many_threads(families):
     for k, (g, x, out) in results.items():
         alone, _ = fm[g].rollout(x, meta_of(cfgs[g]), 4, ME)
         assert np.array_equal(out, alone)
+
+
+def test_device_buffer_requests_equal_host_requests(families):
+    """Requests whose inputs and results are device memory
+    (JC_REQUEST_DEVICE_BUFFERS) give the same bits as host-buffer requests
+    and as the model's own rollout; the server's device-timed span covers
+    the work."""
+    torch = pytest.importorskip("torch")
+    (fm, _, cfgs), (rm, _, _) = families
+    rng = np.random.default_rng(11)
+    reqs = []
+    for k in range(6):
+        task = (engine.TASK_FORWARD, engine.TASK_REWIND, engine.TASK_RECONSTRUCT)[k % 3]
+        g = int(rng.integers(0, len(SIDES)))
+        cfg = cfgs[g]
+        H = int(rng.integers(2, 7))
+        if task == engine.TASK_RECONSTRUCT:
+            known = (rng.random((H + 1, cfg.ny, cfg.nx)) < 0.05).astype(np.uint8)
+            x = np.where(known[:, None], 0.3 * rng.standard_normal((H + 1, 3, cfg.ny, cfg.nx)), 0).astype(np.float32)
+        else:
+            known, x = None, random_drops(cfg, seed=300 + k)
+        reqs.append((task, g, H, x, known, meta_of(cfg)))
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        host = []
+        for task, g, H, x, known, meta in reqs:
+            rid = srv.submit(task, g, x, meta, H, ME, known=known, max_sweeps=3, tol=0.0)
+            host.append(srv.wait(rid, task, g, H, timeout=60)[0])
+        srv.reset_stats()
+        dev_in = [(torch.from_numpy(np.ascontiguousarray(x)).cuda(),
+                   torch.from_numpy(np.ascontiguousarray(known)).cuda() if known is not None else None,
+                   torch.from_numpy(np.ascontiguousarray(meta)).cuda()) for _, _, _, x, known, meta in reqs]
+        outs = [torch.empty(srv.out_shape(task, g, H), device="cuda") for task, g, H, _, _, _ in reqs]
+        torch.cuda.synchronize()
+        ids = [srv.submit_device(task, g, dx.data_ptr(), dm.data_ptr(), H, ME,
+                                 known_ptr=dk.data_ptr() if dk is not None else None, max_sweeps=3, tol=0.0)
+               for (task, g, H, _, _, _), (dx, dk, dm) in zip(reqs, dev_in)]
+        for rid, o in zip(ids, outs):
+            srv.wait_device(rid, o.data_ptr(), o.numel(), timeout=60)
+        st = srv.stats()
+    for (task, g, H, x, known, meta), h, o in zip(reqs, host, outs):
+        assert np.array_equal(o.cpu().numpy(), h), (task, g, H)
+        if task != engine.TASK_RECONSTRUCT:
+            model = fm[g] if task == engine.TASK_FORWARD else rm[g]
+            assert np.array_equal(h, model.rollout(x, meta, H, ME)[0])
+    assert st["completed"] == len(reqs)
+    assert 0 < st["device_span_s"] <= st["span_s"] + 1e-3
+
+
+def test_reconstruct_that_converges_early_matches_the_batch_runner(families):
+    """A tolerance that stops the sweeps before max_sweeps: the server (where
+    the request may freeze in the middle of a chunk while other requests run
+    on) and the batch runner (a graph while loop that ends on the device)
+    apply the same rule, so their volumes, sweep counts and residuals agree
+    bit for bit, alone and in a mix."""
+    (fm, _, cfgs), (rm, _, _) = families
+    g, H = 0, 3
+    cfg = cfgs[g]
+    rng = np.random.default_rng(9)
+    known = (rng.random((H + 1, cfg.ny, cfg.nx)) < 0.1).astype(np.uint8)
+    known[0] = 1
+    vals = np.where(known[:, None], np.stack([random_drops(cfg, seed=60 + t) for t in range(H + 1)]), 0)
+    vals = vals.astype(np.float32)
+    meta = meta_of(cfg)
+    n = len(SIDES)
+    with engine.Batch(fm + rm, max_instances=64, max_cells=1 << 16) as b:
+        # the residual after each sweep count, with a tolerance of 0; a
+        # tolerance just above the fifth makes the sweeps stop early
+        item = {"task": engine.TASK_RECONSTRUCT, "model": g, "reverse_model": g + n, "x": vals, "known": known,
+                "meta": meta, "ticks": H, "max_sweeps": 12, "tol": 0.0}
+        sweeps_res = []
+        for s in range(1, 13):
+            item["max_sweeps"] = s
+            sweeps_res.append(b.rollout([item])[0][2])
+        tol = float(sweeps_res[4]) * 1.0001
+        item["max_sweeps"], item["tol"] = 12, tol
+        (want, w_sweeps, w_resid), = b.rollout([item])
+    assert int(w_sweeps) < 12
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        rid = srv.submit(engine.TASK_RECONSTRUCT, g, vals, meta, H, known=known, max_sweeps=12, tol=tol)
+        alone, info = srv.wait(rid, engine.TASK_RECONSTRUCT, g, H, timeout=60)
+        others = [srv.submit(engine.TASK_FORWARD, k % 3, random_drops(cfgs[k % 3], seed=k), meta_of(cfgs[k % 3]),
+                             20) for k in range(4)]
+        rid = srv.submit(engine.TASK_RECONSTRUCT, g, vals, meta, H, known=known, max_sweeps=12, tol=tol)
+        mixed, info2 = srv.wait(rid, engine.TASK_RECONSTRUCT, g, H, timeout=60)
+        for i, k in zip(others, range(4)):
+            srv.wait(i, engine.TASK_FORWARD, k % 3, 20, timeout=60)
+    assert np.array_equal(alone, want) and np.array_equal(mixed, want)
+    assert info["sweeps"] == info2["sweeps"] == int(w_sweeps)
+    assert info["residual"] == info2["residual"] == np.float32(w_resid)
