@@ -189,7 +189,7 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
 # ---- the served workload (the metric's configuration) ------------------------------------
 
 C5_SIDES = list(range(32, 257, 4))  # grid sides: log-uniform in [32, 256], rounded to a multiple of 4
-C5_RATES = [10.0, 30.0, 100.0, 300.0, 1000.0, 2000.0]
+C5_RATES = [10.0, 40.0, 100.0, 400.0, 1000.0, 2000.0]
 C5_SWEEPS = 4         # reconstruct: Jacobi sweeps (tolerance 0: every sweep runs)
 C5_KNOWN = 0.02       # reconstruct: fraction of space-time cells known
 C5_MAX_CELLS = 8 << 20

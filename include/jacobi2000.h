@@ -306,12 +306,12 @@ void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int
  * default; environment JC_AUTOTUNE=0 starts with it off) the first BF16
  * launch outside a stream capture for each row-count bucket (powers of two of
  * token rows) times the candidate schedules with CUDA events, once, and later
- * launches and graph captures use the fastest: the fused MLP (serial,
- * pipelined or persistent warp-specialised kernel; 32 or 64 hidden columns
- * per step; weight stages) and the attention (shared-memory tiles, or one
- * thread per (row, head) in 64-, 128- or 256-thread CTAs). enable = 0 selects
- * the fixed schedule (serial MLP with 64 columns; attention tiles where the
- * mask is radius 1, dilation 1, else 256 threads); enable < 0 only queries.
+ * launches and graph captures use the fastest: the fused MLP's hidden chunk
+ * width (32 or 64 columns per step) and the attention's form (shared-memory
+ * tiles, or one thread per (row, head) in 64-, 128- or 256-thread CTAs).
+ * enable = 0 selects the fixed schedule (64 columns; attention tiles where
+ * the mask is radius 1, dilation 1, else 256 threads); enable < 0 only
+ * queries.
  * Returns the setting before the call. If JC_AUTOTUNE_CACHE names a file,
  * tuned schedules (with the candidates' times) are appended to it as JSON
  * lines and read back by models created later. Results are identical under

@@ -724,115 +724,6 @@ __global__ void __launch_bounds__(64 * (64 / HD), 5) bf_attn_tile_kernel(Dims d,
     store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
 }
 
-// The same stencil attention with persistent CTAs: a CTA walks the work
-// items (token tile, 8 x 8 half, 64-channel box; item = (2 tile + half) *
-// boxes + box) with stride gridDim.x, through two stages of [key halo, value
-// halo, query] boxes in shared memory. The boxes of the item two steps ahead
-// load by TMA while this item is computed, so a CTA's loads overlap its
-// arithmetic instead of preceding it. Each output is computed exactly as in
-// bf_attn_tile_kernel (same per-thread order, same bits).
-constexpr int kAttStage = 2 * kAttBoxKVPad + kAttBoxQ;  // 34 KB, a multiple of 1024
-constexpr size_t kAttRingSmem = 2 * (size_t)kAttStage;
-
-template <int HD>
-__global__ void __launch_bounds__(128) bf_attn_ring_kernel(Dims d, const CUtensorMap* __restrict__ maps, int kv_slot,
-                                                           int q_slot, const InstDev* inst, int n_inst, int n_ttiles,
-                                                           bf16* __restrict__ out, int* err) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    const int D = d.D;
-    constexpr int HPB = 64 / HD;
-    const int nb = D / 64;
-    const int n_items = n_ttiles * 2 * nb;
-    __shared__ uint64_t bar[2];
-    __shared__ volatile int failed;
-    // item -> instance, token-space origin of its 8 x 8 half, box; false for
-    // the lower half of a tile that overhangs the grid (no load, no work)
-    auto decode = [&](int item, int& lo, int& x0, int& y0, int& bx) {
-        bx = item % nb;
-        const int th = item / nb, tile = th >> 1, half = th & 1;
-        lo = 0;
-        int hi = n_inst - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (inst[mid].tt0 <= tile) lo = mid; else hi = mid - 1;
-        }
-        const int tiles_x = (inst[lo].tx + kConvTX - 1) / kConvTX;
-        const int tl = tile - inst[lo].tt0;
-        x0 = (tl % tiles_x) * kConvTX;
-        y0 = (tl / tiles_x) * kConvTY + half * kAttTile;
-        return y0 < inst[lo].ty;
-    };
-    if (threadIdx.x == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
-        tc::fence_barrier_init();
-        failed = 0;
-        if (tc::smem_u32(smem) & 1023u) {
-            failed = 1;
-            atomicExch(err, 2);
-        }
-    }
-    __syncthreads();
-    JC_PDL_ENTRY;
-    unsigned pending = 0;  // stages with a load in flight (thread 0's view)
-    auto issue = [&](int item, int s) {
-        int lo, x0, y0, bx;
-        if (!decode(item, lo, x0, y0, bx)) return;
-        const CUtensorMap* mkv = maps + kMapsPerInst * lo + kv_slot;
-        const CUtensorMap* mq = maps + kMapsPerInst * lo + q_slot;
-        uint8_t* st = smem + (size_t)s * kAttStage;
-        tc::tensormap_acquire(mkv);
-        tc::tensormap_acquire(mq);
-        tc::mbar_expect_tx(&bar[s], (uint32_t)(2 * kAttBoxKV + kAttBoxQ));
-        tc::tma_load_3d(st, mkv, D + 64 * bx, x0 - 1, y0 - 1, &bar[s]);
-        tc::tma_load_3d(st + kAttBoxKVPad, mkv, 2 * D + 64 * bx, x0 - 1, y0 - 1, &bar[s]);
-        tc::tma_load_3d(st + 2 * kAttBoxKVPad, mq, 64 * bx, x0, y0, &bar[s]);
-        pending |= 1u << s;
-    };
-    if (threadIdx.x == 0 && !failed) {
-        if ((int)blockIdx.x < n_items) issue(blockIdx.x, 0);
-        if ((int)(blockIdx.x + gridDim.x) < n_items) issue(blockIdx.x + gridDim.x, 1);
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int hl = warp % HPB;                 // head within the box
-    const int tok = (warp / HPB) * 32 + lane;  // 0..63 within the half tile
-    const int lx = tok & 7, ly = tok >> 3;
-    const float scale = 1.0f / sqrtf((float)HD);
-    unsigned phase = 0;  // parity of each stage's next completion
-    int k = 0;
-    for (int item = blockIdx.x; item < n_items; item += gridDim.x, k++) {
-        const int s = k & 1;
-        int lo, x0, y0, bx;
-        if (decode(item, lo, x0, y0, bx)) {  // uniform per CTA
-            const bool ok =
-                __syncthreads_and(tc::mbar_wait(&bar[s], (phase >> s) & 1u, err, &failed) ? 1 : 0) != 0;
-            if (!ok) break;
-            phase ^= 1u << s;
-            if (threadIdx.x == 0) pending &= ~(1u << s);
-            const InstDev& I = inst[lo];
-            const uint8_t* sK = smem + (size_t)s * kAttStage;
-            const uint8_t* sV = sK + kAttBoxKVPad;
-            const uint8_t* sQ = sV + kAttBoxKVPad;
-            const int qx = x0 + lx, qy = y0 + ly;
-            if (qx < I.tx && qy < I.ty) {
-                float acc[HD];
-                attn_stencil_token<HD>(sQ, sK, sV, lx, ly, qx, qy, I.tx, I.ty, hl, scale, acc);
-                store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + (bx * HPB + hl) * HD, acc);
-            }
-        }
-        __syncthreads();  // stage s is free
-        if (threadIdx.x == 0 && !failed && item + 2 * (int)gridDim.x < n_items) issue(item + 2 * gridDim.x, s);
-    }
-    // after a failed wait: let this CTA's copies still in flight land (bounded)
-    if (threadIdx.x == 0 && pending) {
-        const unsigned long long t0 = tc::globaltimer();
-        for (int s = 0; s < 2; s++)
-            if (pending & (1u << s))
-                while (!tc::mbar_try_wait(&bar[s], (phase >> s) & 1u) && tc::globaltimer() - t0 < tc::kWaitNs) {
-                }
-    }
-}
-
 // to_cells' output (f32 [rows, HD]) -> the cell-head input zc (f16 [cells,
 // 48], conv1's operand type): upsample along y then x (cpu.rs:211-245;
 // weights (i + 1/2) / P, the far neighbour clamped to the grid), the state
@@ -1342,213 +1233,14 @@ __device__ __forceinline__ void row_resid_ln(uint32_t ta, int r, int D, uint8_t*
 constexpr int kLnMaxD = 128;  // widest row the row-per-thread LayerNorm serves
 
 // Fused MLP: x += gelu(LN2(x) @ W1 + b1) @ W2 + b2, then LayerNorm of the new
-// x (the next block's norm1, or the final norm) into `ln`. The hidden layer
-// is walked in chunks of NC columns: S_j = A @ W1_j (TMEM), h_j = gelu(S_j +
-// b1_j) as bf16 in shared memory, O += h_j @ W2_j (TMEM); the hidden
-// activations never leave the SM.
-//
-// Warp-specialised and pipelined: warp 8 (one elected lane) streams the
-// weight chunks through an NS-stage shared-memory ring and issues every MMA;
-// warps 0-7 (two per TMEM lane quarter, one half of the chunk's columns each)
-// turn S_j into h_j. S and h are double-buffered, so S_{j+1} / S_{j+2} and
-// O += h_{j-1} W2_{j-1} run on the tensor core while the GELU warps work on
-// chunk j. All nine warps run the residual + LayerNorm epilogue from a
-// shared-memory copy of O. Every summation order is fixed by NC-independent
-// K slices of 16, so every chunk width gives the same bits.
-constexpr int kMlpWarps = 8;                       // GELU / epilogue warps
-constexpr int kMlpThreads = (kMlpWarps + 1) * 32;  // + the producer / MMA warp
-
-struct MlpSmem {
-    int D, NC, NS;
-    size_t a, w, h, b1, total, tile;
-    __host__ __device__ MlpSmem(int D_, int F, int NC_, int NS_) : D(D_), NC(NC_), NS(NS_) {
-        a = 0;                                           // [D/8][128][8]
-        w = a + (size_t)D * 256;                         // NS x ([D/8][NC][8] W1 | [NC/8][D][8] W2)
-        h = w + (size_t)NS * 4 * D * NC;                 // 2 x [NC/8][128][8]
-        b1 = h + (size_t)2 * NC * 256;                   // [F] f32
-        total = b1 + (size_t)F * 4;
-        tile = (size_t)128 * D * 4;                      // epilogue: f32 [128][D]
-        if (tile > total) total = tile;
-    }
-};
-
-__global__ void __launch_bounds__(kMlpThreads, 2) tc_mlp_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                             const bf16* __restrict__ W1, const bf16* __restrict__ W2,
-                                                             const float* __restrict__ b1,
-                                                             const float* __restrict__ b2, int D, int F, int NC, int NS,
-                                                             int R, float* __restrict__ x, const float* __restrict__ g,
-                                                             const float* __restrict__ b, bf16* __restrict__ ln,
-                                                             int* err) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    const MlpSmem L(D, F, NC, NS);
-    uint8_t* sA = smem + L.a;
-    uint8_t* sW = smem + L.w;
-    uint8_t* sH = smem + L.h;
-    float* sb1 = reinterpret_cast<float*>(smem + L.b1);
-    constexpr int kMaxStages = 4;
-    __shared__ uint64_t bar_a, bar_o, bar_w[kMaxStages], bar_wfree[kMaxStages], bar_s[2], bar_h[2], bar_hfree[2];
-    __shared__ uint32_t tmem_base;
-    __shared__ volatile int failed;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * 128;
-    const int nch = F / NC;
-    const uint32_t s_col = (uint32_t)(D < 64 ? 64 : D);
-    uint32_t ncols = 32;
-    while (ncols < s_col + 2u * NC) ncols <<= 1;
-    if (threadIdx.x == 0) {
-        tc::mbar_init(&bar_a, 1);
-        tc::mbar_init(&bar_o, 1);
-        for (int i = 0; i < NS; i++) {
-            tc::mbar_init(&bar_w[i], 1);
-            tc::mbar_init(&bar_wfree[i], 1);
-        }
-        for (int i = 0; i < 2; i++) {
-            tc::mbar_init(&bar_s[i], 1);
-            tc::mbar_init(&bar_h[i], kMlpWarps * 32);
-            tc::mbar_init(&bar_hfree[i], 1);
-        }
-        tc::fence_barrier_init();
-        failed = 0;
-        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages) {
-            failed = 1;
-            atomicExch(err, 2);
-        }
-    }
-    for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
-    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
-    tc::tc_fence_before();
-    __syncthreads();
-    JC_PDL_ENTRY;
-    tc::tc_fence_after();
-    const uint32_t tO = tmem_base;
-    const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
-    bool ok = !failed;
-    if (warp == kMlpWarps) {
-        if (lane == 0 && ok) {
-            // producer + MMA issuer
-            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH), w0 = tc::smem_u32(sW);
-            auto load_w = [&](int j) {
-                uint64_t* bar = &bar_w[j % NS];
-                uint8_t* dst = sW + (size_t)(j % NS) * 2 * wbytes;
-                tc::mbar_expect_tx(bar, 2 * wbytes);
-                tc::bulk_load(dst, W1 + (size_t)j * D * NC, wbytes, bar);
-                tc::bulk_load(dst + wbytes, W2 + (size_t)j * D * NC, wbytes, bar);
-            };
-            auto issue_s = [&](int j) -> bool {
-                if (!tc::mbar_wait(&bar_w[j % NS], (uint32_t)(j / NS) & 1u, err, &failed)) return false;
-                tc::tc_fence_after();
-                const uint32_t ws = w0 + (uint32_t)(j % NS) * 2 * wbytes;
-                const uint32_t idesc = tc::idesc_bf16(128, NC);
-                const uint32_t tS = tO + s_col + (uint32_t)(j & 1) * NC;
-                for (int k = 0; k < D / 16; k++)
-                    tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(ws + k * 2 * NC * 16, NC * 16, 128),
-                                 idesc, k > 0 ? 1u : 0u);
-                tc::mma_commit(&bar_s[j & 1]);
-                return true;
-            };
-            tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
-            for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &bar_a);
-            for (int j = 0; j < NS && j < nch; j++) load_w(j);
-            bool good = tc::mbar_wait(&bar_a, 0, err, &failed);
-            for (int j = 0; j < 2 && j < nch && good; j++) good = issue_s(j);
-            for (int j = 0; j < nch && good; j++) {
-                if (!tc::mbar_wait(&bar_h[j & 1], (uint32_t)(j >> 1) & 1u, err, &failed)) {
-                    good = false;
-                    break;
-                }
-                tc::tc_fence_after();
-                const uint32_t ws2 = w0 + (uint32_t)(j % NS) * 2 * wbytes + wbytes;
-                const uint32_t hs = h0 + (uint32_t)(j & 1) * NC * 256;
-                const uint32_t idesc = tc::idesc_bf16(128, D);
-                for (int k = 0; k < NC / 16; k++)
-                    tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(ws2 + k * 2 * D * 16, D * 16, 128),
-                                 idesc, (j > 0 || k > 0) ? 1u : 0u);
-                tc::mma_commit(&bar_wfree[j % NS]);
-                tc::mma_commit(&bar_hfree[j & 1]);
-                // refill the stage O_j used with chunk j + NS once O_j is done;
-                // with two stages that chunk is the one S_{j+2} needs, so the
-                // refill comes first, otherwise S_{j+2} (loaded earlier) does
-                auto refill = [&]() -> bool {
-                    if (j + NS >= nch) return true;
-                    if (!tc::mbar_wait(&bar_wfree[j % NS], (uint32_t)(j / NS) & 1u, err, &failed)) return false;
-                    load_w(j + NS);
-                    return true;
-                };
-                if (NS == 2 && !refill()) {
-                    good = false;
-                    break;
-                }
-                if (j + 2 < nch && !issue_s(j + 2)) {
-                    good = false;
-                    break;
-                }
-                if (NS > 2 && !refill()) {
-                    good = false;
-                    break;
-                }
-            }
-            if (good) tc::mma_commit(&bar_o);
-        }
-        __syncwarp();
-    } else if (ok) {
-        // GELU warps: chunk j's S (TMEM) -> h_j (bf16, core-matrix layout)
-        const int quarter = warp & 3, half = warp >> 2;
-        const int r = quarter * 32 + lane;
-        const int cw = NC / 2;  // columns per warp half: 16 or 32
-        for (int j = 0; j < nch; j++) {
-            const bool s_ready = tc::mbar_wait(&bar_s[j & 1], (uint32_t)(j >> 1) & 1u, err, &failed);
-            const bool h_free = j < 2 || tc::mbar_wait(&bar_hfree[j & 1], (uint32_t)((j - 2) >> 1) & 1u, err, &failed);
-            // the TMEM load below is warp-collective: every lane runs it, and a
-            // failed wait anywhere ends the loop for the whole warp
-            if (!__all_sync(0xffffffffu, s_ready && h_free)) break;
-            tc::tc_fence_after();
-            const uint32_t ta = lane_addr(tO + s_col + (uint32_t)(j & 1) * NC);
-            uint8_t* hb = sH + (size_t)(j & 1) * NC * 256;
-            for (int c = half * cw; c < (half + 1) * cw; c += 16) {
-                float a[16];
-                tc::tmem_ld16(ta + c, a);
-                const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const float4 bv = bb[i];
-                    a[4 * i] = gelu_fast(a[4 * i] + bv.x);
-                    a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
-                    a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
-                    a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
-                }
-                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
-                BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
-            }
-            tc::fence_async_shared();
-            tc::tc_fence_before();
-            tc::mbar_arrive(&bar_h[j & 1]);
-        }
-    }
-    // all MMAs done (or a wait gave up)
-    bool done = true;
-    if (warp < kMlpWarps) done = tc::mbar_wait(&bar_o, 0, err, &failed);
-    ok = __syncthreads_and(ok && done && !failed) != 0;
-    tc::tc_fence_after();
-    if (ok) {
-        float* tile = reinterpret_cast<float*>(smem);
-        if (warp < kMlpWarps) {
-            const int quarter = warp & 3, half = warp >> 2;
-            stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
-        }
-        __syncthreads();
-        rows_resid_ln_any(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpWarps + 1);
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
-}
-
-// The same MLP as tc_mlp_kernel without warp specialisation: per chunk of NC
-// hidden columns, one after the other, S = A @ W1_chunk (TMEM), h = gelu(S + b1) written to
-// shared memory as bf16 by all 8 warps (two per TMEM lane quarter, one
-// column half each), O += h @ W2_chunk (TMEM). The hidden activations never
-// leave the SM. The residual + LayerNorm epilogue stages O through shared
-// memory and runs one warp per row.
+// x (the next block's norm1, or the final norm) into `ln`. Per chunk of NC
+// hidden columns, one after the other, S = A @ W1_chunk (TMEM), h = gelu(S +
+// b1) written to shared memory as bf16 by all 8 warps (two per TMEM lane
+// quarter, one column half each), O += h @ W2_chunk (TMEM); the hidden
+// activations never leave the SM. Every summation order is fixed by
+// NC-independent K slices of 16, so every chunk width gives the same bits.
+// The residual + LayerNorm epilogue stages O through shared memory and runs
+// one warp per row.
 constexpr int kMlpSerialThreads = 256;
 
 __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const __grid_constant__ CUtensorMap tmA,
@@ -1698,261 +1390,6 @@ __device__ __forceinline__ bool all_of(bool v, int bar, int n) {
         : "r"(v ? 1u : 0u), "r"(bar), "r"(n)
         : "memory");
     return r != 0;
-}
-
-// Persistent form of the fused MLP: one CTA per SM walks row tiles (tile =
-// blockIdx.x + k * gridDim.x) with every stage on its own warps, so the
-// tensor core, the GELU arithmetic and the residual + LayerNorm epilogue of
-// consecutive tiles overlap:
-//   warp 0      (one lane) TMA-loads the A tile (single buffer, refilled once
-//               the tile's last S MMA has read it);
-//   warps 1, 2  (one lane each) stream the W1 and the W2 chunks through two
-//               separate NS-stage rings, continuing across tiles (W1_j is
-//               released when S_j is done, W2_j when O += h_j W2_j is, so
-//               neither waits on the other);
-//   warp 3      (one lane) issues every MMA: S_g = A @ W1_j into one of two
-//               TMEM S buffers, O += h_g @ W2_j into one of two TMEM O
-//               buffers (one per tile in flight);
-//   warps 4-19  turn S_g into h_g = gelu(S_g + b1) (bf16, two h buffers;
-//               four warps per TMEM lane quarter, 16 columns each);
-//   warps 20-23 thread r owns tile row r: the residual update of the tile's
-//               f32 x rows (prefetched by TMA), the LayerNorm in the shared
-//               arithmetic, ln rows to global, x rows back by TMA.
-// g counts chunks over all of this CTA's tiles. The arithmetic and its order
-// are those of the other MLP kernels (the same K slices of 16 in the same
-// order, the same LayerNorm arithmetic), so the result is bit-identical.
-constexpr int kMlpPGelu = 16;                  // GELU warps (NC = 64: 16 columns each)
-constexpr int kMlpPWarps = 4 + kMlpPGelu + 4;  // + A, W1, W2 producers, MMA issuer; + 4 epilogue
-constexpr int kMlpPThreads = kMlpPWarps * 32;
-
-struct MlpPSmem {
-    size_t a, w1, w2, h, b1, epi, total;
-    __host__ __device__ MlpPSmem(int D, int F, int NC, int NS) {
-        a = 0;                                  // [D/8][128][8]
-        w1 = a + (size_t)D * 256;               // NS x W1_j [D/8][NC][8]
-        w2 = w1 + (size_t)NS * 2 * D * NC;      // NS x W2_j [NC/8][D][8]
-        h = w2 + (size_t)NS * 2 * D * NC;       // 2 x [NC/8][128][8]
-        b1 = h + (size_t)2 * NC * 256;          // [F] f32
-        epi = (b1 + (size_t)F * 4 + 1023) / 1024 * 1024;  // x rows: D/32 swizzled boxes of 32 f32 x 128 rows
-        total = epi + (size_t)128 * D * 4;
-    }
-};
-
-__global__ void __launch_bounds__(kMlpPThreads, 1) tc_mlp_persistent_kernel(
-    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, const bf16* __restrict__ W1,
-    const bf16* __restrict__ W2,
-    const float* __restrict__ b1, const float* __restrict__ b2, int D, int F, int NC, int NS, int R,
-    float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b, bf16* __restrict__ ln, int* err) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    const MlpPSmem L(D, F, NC, NS);
-    uint8_t* sA = smem + L.a;
-    uint8_t* sW1 = smem + L.w1;
-    uint8_t* sW2 = smem + L.w2;
-    uint8_t* sH = smem + L.h;
-    float* sb1 = reinterpret_cast<float*>(smem + L.b1);
-    uint8_t* sX = smem + L.epi;
-    constexpr int kMaxStages = 4;
-    __shared__ uint64_t a_full, a_empty, w1_full[kMaxStages], w1_empty[kMaxStages], w2_full[kMaxStages],
-        w2_empty[kMaxStages], s_full[2], h_full[2], h_empty[2], o_full[2], o_empty[2], x_full;
-    __shared__ __align__(16) float sb2[kLnMaxD], sgam[kLnMaxD], sbet[kLnMaxD];
-    __shared__ uint32_t tmem_base;
-    __shared__ volatile int failed;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_tiles = (R + 127) / 128;
-    const int my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int nch = F / NC;
-    const int total = my_tiles * nch;  // chunks this CTA walks
-    const uint32_t s_col = 2u * D;     // O buffers in [0, 2D), S buffers after
-    uint32_t ncols = 32;
-    while (ncols < s_col + 2u * NC) ncols <<= 1;
-    if (threadIdx.x == 0) {
-        tc::mbar_init(&a_full, 1);
-        tc::mbar_init(&a_empty, 1);
-        for (int i = 0; i < NS && i < kMaxStages; i++) {
-            tc::mbar_init(&w1_full[i], 1);
-            tc::mbar_init(&w1_empty[i], 1);
-            tc::mbar_init(&w2_full[i], 1);
-            tc::mbar_init(&w2_empty[i], 1);
-        }
-        for (int i = 0; i < 2; i++) {
-            tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&h_full[i], kMlpPGelu * 32);
-            tc::mbar_init(&h_empty[i], 1);
-            tc::mbar_init(&o_full[i], 1);
-            tc::mbar_init(&o_empty[i], 4 * 32);
-        }
-        tc::mbar_init(&x_full, 1);
-        tc::fence_barrier_init();
-        failed = 0;
-        if ((tc::smem_u32(smem) & 1023u) || NS < 2 || NS > kMaxStages || ncols > 512 || NC != 4 * 16 ||
-            D > kLnMaxD || D % 32) {
-            failed = 1;
-            atomicExch(err, 2);
-        }
-    }
-    for (int i = threadIdx.x; i < F; i += blockDim.x) sb1[i] = b1[i];
-    for (int i = threadIdx.x; i < D && i < kLnMaxD; i += blockDim.x) {
-        sb2[i] = b2[i];
-        sgam[i] = g[i];
-        sbet[i] = b[i];
-    }
-    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
-    tc::tc_fence_before();
-    __syncthreads();
-    JC_PDL_ENTRY;
-    tc::tc_fence_after();
-    const uint32_t tmem = tmem_base;
-    const uint32_t wbytes = (uint32_t)D * NC * 2;  // one of W1_j, W2_j
-    if (warp == 0) {
-        if (lane == 0 && !failed) {
-            // A producer
-            for (int it = 0; it < my_tiles; it++) {
-                if (it > 0 && !tc::mbar_wait(&a_empty, (uint32_t)(it - 1) & 1u, err, &failed)) break;
-                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
-                tc::mbar_expect_tx(&a_full, (uint32_t)D * 256);
-                for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &a_full);
-            }
-        }
-        __syncwarp();
-    } else if (warp == 1 || warp == 2) {
-        if (lane == 0 && !failed) {
-            // W1 (warp 1) or W2 (warp 2) producer
-            const bool first = warp == 1;
-            uint64_t* full = first ? w1_full : w2_full;
-            uint64_t* empty = first ? w1_empty : w2_empty;
-            uint8_t* ring = first ? sW1 : sW2;
-            const bf16* src = first ? W1 : W2;
-            for (int gi = 0; gi < total; gi++) {
-                const int st = gi % NS, j = gi % nch;
-                if (gi >= NS && !tc::mbar_wait(&empty[st], (uint32_t)(gi / NS - 1) & 1u, err, &failed)) break;
-                tc::mbar_expect_tx(&full[st], wbytes);
-                tc::bulk_load(ring + (size_t)st * wbytes, src + (size_t)j * D * NC, wbytes, &full[st]);
-            }
-        }
-        __syncwarp();
-    } else if (warp == 3) {
-        if (lane == 0 && !failed) {
-            // MMA issuer
-            const uint32_t a0 = tc::smem_u32(sA), h0 = tc::smem_u32(sH);
-            const uint32_t w1s = tc::smem_u32(sW1), w2s = tc::smem_u32(sW2);
-            const uint32_t idesc_s = tc::idesc_bf16(128, NC), idesc_o = tc::idesc_bf16(128, D);
-            auto issue_s = [&](int gi) -> bool {
-                const int st = gi % NS, j = gi % nch, it = gi / nch;
-                if (j == 0 && !tc::mbar_wait(&a_full, (uint32_t)it & 1u, err, &failed)) return false;
-                if (!tc::mbar_wait(&w1_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) return false;
-                tc::tc_fence_after();
-                const uint32_t ws = w1s + (uint32_t)st * wbytes;
-                const uint32_t tS = tmem + s_col + (uint32_t)(gi & 1) * NC;
-                for (int k = 0; k < D / 16; k++)
-                    tc::mma_bf16(tS, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(ws + k * 2 * NC * 16, NC * 16, 128),
-                                 idesc_s, k > 0 ? 1u : 0u);
-                tc::mma_commit(&w1_empty[st]);
-                tc::mma_commit(&s_full[gi & 1]);
-                if (j == nch - 1) tc::mma_commit(&a_empty);  // the tile's last read of A
-                return true;
-            };
-            bool good = true;
-            for (int gi = 0; gi < 2 && gi < total && good; gi++) good = issue_s(gi);
-            for (int gi = 0; gi < total && good; gi++) {
-                const int st = gi % NS, j = gi % nch, it = gi / nch;
-                if (j == 0 && it >= 2 &&
-                    !tc::mbar_wait(&o_empty[it & 1], (uint32_t)((it - 2) >> 1) & 1u, err, &failed)) {
-                    good = false;
-                    break;
-                }
-                if (!tc::mbar_wait(&h_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed)) {
-                    good = false;
-                    break;
-                }
-                // h_g is written, so S buffer g & 1 is free: S_{g+2} goes first,
-                // so the GELU warps never wait on this thread's wait for W2_g
-                if (gi + 2 < total && !issue_s(gi + 2)) {
-                    good = false;
-                    break;
-                }
-                if (!tc::mbar_wait(&w2_full[st], (uint32_t)(gi / NS) & 1u, err, &failed)) {
-                    good = false;
-                    break;
-                }
-                tc::tc_fence_after();
-                const uint32_t ws2 = w2s + (uint32_t)st * wbytes;
-                const uint32_t hs = h0 + (uint32_t)(gi & 1) * NC * 256;
-                const uint32_t tO = tmem + (uint32_t)(it & 1) * D;
-                for (int k = 0; k < NC / 16; k++)
-                    tc::mma_bf16(tO, tc::sdesc(hs + k * 4096, 2048, 128), tc::sdesc(ws2 + k * 2 * D * 16, D * 16, 128),
-                                 idesc_o, (j > 0 || k > 0) ? 1u : 0u);
-                tc::mma_commit(&w2_empty[st]);
-                tc::mma_commit(&h_empty[gi & 1]);
-                if (j == nch - 1) tc::mma_commit(&o_full[it & 1]);
-            }
-        }
-        __syncwarp();
-    } else if (warp < 4 + kMlpPGelu) {
-        // GELU warps
-        const int part = (warp - 4) >> 2;  // columns 16 part .. 16 part + 15 of the chunk
-        const int r = (warp & 3) * 32 + lane;
-        for (int gi = 0; gi < total; gi++) {
-            const int j = gi % nch;
-            const bool s_ready = tc::mbar_wait(&s_full[gi & 1], (uint32_t)(gi >> 1) & 1u, err, &failed);
-            const bool h_free = gi < 2 || tc::mbar_wait(&h_empty[gi & 1], (uint32_t)((gi - 2) >> 1) & 1u, err, &failed);
-            if (!__all_sync(0xffffffffu, s_ready && h_free)) break;  // the TMEM load is warp-collective
-            tc::tc_fence_after();
-            const uint32_t ta = lane_addr(tmem + s_col + (uint32_t)(gi & 1) * NC);
-            uint8_t* hb = sH + (size_t)(gi & 1) * NC * 256;
-            const int c = part * 16;
-            float a[16];
-            tc::tmem_ld16(ta + c, a);
-            const float4* bb = reinterpret_cast<const float4*>(sb1 + j * NC + c);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const float4 bv = bb[i];
-                a[4 * i] = gelu_fast(a[4 * i] + bv.x);
-                a[4 * i + 1] = gelu_fast(a[4 * i + 1] + bv.y);
-                a[4 * i + 2] = gelu_fast(a[4 * i + 2] + bv.z);
-                a[4 * i + 3] = gelu_fast(a[4 * i + 3] + bv.w);
-            }
-            BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8) * 2048 + r * 16), a);
-            BfVec<8>::store(reinterpret_cast<bf16*>(hb + (size_t)(c / 8 + 1) * 2048 + r * 16), a + 8);
-            tc::fence_async_shared();
-            tc::tc_fence_before();
-            tc::mbar_arrive(&h_full[gi & 1]);
-        }
-    } else {
-        // epilogue warps: thread r owns tile row r (TMEM lane r). The x rows
-        // of the next tile are prefetched by TMA into sX as soon as the
-        // previous tile's x store has read it.
-        const int r = (warp & 3) * 32 + lane;
-        const bool leader = warp == 4 + kMlpPGelu && lane == 0;
-        auto load_x = [&](int it) {
-            const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
-            tc::mbar_expect_tx(&x_full, (uint32_t)D * 512);
-            for (int bx = 0; bx < D / 32; bx++) tc::tma_load_2d(sX + bx * 16384, &tmX, bx * 32, m0, &x_full);
-        };
-        if (leader && my_tiles > 0 && !failed) load_x(0);
-        for (int it = 0; it < my_tiles; it++) {
-            const bool ready = tc::mbar_wait(&o_full[it & 1], (uint32_t)(it >> 1) & 1u, err, &failed) &&
-                               tc::mbar_wait(&x_full, (uint32_t)it & 1u, err, &failed);
-            if (!all_of(ready, 1, 128)) break;  // the four epilogue warps meet at barrier 1 below
-            tc::tc_fence_after();
-            const int row = ((int)blockIdx.x + it * (int)gridDim.x) * 128 + r;
-            row_resid_ln_t<0>(lane_addr(tmem + (uint32_t)(it & 1) * D), r, D, sX, sb2, sgam, sbet, nullptr,
-                         row < R ? ln + (size_t)row * D : nullptr);
-            tc::tc_fence_before();
-            tc::mbar_arrive(&o_empty[it & 1]);
-            tc::fence_async_shared();
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            if (leader) {
-                const int m0 = ((int)blockIdx.x + it * (int)gridDim.x) * 128;
-                for (int bx = 0; bx < D / 32; bx++) tc::tma_store_2d(&tmX, sX + bx * 16384, bx * 32, m0);
-                tc::bulk_commit();
-                tc::bulk_wait_read();
-                if (it + 1 < my_tiles && !failed) load_x(it + 1);
-            }
-        }
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
 
@@ -2669,9 +2106,9 @@ BF16Path::BF16Path(const Dims& d, const TensorMap* tp, DeviceArena* ap) {
         cuda_check(cudaDeviceGetAttribute(&n_sms_, cudaDevAttrMultiProcessorCount, dev), "SM count");
     }
     // default: the serial kernel, 64 columns (fits every supported width)
-    def_tuning_ = Tuning{64, 1, 256, 0};
-    if (!mlp_fits(64, 1, 0)) def_tuning_.nc = 32;
-    if (!mlp_fits(def_tuning_.nc, 1, 0)) throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
+    def_tuning_ = Tuning{64, 256};
+    if (!mlp_fits(64)) def_tuning_.nc = 32;
+    if (!mlp_fits(def_tuning_.nc)) throw Error(JC_LIMIT, "the BF16 MLP does not fit in shared memory at this width");
     if (attn_tile_ok(d)) def_tuning_.attn_threads = 0;  // shared-memory attention tiles
     for (int l = 0; l < kMaxLayers; l++) {
         wqkv[l] = wp[l] = nullptr;
@@ -2762,16 +2199,12 @@ void BF16Path::set_kernel_attributes() {
     set_smem(tc_gemm_kernel<EPI_BF16>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_F32>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
-    set_smem(tc_mlp_kernel, kMlpSmemMax);
     set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
     set_smem(tc_projln_persistent_kernel, 225 * 1024);  // 227 KB per CTA less the static shared memory
     set_smem(tc_qkv_persistent_kernel, 225 * 1024);
     set_smem(tc_conv1_persistent_kernel, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
-    set_smem(bf_attn_ring_kernel<32>, kAttRingSmem);
-    set_smem(bf_attn_ring_kernel<64>, kAttRingSmem);
-    set_smem(tc_mlp_persistent_kernel, kMlpSmemMax);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
     set_smem(bf_embed_kernel<1>, 100 * 1024);
@@ -2789,37 +2222,6 @@ void BF16Path::set_kernel_attributes() {
 
 static void launch_attention(const Dims& d, const bf16* qkv, const InstDev* inst, int n, int R, bf16* attn,
                              int threads, cudaStream_t s, const Pack* p = nullptr) {
-    if (threads == -1) {
-        // persistent CTAs over (token tile, half, box) items, two load stages
-        const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
-        const int items = p->n_ttiles * 2 * (d.D / 64);
-        static int per_sm[2] = {0, 0}, sms = 0;  // CTAs per SM for head width 32 / 64
-        if (sms == 0) {
-            int dev = 0;
-            cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-            cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-        }
-        const bool h32 = d.D / d.heads == 32;
-        int& occ = per_sm[h32 ? 0 : 1];
-        if (occ == 0) {
-            if (h32)
-                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bf_attn_ring_kernel<32>, 128, kAttRingSmem),
-                           "occupancy");
-            else
-                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bf_attn_ring_kernel<64>, 64, kAttRingSmem),
-                           "occupancy");
-        }
-        const unsigned grid = (unsigned)std::max(1, std::min(items, std::max(1, occ) * sms));
-        if (h32)
-            cuda_check(launch_pdl(bf_attn_ring_kernel<32>, grid, 128, kAttRingSmem, s, 1u, d, maps, 4, 5, inst, n,
-                                  p->n_ttiles, attn, p->err),
-                       "launch");
-        else
-            cuda_check(launch_pdl(bf_attn_ring_kernel<64>, grid, 64, kAttRingSmem, s, 1u, d, maps, 4, 5, inst, n,
-                                  p->n_ttiles, attn, p->err),
-                       "launch");
-        return;
-    }
     if (threads == 0) {
         // shared-memory tiles: grid (8 x 16 token tiles, their two 8 x 8 halves)
         const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(p->tmaps);
@@ -2873,18 +2275,13 @@ Tuning BF16Path::tuning_for(int rows) const {
     return def_tuning_;
 }
 
-// Shared memory of the serial MLP kernel (one stage, one h buffer).
+// Shared memory of the MLP kernel (one stage, one h buffer).
 static size_t mlp_serial_smem(int D, int NC) {
     return std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
 }
 
-bool BF16Path::mlp_fits(int nc, int ns, int form) const {
-    if (!(nc == 32 || nc == 64) || dims_F_ % nc) return false;
-    if (form == 0) return ns == 1 && mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
-    if (ns < 2 || ns > 4) return false;
-    if (form == 1) return MlpSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
-    return form == 2 && nc == 64 && dims_D_ <= kLnMaxD && 2 * dims_D_ + 2 * nc <= 512 &&
-           MlpPSmem(dims_D_, dims_F_, nc, ns).total <= kMlpSmemMax;
+bool BF16Path::mlp_fits(int nc) const {
+    return (nc == 32 || nc == 64) && dims_F_ % nc == 0 && mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
 }
 
 void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln,
@@ -2893,24 +2290,10 @@ void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tunin
     const int v = tu.nc == 64 ? 1 : 0;
     const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
     const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
-    if (tu.form == 0) {
-        cuda_check(launch_pdl(tc_mlp_serial_kernel, (unsigned)((R + 127) / 128), kMlpSerialThreads, mlp_serial_smem(D, tu.nc), s, 1u, 
-            m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, R, p.x, ng, nbeta,
-            reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
-        return;
-    }
-    if (tu.form == 2) {
-        const unsigned grid = (unsigned)std::min((R + 127) / 128, n_sms_);
-        const CUtensorMap m_x = store_map(p.x, D, R, D, true);
-        cuda_check(launch_pdl(tc_mlp_persistent_kernel, grid, kMlpPThreads, MlpPSmem(D, d.F, tu.nc, tu.ns).total, s, 1u, 
-            m_ln, m_x, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
-            reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
-        return;
-    }
-    const size_t smem = MlpSmem(D, d.F, tu.nc, tu.ns).total;
-    cuda_check(launch_pdl(tc_mlp_kernel, (unsigned)((R + 127) / 128), kMlpThreads, smem, s, 1u, 
-        m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D, d.F, tu.nc, tu.ns, R, p.x, ng, nbeta,
-        reinterpret_cast<bf16*>(p.bt[0]), p.err), "launch");
+    cuda_check(launch_pdl(tc_mlp_serial_kernel, (unsigned)((R + 127) / 128), kMlpSerialThreads,
+                          mlp_serial_smem(D, tu.nc), s, 1u, m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D,
+                          d.F, tu.nc, R, p.x, ng, nbeta, reinterpret_cast<bf16*>(p.bt[0]), p.err),
+               "launch");
 }
 
 // Times `launch` with CUDA events: one warm-up, then `reps` launches.
@@ -2950,27 +2333,20 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     // anything in it (every forward rewrites it from the state)
     std::string log;
     float best_ms = 1e30f;
-    // {chunk width, weight stages, form}
-    const int cand[][3] = {{32, 1, 0}, {64, 1, 0}, {32, 2, 1}, {32, 3, 1}, {64, 2, 1}, {64, 3, 1}, {64, 2, 2}};
-    for (const auto& c : cand) {
-        if (!mlp_fits(c[0], c[1], c[2])) continue;
+    for (int nc : {32, 64}) {
+        if (!mlp_fits(nc)) continue;
         Tuning t = best;
-        t.nc = c[0];
-        t.ns = c[1];
-        t.form = c[2];
+        t.nc = nc;
         const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, 3, s);
-        log += (log.empty() ? "" : ", ") + std::string("\"mlp_f") + std::to_string(c[2]) + "_" + std::to_string(c[0]) +
-               "x" + std::to_string(c[1]) + "_ms\": " + std::to_string(ms);
+        log += (log.empty() ? "" : ", ") + std::string("\"mlp_nc") + std::to_string(nc) + "_ms\": " + std::to_string(ms);
         if (ms < best_ms) {
             best_ms = ms;
-            best.nc = t.nc;
-            best.ns = t.ns;
-            best.form = t.form;
+            best.nc = nc;
         }
     }
     best_ms = 1e30f;
-    for (int threads : {-1, 0, 64, 128, 256}) {
-        if (threads <= 0 && !attn_tile_ok(d)) continue;
+    for (int threads : {0, 64, 128, 256}) {
+        if (threads == 0 && !attn_tile_ok(d)) continue;
         const float ms =
             time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s, &p); }, 3, s);
         log += ", \"attn_" + std::to_string(threads) + "_ms\": " + std::to_string(ms);
@@ -2989,7 +2365,7 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
 
 // Tuned schedules persist in the JSON-lines file named by JC_AUTOTUNE_CACHE,
 // one object per tuned row bucket:
-//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "mlp_form": 2, "nc": 32, "stages": 3, "attn_threads": 256}
+//   {"model": "d128_l4_f512_r1_k1_g1", "rows": 65536, "nc": 64, "attn_threads": 0}
 // keyed by the model shape (dim, layers, MLP width, mask radius, kind and
 // dilation), followed by the candidates' measured times. Lines that do not
 // parse or name another shape are skipped; later lines override earlier ones.
@@ -3000,15 +2376,12 @@ void BF16Path::load_cache() {
     if (!f) return;
     char line[512], key[128];
     while (std::fgets(line, sizeof line, f)) {
-        int bucket, form, nc, ns, th;
-        if (std::sscanf(line,
-                        " {\"model\": \"%127[^\"]\", \"rows\": %d, \"mlp_form\": %d, \"nc\": %d, \"stages\": %d, "
-                        "\"attn_threads\": %d",
-                        key, &bucket, &form, &nc, &ns, &th) != 6)
+        int bucket, nc, th;
+        if (std::sscanf(line, " {\"model\": \"%127[^\"]\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d", key,
+                        &bucket, &nc, &th) != 4)
             continue;
-        if (cache_key_ == key && mlp_fits(nc, ns, form) &&
-            (th == 64 || th == 128 || th == 256 || (th <= 0 && th >= -1 && attn_tile_ok(dims_))))
-            tuned_[bucket] = Tuning{nc, ns, th, form};
+        if (cache_key_ == key && mlp_fits(nc) && (th == 64 || th == 128 || th == 256 || (th == 0 && attn_tile_ok(dims_))))
+            tuned_[bucket] = Tuning{nc, th};
     }
     std::fclose(f);
 }
@@ -3019,11 +2392,8 @@ void BF16Path::save_cache(int bucket, const Tuning& t, const std::string& timing
     std::lock_guard<std::mutex> lk(tune_mu_);
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f,
-                 "{\"model\": \"%s\", \"rows\": %d, \"mlp_form\": %d, \"nc\": %d, \"stages\": %d, \"attn_threads\": "
-                 "%d%s%s}\n",
-                 cache_key_.c_str(), bucket, t.form, t.nc, t.ns, t.attn_threads, timings.empty() ? "" : ", ",
-                 timings.c_str());
+    std::fprintf(f, "{\"model\": \"%s\", \"rows\": %d, \"nc\": %d, \"attn_threads\": %d%s%s}\n", cache_key_.c_str(),
+                 bucket, t.nc, t.attn_threads, timings.empty() ? "" : ", ", timings.c_str());
     std::fclose(f);
 }
 

@@ -15,20 +15,18 @@
 namespace jc {
 
 // A schedule the autotuner picks per (row-count bucket): the MLP's hidden
-// chunk width and the attention kernel's CTA size. Every schedule gives the
-// same bits: the candidates change tiling, never the order of a sum, so an
+// chunk width and the attention kernel's form. Every schedule gives the same
+// bits: the candidates change tiling, never the order of a sum, so an
 // instance's result does not depend on the batch it runs in.
 struct Tuning {
     int nc;            // 32 or 64 hidden columns per MLP step
-    int ns;            // MLP weight-ring stages (2-4; 1 for the serial form)
-    int attn_threads;  // 64, 128 or 256 threads per attention CTA; 0 = shared-memory tiles, -1 = persistent tiles
-    int form;          // MLP kernel: 0 serial, 1 pipelined per tile, 2 persistent
+    int attn_threads;  // 64, 128 or 256 threads per attention CTA; 0 = shared-memory tiles
 };
 
 // 1 (default; environment JC_AUTOTUNE=0 turns it off): BF16 launches time the
 // candidate schedules once per row-count bucket and keep the fastest; 0: the
-// fixed default schedule {serial MLP, nc 64; shared-memory attention tiles
-// where they apply, else 256 attention threads}.
+// fixed default schedule {MLP with 64 hidden columns per step; shared-memory
+// attention tiles where they apply, else 256 attention threads}.
 extern std::atomic<int> g_autotune;
 
 class BF16Path {
@@ -64,9 +62,9 @@ class BF16Path {
     static constexpr size_t kMlpSmemMax = 200 * 1024;
     int dims_D_ = 0, dims_F_ = 0;
     Dims dims_{};
-    Tuning def_tuning_{64, 1, 256, 0};
+    Tuning def_tuning_{64, 256};
     int n_sms_ = 1;
-    bool mlp_fits(int nc, int ns, int form) const;
+    bool mlp_fits(int nc) const;
     void launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln, const Pack& p,
                     cudaStream_t s) const;
     mutable std::mutex tune_mu_;

@@ -57,18 +57,16 @@ def test_every_schedule_gives_identical_results(tmp_path, monkeypatch, dim):
         cache = tmp_path / "tune.txt"
         monkeypatch.setenv("JC_AUTOTUNE_CACHE", str(cache))
         engine.autotune(True)
-        mlp = [(0, 32, 1), (0, 64, 1), (1, 32, 2), (1, 32, 3), (1, 64, 2), (1, 64, 3), (2, 64, 2)]
-        scheds = [m + (256,) for m in mlp] + [(0, 64, 1, 64), (0, 64, 1, 128), (0, 64, 1, 0), (0, 64, 1, -1)]
-        for form, nc, ns, threads in scheds:
+        scheds = [(32, 256), (64, 256), (64, 64), (64, 128), (64, 0)]
+        for nc, threads in scheds:
             # a cache file written beforehand fixes the schedule of every row bucket
             key = _key(fam[0][2])
-            cache.write_text("".join(json.dumps({"model": key, "rows": 1 << b, "mlp_form": form, "nc": nc,
-                                                 "stages": ns, "attn_threads": threads}) + "\n"
-                                     for b in range(7, 25)))
+            cache.write_text("".join(json.dumps({"model": key, "rows": 1 << b, "nc": nc, "attn_threads": threads})
+                                     + "\n" for b in range(7, 25)))
             got, got1 = _run(fam, spec)
             for a, g in zip(base, got):
-                assert np.array_equal(a, g), (form, nc, ns, threads)
-            assert np.array_equal(base1, got1), (form, nc, ns, threads)
+                assert np.array_equal(a, g), (nc, threads)
+            assert np.array_equal(base1, got1), (nc, threads)
     finally:
         engine.autotune(prev)
 
@@ -83,8 +81,7 @@ def test_tuning_is_recorded_and_reused(tmp_path, monkeypatch):
         rows = [json.loads(ln) for ln in cache.read_text().splitlines()]
         assert len(rows) >= 2  # the batch's row bucket and the single forward's
         assert all(r["model"] == _key(fam[0][2]) for r in rows)
-        assert all(r["mlp_form"] in (0, 1, 2) and r["nc"] in (32, 64) and r["stages"] in (1, 2, 3, 4)
-                   and r["attn_threads"] in (-1, 0, 64, 128, 256) for r in rows)
+        assert all(r["nc"] in (32, 64) and r["attn_threads"] in (0, 64, 128, 256) for r in rows)
         size = cache.stat().st_size
         again, _ = _run(fam, [(1, 2), (1, 2), (0, 2)])
         assert cache.stat().st_size == size  # read back, not tuned again
