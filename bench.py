@@ -84,6 +84,8 @@ def parse_args():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-task batch measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 256x256 error report against the f64 oracle")
     ap.add_argument("--no-eval", action="store_true", help="skip the eval-metrics measurement")
+    ap.add_argument("--only-served", action="store_true",
+                    help="the served steps alone (for profiling): no FP32, batched, CPU or accuracy runs")
     return ap.parse_args()
 
 
@@ -186,6 +188,47 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
     return None, None
 
 
+PER_LAYER = ("tc_qkv", "bf_attention", "tc_proj_ln", "tc_mlp")
+
+
+def work_table(prof, cells, proj_cells, D, F, L, pk, pk_kind, where):
+    """Per-kernel rates from a profile {name: (launches, total ms)} of work that
+    stepped `cells` forward cell-ticks in all (`proj_cells` of them projected):
+    algorithmic FLOPs (contractions) or compulsory bytes (memory-bound
+    kernels) summed over the launches, over the kernel's total device time;
+    and the roofline of the kernel with the largest share."""
+    total_ms = sum(v[1] for v in prof.values())
+    table, best = {}, None
+    for name, (n, ms) in prof.items():
+        kind, amount = kernel_work(name, 1, proj_cells if name == "projection" else cells, D, F)
+        if kind is None:
+            table[name] = {"launches": n, "total_ms": ms, "share": ms / total_ms}
+            continue
+        amount *= L if name in PER_LAYER else 1
+        rate = amount / (ms / 1e3)
+        row = {"launches": n, "total_ms": ms, "avg_ms": ms / n, "share": ms / total_ms}
+        row.update({"tflops": rate / 1e12} if kind == "flop" else {"gbs": rate / 1e9})
+        table[name] = row
+        if best is None or ms > best[2]:
+            best = (name, kind, ms, amount, n)
+    name, kind, ms, amount, n = best
+    traffic = ncu_traffic().get(name)
+    if traffic is not None:  # ncu bytes of one launch over 64 x 128x128 cells, scaled to this run's average launch
+        traffic *= (amount / n) / (kernel_work(name, 64, 128 * 128, D, F)[1])
+    if kind == "flop":
+        ach = amount / (ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "kernel": name, "achieved": ach, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": ach / pk["bf16_tflops"], "traffic": traffic, "peak_kind": f"{pk_kind} bf16 dense burst",
+                "flop_per_launch": amount / n}
+    else:
+        ach = amount / (ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / pk["hbm_gbs"], "traffic": traffic, "peak_kind": f"{pk_kind} copy bandwidth",
+                "bytes_per_launch": amount / n}
+    roof.update({"avg_launch_ms": ms / n, "share": ms / total_ms, "measured_on": where})
+    return table, roof
+
+
 # ---- the served workload (the metric's configuration) ------------------------------------
 
 C5_SIDES = list(range(32, 257, 4))  # grid sides: log-uniform in [32, 256], rounded to a multiple of 4
@@ -245,6 +288,12 @@ class C5:
 
     def useful(self, reqs):
         return sum(self.side(r) ** 2 * r["ticks"] for r in reqs)
+
+    def projected(self, reqs):
+        """Cell-ticks of the forward and rewind requests (the projected ones)."""
+        from jacobi2000_gb300 import engine
+
+        return sum(self.side(r) ** 2 * r["ticks"] for r in reqs if r["task"] != engine.TASK_RECONSTRUCT)
 
     def work(self, reqs):
         """Forward cell-ticks the requests cost (a reconstruct sweep steps 2H slices)."""
@@ -821,6 +870,15 @@ def main():
     # end to end with host buffers through the C ABI
     e2e_runs = [run_served(srv, wl, step_reqs, metas, device=False) for _ in range(2)]
     e2e_ms = max_over_ranks(1e3 * statistics.mean(r["wall_s"] for r in e2e_runs), world, "cuda")
+    # one more step with CUDA events around every launch of the loop: the
+    # per-kernel table and the roofline of the served workload's top kernel
+    srv.profile_start()
+    run_served(srv, wl, step_reqs, metas, device=True)
+    sprof = srv.profile_stop()
+    table, roof = work_table(sprof, wl.work(step_reqs), wl.projected(step_reqs), args.dim, 4 * args.dim,
+                             args.layers, pk, pk_kind,
+                             f"one served step ({args.requests} requests), CUDA events around each launch on the "
+                             f"server's stream, outside the timed steps")
 
     served = None
     if rank == 0:
@@ -847,7 +905,7 @@ def main():
         m.close()
 
     plain = None
-    if rank == 0:
+    if rank == 0 and not args.only_served:
         fm32, rm32 = c5_models(args, engine.FP32)
         with engine.Server(fm32, rm32, max_active_cells=C5_MAX_CELLS, hbm_fraction=C5_HBM) as s32:
             preqs = C5.draw(99, args.plain_requests, rate)
@@ -867,14 +925,17 @@ def main():
                               "frac": work_rate * flop / 1e12 / fp32_peak if flop else None,
                               "peak_kind": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x max SM clock)",
                               "flop_per_cell_tick": flop}}
-    batched, roof, table = batched_bench(args, world, barrier)
-
-    mixed = mixed_batch_bench(args) if rank == 0 and not args.no_mixed else None
-    accuracy = accuracy_c3() if rank == 0 and not args.no_accuracy else None
-    evalm = eval_bench(args) if rank == 0 and not args.no_eval else None
+    batched = broof = btable = None
+    if not args.only_served:
+        batched, broof, btable = batched_bench(args, world, barrier)
+        batched.update({"roofline": broof, "kernels": btable})
+    extras = rank == 0 and not args.only_served
+    mixed = mixed_batch_bench(args) if extras and not args.no_mixed else None
+    accuracy = accuracy_c3() if extras and not args.no_accuracy else None
+    evalm = eval_bench(args) if extras and not args.no_eval else None
 
     cpu = None
-    if rank == 0:
+    if extras:
         v, cores, dt, n = cpu_served_sample(args, args.cpu_requests, seed=31)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} requests of the served workload, one at a time, each at most 5 ticks (a "

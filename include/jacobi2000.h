@@ -262,6 +262,13 @@ jc_status jc_server_wait(jc_server* s, uint64_t id, float* out, size_t out_len, 
 jc_status jc_server_get_stats(jc_server* s, jc_server_stats* out);
 /* Zeroes the statistics; the next iteration starts a new device span. */
 jc_status jc_server_reset_stats(jc_server* s);
+/* Instrumentation, with no counterpart in the reference: enable = 1 clears
+ * and starts per-kernel timing (CUDA events around every kernel launch of the
+ * loop, which adds a little host work per launch); enable = 0 stops it and,
+ * when report is non-null, writes one "name,launches,total_ms" line per
+ * kernel over the iterations in between (NUL-terminated, truncated to cap
+ * bytes). */
+jc_status jc_server_profile(jc_server* s, int32_t enable, char* report, size_t cap);
 
 /* Instrumentation, with no counterpart in the reference: runs the instances
  * once, outside any graph, with CUDA events around every kernel launch, and
@@ -306,7 +313,8 @@ void   jc_project_energy(float* x, double prev_energy, const jc_config* cfg, int
  * default; environment JC_AUTOTUNE=0 starts with it off) the first BF16
  * launch outside a stream capture for each row-count bucket (powers of two of
  * token rows) times the candidate schedules with CUDA events, once, and later
- * launches and graph captures use the fastest: the fused MLP's hidden chunk
+ * launches and graph captures use the fastest, where a candidate replaces
+ * the fixed schedule only when it is at least 5% faster: the fused MLP's hidden chunk
  * width (32 or 64 columns per step) and the attention's form (shared-memory
  * tiles, or one thread per (row, head) in 64-, 128- or 256-thread CTAs).
  * enable = 0 selects the fixed schedule (64 columns; attention tiles where

@@ -2332,25 +2332,36 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     // the workspace holds transient values; the timed launches may leave
     // anything in it (every forward rewrites it from the state)
     std::string log;
-    float best_ms = 1e30f;
-    for (int nc : {32, 64}) {
+    // A candidate replaces the default only when it is clearly faster (by
+    // kTuneMargin): a bucket's choice also serves other mixes of instance
+    // sizes with that row count, and single timings vary by a few percent.
+    constexpr float kTuneMargin = 0.95f;
+    constexpr int kTuneReps = 8;
+    float def_ms = 0.f, best_ms = 1e30f;
+    for (int nc : {def_tuning_.nc, 96 - def_tuning_.nc}) {  // the default width first, then the other
         if (!mlp_fits(nc)) continue;
         Tuning t = best;
         t.nc = nc;
-        const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, 3, s);
+        const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, kTuneReps, s);
         log += (log.empty() ? "" : ", ") + std::string("\"mlp_nc") + std::to_string(nc) + "_ms\": " + std::to_string(ms);
-        if (ms < best_ms) {
+        if (nc == def_tuning_.nc) {
+            def_ms = best_ms = ms;
+        } else if (ms < kTuneMargin * def_ms && ms < best_ms) {
             best_ms = ms;
             best.nc = nc;
         }
     }
-    best_ms = 1e30f;
-    for (int threads : {0, 64, 128, 256}) {
-        if (threads == 0 && !attn_tile_ok(d)) continue;
-        const float ms =
-            time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s, &p); }, 3, s);
+    const int def_attn = def_tuning_.attn_threads;
+    std::vector<int> forms = {def_attn};
+    for (int threads : {0, 64, 128, 256})
+        if (threads != def_attn && (threads != 0 || attn_tile_ok(d))) forms.push_back(threads);
+    for (int threads : forms) {
+        const float ms = time_launches([&] { launch_attention(d, qkv, p.inst, p.n_inst, R, attn, threads, s, &p); },
+                                       kTuneReps, s);
         log += ", \"attn_" + std::to_string(threads) + "_ms\": " + std::to_string(ms);
-        if (ms < best_ms) {
+        if (threads == def_attn) {
+            def_ms = best_ms = ms;
+        } else if (ms < kTuneMargin * def_ms && ms < best_ms) {
             best_ms = ms;
             best.attn_threads = threads;
         }

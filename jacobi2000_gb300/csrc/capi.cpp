@@ -224,6 +224,11 @@ jc_status jc_server_reset_stats(jc_server* s) {
     return guard([&] { jc::server_reset_stats(s); });
 }
 
+jc_status jc_server_profile(jc_server* s, int32_t enable, char* report, size_t cap) {
+    if (!s) return fail(JC_BAD_ARGUMENT, "server is null");
+    return guard([&] { jc::server_profile(s, enable, report, cap); });
+}
+
 jc_status jc_batch_profile(jc_batch* b, const jc_instance* instances, int32_t n, int32_t device_pointers,
                            char* report, size_t cap) {
     if (!b || !report || cap == 0) return fail(JC_BAD_ARGUMENT, "null argument");

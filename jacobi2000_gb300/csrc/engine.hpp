@@ -106,11 +106,12 @@ struct ReconDev {
     float last_resid;
 };
 
-// X <- known ? value : 0 and bookkeeping reset, for n reconstruct instances.
-void recon_init(ReconDev* d, int n, cudaStream_t s);
+// X <- known ? value : 0 and bookkeeping reset, for n reconstruct instances
+// (max_cells / max_h: the largest cell count and horizon among them).
+void recon_init(ReconDev* d, int n, long long max_cells, int max_h, cudaStream_t s);
 // X_t <- known_t ? value : mean of the available step results, for every
 // instance not yet frozen; records each instance's largest change.
-void recon_update(ReconDev* d, int n, cudaStream_t s);
+void recon_update(ReconDev* d, int n, long long max_cells, int max_h, cudaStream_t s);
 // Counts the sweep, freezes converged or exhausted instances and, when
 // use_handle, sets the graph's while condition to "some instance still runs".
 void recon_finalize(ReconDev* d, int n, unsigned long long handle, int use_handle, cudaStream_t s);

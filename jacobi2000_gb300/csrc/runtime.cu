@@ -1142,7 +1142,13 @@ void Batch::enqueue_sweep(const Plan& p, cudaStream_t s) const {
         v.max_inst_cells = G.max_cells;
         models_[G.model]->forward_pack(v, kWriteNextState, s);
     }
-    recon_update(d_recon_, (int)p.recons.size(), s);
+    long long mc = 0;
+    int mh = 0;
+    for (const auto& r : p.recons) {
+        mc = std::max(mc, r.cells);
+        mh = std::max(mh, r.H);
+    }
+    recon_update(d_recon_, (int)p.recons.size(), mc, mh, s);
 }
 
 void Batch::enqueue(const Plan& p, cudaStream_t s, bool capture) const {
@@ -1168,7 +1174,15 @@ void Batch::enqueue(const Plan& p, cudaStream_t s, bool capture) const {
     }
     if (p.recons.empty()) return;
     const int nrec = (int)p.recons.size();
-    recon_init(d_recon_, nrec, s);
+    {
+        long long mc = 0;
+        int mh = 0;
+        for (const auto& r : p.recons) {
+            mc = std::max(mc, r.cells);
+            mh = std::max(mh, r.H);
+        }
+        recon_init(d_recon_, nrec, mc, mh, s);
+    }
     if (!capture) {
         // outside a graph (profiling): sweeps up to the largest limit; frozen
         // instances are left unchanged by the update

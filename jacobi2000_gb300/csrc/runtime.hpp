@@ -259,6 +259,7 @@ uint64_t server_submit(jc_server* s, const jc_request* r);
 void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* info, double timeout);
 void server_stats(jc_server* s, jc_server_stats* st);
 void server_reset_stats(jc_server* s);
+void server_profile(jc_server* s, int enable, char* report, size_t cap);
 
 // fnv1a-64 of a safetensors image and its config text: the source identity a
 // pre-packed checkpoint records.

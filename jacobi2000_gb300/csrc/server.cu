@@ -55,15 +55,22 @@ double now_s() {
 constexpr double kChunkTargetS = 4e-3;
 constexpr int kMaxChunk = 64;
 
-// X_t <- known_t ? value : 0 (the normalized mean state) for every t.
+// X_t <- known_t ? value : 0 (the normalized mean state) for every t. Work
+// unit = (time slice, block of blockDim.x cells): a CTA takes units with
+// stride gridDim.x, a thread one cell of the unit and its three channels.
 __global__ void recon_fill_kernel(float* __restrict__ vol, const float* __restrict__ vals,
                                   const uint8_t* __restrict__ known, int H, long long cells) {
-    const long long per = 3 * cells, total = (long long)(H + 1) * per;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int t = (int)(i / per);
-        const long long cell = (i - (long long)t * per) % cells;
-        vol[i] = known[(long long)t * cells + cell] ? vals[i] : 0.0f;
+    const long long per = 3 * cells, ncb = (cells + blockDim.x - 1) / blockDim.x;
+    const long long units = (long long)(H + 1) * ncb;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        const long long t = u / ncb, cell = (u - t * ncb) * blockDim.x + threadIdx.x;
+        if (cell >= cells) continue;
+        const bool k = known[t * cells + cell] != 0;
+#pragma unroll
+        for (int ch = 0; ch < 3; ch++) {
+            const long long i = t * per + ch * cells + cell;
+            vol[i] = k ? vals[i] : 0.0f;
+        }
     }
 }
 
@@ -118,6 +125,11 @@ class Server {
     void wait(uint64_t id, float* out, size_t out_len, jc_result* info, double timeout_s);
     void stats(jc_server_stats* s);
     void reset_stats();
+    // Per-kernel device time (CUDA events around every launch of the loop):
+    // start() clears and enables it, stop() disables it and returns
+    // name -> (launches, total ms) of the iterations in between.
+    void profile_start();
+    std::map<std::string, std::pair<int, double>> profile_stop();
 
    private:
     std::vector<Model*> fwd_, rev_;
@@ -152,6 +164,8 @@ class Server {
     double cell_ticks_ = 0, busy_s_ = 0, first_submit_ = 0, last_done_ = 0, device_span_s_ = 0;
     int iterations_ = 0;
     long long launches_ = 0;
+    bool profiling_ = false;
+    std::map<std::string, std::pair<int, double>> prof_;
 
     void loop();
     int chunk_length(const std::vector<Request*>& act, long long head_cells, int head_inst) const;
@@ -370,6 +384,20 @@ void Server::reset_stats() {
     span_open_ = false;
 }
 
+void Server::profile_start() {
+    std::lock_guard<std::mutex> lk(mu_);
+    prof_.clear();
+    profiling_ = true;
+}
+
+std::map<std::string, std::pair<int, double>> Server::profile_stop() {
+    std::lock_guard<std::mutex> lk(mu_);
+    profiling_ = false;
+    std::map<std::string, std::pair<int, double>> out;
+    out.swap(prof_);
+    return out;
+}
+
 void Server::fail_locked(Request& q, int status, const std::string& msg) {
     q.status = status;
     q.error = msg;
@@ -402,8 +430,9 @@ void Server::allocate(Request& q) {
         cuda_check(cudaMemcpyAsync(q.d_known, q.device_io ? q.dev_known : q.known.data(), (H + 1) * q.cells, in_kind,
                                    stream_),
                    "reconstruct mask", JC_MAP);
-        g_launches++;
-        recon_fill_kernel<<<1024, 256, 0, stream_>>>(q.d_state, q.d_vals, q.d_known, (int)H, (long long)q.cells);
+        KScope k("recon_fill", stream_);
+        recon_fill_kernel<<<(unsigned)std::min<size_t>((H + 1) * ((q.cells + 255) / 256), 4096), 256, 0, stream_>>>(
+            q.d_state, q.d_vals, q.d_known, (int)H, (long long)q.cells);
         cuda_check(cudaGetLastError(), "reconstruct fill");
     } else {
         q.d_state = static_cast<float*>(get(len * 4));
@@ -482,9 +511,11 @@ int Server::chunk_length(const std::vector<Request*>& act, long long head_cells,
 
 void Server::loop() {
     std::vector<Request*> act;
+    KernelTimer kt;
     while (true) {
         long long head_cells = -1;
         int head_inst = 0;
+        bool prof = false;
         {
             std::unique_lock<std::mutex> lk(mu_);
             admit_locked();
@@ -500,13 +531,27 @@ void Server::loop() {
                 head_cells = h.inst_cells();
                 head_inst = h.n_inst();
             }
+            prof = profiling_;
         }
         const int K = chunk_length(act, head_cells, head_inst);
         const double t0 = now_s();
         const long long l0 = g_launches;
+        if (prof) g_ktimer = &kt;
         try {
             iteration(act, K);
+            if (prof) {
+                g_ktimer = nullptr;
+                auto sm = kt.summary();
+                std::lock_guard<std::mutex> lk(mu_);
+                for (const auto& kv : sm) {
+                    auto& v = prof_[kv.first];
+                    v.first += kv.second.first;
+                    v.second += kv.second.second;
+                }
+            }
         } catch (const std::exception& e) {
+            g_ktimer = nullptr;
+            kt.summary();
             const Error* je = dynamic_cast<const Error*>(&e);
             cudaStreamSynchronize(stream_);
             cudaGetLastError();
@@ -738,9 +783,15 @@ void Server::iteration(std::vector<Request*>& act, int K) {
             projection(dims_, pv, 0, s);
         }
         int nrec = 0;
-        while (nrec < (int)recon.size() && recon[nrec]->remaining() >= t) nrec++;
+        long long rc = 0;
+        int rh = 0;
+        while (nrec < (int)recon.size() && recon[nrec]->remaining() >= t) {
+            rc = std::max(rc, (long long)recon[nrec]->cells);
+            rh = std::max(rh, recon[nrec]->r.ticks);
+            nrec++;
+        }
         if (nrec) {
-            recon_update(d_recon_, nrec, s);
+            recon_update(d_recon_, nrec, rc, rh, s);
             recon_finalize(d_recon_, nrec, 0ull, 0, s);
         }
     }
@@ -839,4 +890,18 @@ void server_wait(jc_server* s, uint64_t id, float* out, size_t n, jc_result* inf
 }
 void server_stats(jc_server* s, jc_server_stats* st) { s->s->stats(st); }
 void server_reset_stats(jc_server* s) { s->s->reset_stats(); }
+void server_profile(jc_server* s, int enable, char* report, size_t cap) {
+    if (enable) {
+        s->s->profile_start();
+        return;
+    }
+    const auto m = s->s->profile_stop();
+    if (!report || cap == 0) return;
+    std::string out;
+    for (const auto& kv : m)
+        out += kv.first + "," + std::to_string(kv.second.first) + "," + std::to_string(kv.second.second) + "\n";
+    const size_t n = std::min(out.size(), cap - 1);
+    std::memcpy(report, out.data(), n);
+    report[n] = 0;
+}
 }  // namespace jc

@@ -396,7 +396,7 @@ class JcServerStats(C.Structure):
 REQUEST_DEVICE_BUFFERS = 0x100
 
 EXPORTED += ["jc_server_create", "jc_server_destroy", "jc_server_submit", "jc_server_wait", "jc_server_get_stats",
-             "jc_server_reset_stats"]
+             "jc_server_reset_stats", "jc_server_profile"]
 
 
 def _declare_server(L):
@@ -415,6 +415,8 @@ def _declare_server(L):
     L.jc_server_get_stats.restype = C.c_int
     L.jc_server_reset_stats.argtypes = [vp]
     L.jc_server_reset_stats.restype = C.c_int
+    L.jc_server_profile.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t]
+    L.jc_server_profile.restype = C.c_int
     L._server_declared = True
 
 
@@ -487,6 +489,20 @@ class Server:
 
     def reset_stats(self) -> None:
         _check(self._L.jc_server_reset_stats(self._h))
+
+    def profile_start(self) -> None:
+        """Per-kernel timing of the loop's launches from now on (jc_server_profile)."""
+        _check(self._L.jc_server_profile(self._h, 1, None, 0))
+
+    def profile_stop(self) -> dict:
+        """{kernel name: (launches, total device ms)} since profile_start()."""
+        buf = C.create_string_buffer(1 << 16)
+        _check(self._L.jc_server_profile(self._h, 0, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split(",")
+            out[name] = (int(n), float(ms))
+        return out
 
     def out_shape(self, task: int, grid: int, ticks: int):
         c = self.forward_models[grid].config

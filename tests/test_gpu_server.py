@@ -258,3 +258,20 @@ def test_reconstruct_that_converges_early_matches_the_batch_runner(families):
     assert np.array_equal(alone, want) and np.array_equal(mixed, want)
     assert info["sweeps"] == info2["sweeps"] == int(w_sweeps)
     assert info["residual"] == info2["residual"] == np.float32(w_resid)
+
+
+def test_loop_profile_reports_its_kernels(families):
+    """jc_server_profile: per-kernel device times of the loop's launches
+    between start and stop; nothing is recorded once stopped."""
+    (fm, _, cfgs), (rm, _, _) = families
+    with engine.Server(fm, rm, max_active_cells=1 << 18) as srv:
+        srv.profile_start()
+        rid = srv.submit(engine.TASK_FORWARD, 1, random_drops(cfgs[1], seed=3), meta_of(cfgs[1]), 4)
+        srv.wait(rid, engine.TASK_FORWARD, 1, 4, timeout=60)
+        prof = srv.profile_stop()
+        rid = srv.submit(engine.TASK_FORWARD, 1, random_drops(cfgs[1], seed=4), meta_of(cfgs[1]), 4)
+        srv.wait(rid, engine.TASK_FORWARD, 1, 4, timeout=60)
+        assert srv.profile_stop() == {}
+    assert "projection" in prof and all(n > 0 and ms > 0 for n, ms in prof.values())
+    per_tick = "tc_mlp" if fm[1].precision == engine.BF16 else "f32_attention"
+    assert prof[per_tick][0] == 4 * fm[1].config.layers  # one launch per layer and tick
