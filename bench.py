@@ -850,9 +850,12 @@ def main():
     srv = engine.Server(fm, rm, max_active_cells=C5_MAX_CELLS, hbm_fraction=C5_HBM)
     rate = C5_RATES[-1]
     step_reqs = C5.draw(7 + 1000 * rank, args.requests, rate)
-    # warm-up: the same requests (tunes and allocates outside the timed steps)
+    # warm-up: the same requests (tunes and allocates outside the timed steps),
+    # then requests one at a time, so the row buckets of small batches (low
+    # arrival rates) are tuned before the rate sweep measures latency
     for _ in range(args.warmup):
         run_served(srv, wl, step_reqs, metas, device=True)
+    run_served(srv, wl, C5.draw(3 + 1000 * rank, 24, rate), metas, concurrent=False)
     barrier()
     out_dir = Path(os.environ.get("JC_BENCH_OUT") or tempfile.gettempdir())
     out_dir.mkdir(parents=True, exist_ok=True)
