@@ -173,6 +173,7 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
     memory-bound kernels. R tokens = B cells / 16, N cells = B cells."""
     R, N = B * cells // 16, B * cells
     flop = {"tc_qkv": 2 * R * D * 3 * D, "tc_proj_ln": 2 * R * D * D, "tc_mlp": 4 * R * D * F,
+            "tc_proj_mlp": 2 * R * D * D + 4 * R * D * F,
             "tc_token_mix": 18 * R * D * D, "tc_to_cells": 2 * R * D * 32, "tc_conv1": 2 * N * 35 * 9 * 32,
             "f32_ln_qkv": 2 * R * D * 3 * D, "f32_proj": 2 * R * D * D, "f32_ln_ff1": 2 * R * D * F,
             "f32_ff2": 2 * R * F * D, "f32_token_mix": 18 * R * D * D, "f32_to_cells": 2 * R * D * 32,
@@ -188,7 +189,7 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
     return None, None
 
 
-PER_LAYER = ("tc_qkv", "bf_attention", "tc_proj_ln", "tc_mlp")
+PER_LAYER = ("tc_qkv", "bf_attention", "tc_proj_ln", "tc_mlp", "tc_proj_mlp")
 
 
 def work_table(prof, cells, proj_cells, D, F, L, pk, pk_kind, where):

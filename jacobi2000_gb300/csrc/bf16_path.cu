@@ -1241,22 +1241,34 @@ constexpr int kLnMaxD = 128;  // widest row the row-per-thread LayerNorm serves
 // NC-independent K slices of 16, so every chunk width gives the same bits.
 // The residual + LayerNorm epilogue stages O through shared memory and runs
 // one warp per row.
+//
+// PROJ: the block's output projection first (cpu.rs:300-305: x += attn @ Wp
+// + bp, then LayerNorm2 into `ln`): the tile's attention rows (TMA, tmP) and
+// Wp (one bulk copy into the weight buffers, which need D * D * 2 bytes:
+// dim 128 with 64-column chunks) give P in the O accumulator; its residual +
+// LayerNorm epilogue is the one above (the arithmetic every residual +
+// LayerNorm here shares, so the result equals the separate projection
+// kernel's bit for bit); the LN2 rows are written to `ln` and read back by
+// the MLP's A load. The tile's rows of x and ln are only touched by this CTA.
 constexpr int kMlpSerialThreads = 256;
 
-__global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const __grid_constant__ CUtensorMap tmA,
+template <bool PROJ>
+__global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(const __grid_constant__ CUtensorMap tmA,
                                                              const bf16* __restrict__ W1, const bf16* __restrict__ W2,
                                                              const float* __restrict__ b1,
                                                              const float* __restrict__ b2, int D, int F, int NC, int R,
                                                              float* __restrict__ x, const float* __restrict__ g,
                                                              const float* __restrict__ b, bf16* __restrict__ ln,
-                                                             int* err) {
+                                                             int* err, const __grid_constant__ CUtensorMap tmP,
+                                                             const bf16* __restrict__ Wp, const float* __restrict__ bp,
+                                                             const float* __restrict__ g2, const float* __restrict__ be2) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;                           // [D/8][128][8]
     uint8_t* sB1 = sA + (size_t)D * 256;          // [D/8][NC][8]
     uint8_t* sB2 = sB1 + (size_t)D * NC * 2;      // [NC/8][D][8]
     uint8_t* sH = sB2 + (size_t)D * NC * 2;       // [NC/8][128][8]
     __shared__ __align__(16) float sb1[1024];
-    __shared__ uint64_t bar_a, bar_w1, bar_w2, bar_s, bar_o;
+    __shared__ uint64_t bar_a, bar_w1, bar_w2, bar_s, bar_o, bar_p, bar_pm;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1265,6 +1277,8 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     const uint32_t ncols = D <= 128 ? 256 : 512;
     const uint32_t s_col = D <= 128 ? 128 : 256;  // O in [0, D), S in [s_col, s_col + NC)
     if (threadIdx.x == 0) {
+        tc::mbar_init(&bar_p, 1);
+        tc::mbar_init(&bar_pm, 1);
         tc::mbar_init(&bar_a, 1);
         tc::mbar_init(&bar_w1, 1);
         tc::mbar_init(&bar_w2, 1);
@@ -1285,6 +1299,37 @@ __global__ void __launch_bounds__(kMlpSerialThreads) tc_mlp_serial_kernel(const 
     tc::tc_fence_after();
     const uint32_t tO = tmem_base, tS = tmem_base + s_col;
     const uint32_t a0 = tc::smem_u32(sA), w1s = tc::smem_u32(sB1), w2s = tc::smem_u32(sB2), hs = tc::smem_u32(sH);
+    if constexpr (PROJ) {
+        // P = attn @ Wp into the O accumulator, then x += P + bp, ln = LN2(x)
+        if (threadIdx.x == 0 && !failed) {
+            tc::mbar_expect_tx(&bar_p, (uint32_t)D * 256 + (uint32_t)D * D * 2);
+            for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmP, kc * 8, m0, &bar_p);
+            tc::bulk_load(sB1, Wp, (uint32_t)D * D * 2, &bar_p);
+            if (tc::mbar_wait(&bar_p, 0, err, &failed)) {
+                tc::tc_fence_after();
+                const uint32_t idesc = tc::idesc_bf16(128, D);
+                for (int k = 0; k < D / 16; k++)
+                    tc::mma_bf16(tO, tc::sdesc(a0 + k * 4096, 2048, 128), tc::sdesc(w1s + k * 2 * D * 16, D * 16, 128),
+                                 idesc, k > 0 ? 1u : 0u);
+                tc::mma_commit(&bar_pm);
+            }
+        }
+        __syncwarp();
+        const bool pok = __syncthreads_and(tc::mbar_wait(&bar_pm, 0, err, &failed) ? 1 : 0) != 0;
+        tc::tc_fence_after();
+        if (pok) {
+            // the attention tile and Wp are consumed: their shared memory holds the f32 P tile
+            float* tile = reinterpret_cast<float*>(smem);
+            stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
+            __syncthreads();
+            rows_resid_ln_any<true>(tile, D, m0, R, bp, x, g2, be2, ln, warp, kMlpSerialThreads / 32);
+        }
+        // the ln rows written above are read back by the A load (async proxy)
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        tc::tc_fence_before();
+        __syncthreads();
+        tc::tc_fence_after();
+    }
     const int nchunks = F / NC;
     const uint32_t wbytes = (uint32_t)D * NC * 2;
     auto issue_s = [&]() {  // S = A @ W1_chunk into tS
@@ -2199,7 +2244,8 @@ void BF16Path::set_kernel_attributes() {
     set_smem(tc_gemm_kernel<EPI_BF16>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_F32>, 200 * 1024);
     set_smem(tc_gemm_kernel<EPI_RESID_LN>, 200 * 1024);
-    set_smem(tc_mlp_serial_kernel, kMlpSmemMax);
+    set_smem(tc_mlp_serial_kernel<false>, kMlpSmemMax);
+    set_smem(tc_mlp_serial_kernel<true>, kMlpSmemMax);
     set_smem(tc_projln_persistent_kernel, 225 * 1024);  // 227 KB per CTA less the static shared memory
     set_smem(tc_qkv_persistent_kernel, 225 * 1024);
     set_smem(tc_conv1_persistent_kernel, 200 * 1024);
@@ -2284,15 +2330,27 @@ bool BF16Path::mlp_fits(int nc) const {
     return (nc == 32 || nc == 64) && dims_F_ % nc == 0 && mlp_serial_smem(dims_D_, nc) <= kMlpSmemMax;
 }
 
+bool BF16Path::proj_fuses(const Tuning& tu) const { return dims_D_ == 128 && tu.nc == 64; }
+
 void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln,
-                          const Pack& p, cudaStream_t s) const {
+                          const Pack& p, cudaStream_t s, const CUtensorMap* m_attn) const {
     const int D = d.D, R = p.R;
     const int v = tu.nc == 64 ? 1 : 0;
     const float* ng = l + 1 < d.L ? w.blk[l + 1].n1g : w.norm_g;
     const float* nbeta = l + 1 < d.L ? w.blk[l + 1].n1b : w.norm_b;
-    cuda_check(launch_pdl(tc_mlp_serial_kernel, (unsigned)((R + 127) / 128), kMlpSerialThreads,
-                          mlp_serial_smem(D, tu.nc), s, 1u, m_ln, w1v[v][l], w2v[v][l], w.blk[l].b1, w.blk[l].b2, D,
-                          d.F, tu.nc, R, p.x, ng, nbeta, reinterpret_cast<bf16*>(p.bt[0]), p.err),
+    const auto& B = w.blk[l];
+    bf16* ln = reinterpret_cast<bf16*>(p.bt[0]);
+    if (m_attn) {
+        if (!proj_fuses(tu)) throw Error(JC_LIMIT, "the fused projection needs dim 128 and 64-column MLP chunks");
+        cuda_check(launch_pdl(tc_mlp_serial_kernel<true>, (unsigned)((R + 127) / 128), kMlpSerialThreads,
+                              mlp_serial_smem(D, tu.nc), s, 1u, m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, tu.nc, R,
+                              p.x, ng, nbeta, ln, p.err, *m_attn, wp[l], B.bp, B.n2g, B.n2b),
+                   "launch");
+        return;
+    }
+    cuda_check(launch_pdl(tc_mlp_serial_kernel<false>, (unsigned)((R + 127) / 128), kMlpSerialThreads,
+                          mlp_serial_smem(D, tu.nc), s, 1u, m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, tu.nc, R,
+                          p.x, ng, nbeta, ln, p.err, m_ln, wp[l], B.bp, B.n2g, B.n2b),
                "launch");
 }
 
@@ -2339,7 +2397,9 @@ void BF16Path::tune(const Dims& d, const WeightsF32& w, const Pack& p, cudaStrea
     constexpr int kTuneReps = 8;
     float def_ms = 0.f, best_ms = 1e30f;
     for (int nc : {def_tuning_.nc, 96 - def_tuning_.nc}) {  // the default width first, then the other
-        if (!mlp_fits(nc)) continue;
+        // where the default width carries the fused output projection, the
+        // MLP alone is not the comparison: keep it
+        if (!mlp_fits(nc) || (nc != def_tuning_.nc && proj_fuses(def_tuning_))) continue;
         Tuning t = best;
         t.nc = nc;
         const float ms = time_launches([&] { launch_mlp(d, w, 0, t, m_ln, p, s); }, kTuneReps, s);
@@ -2501,6 +2561,13 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
             KScope k("bf_attention", s);
             launch_attention(d, qkv, p.inst, n, R, attn, tu.attn_threads, s, &p);
             check_launch("bf_attention");
+        }
+        if (proj_fuses(tu)) {
+            // output projection + LayerNorm2 inside the MLP kernel
+            KScope k("tc_proj_mlp", s);
+            launch_mlp(d, w, l, tu, m_ln, p, s, &m_attn);
+            check_launch("tc_proj_mlp");
+            continue;
         }
         {
             KScope k("tc_proj_ln", s);

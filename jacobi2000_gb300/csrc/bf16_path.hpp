@@ -65,8 +65,11 @@ class BF16Path {
     Tuning def_tuning_{64, 256};
     int n_sms_ = 1;
     bool mlp_fits(int nc) const;
+    // The fused MLP of layer l; with m_attn (attention rows) the layer's output
+    // projection + LayerNorm2 runs first in the same kernel (proj_fuses).
     void launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tuning& tu, const CUtensorMap& m_ln, const Pack& p,
-                    cudaStream_t s) const;
+                    cudaStream_t s, const CUtensorMap* m_attn = nullptr) const;
+    bool proj_fuses(const Tuning& tu) const;
     mutable std::mutex tune_mu_;
     mutable std::map<int, Tuning> tuned_;  // row-count bucket -> schedule
     std::string cache_key_;

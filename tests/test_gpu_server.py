@@ -273,5 +273,5 @@ def test_loop_profile_reports_its_kernels(families):
         srv.wait(rid, engine.TASK_FORWARD, 1, 4, timeout=60)
         assert srv.profile_stop() == {}
     assert "projection" in prof and all(n > 0 and ms > 0 for n, ms in prof.values())
-    per_tick = "tc_mlp" if fm[1].precision == engine.BF16 else "f32_attention"
+    per_tick = "tc_qkv" if fm[1].precision == engine.BF16 else "f32_attention"
     assert prof[per_tick][0] == 4 * fm[1].config.layers  # one launch per layer and tick
