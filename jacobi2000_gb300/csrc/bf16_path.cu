@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(256, (CPL <= 4 ? 3 : 1)) bf_embed_kernel(Dims 
                 float sq = 0.f;
 #pragma unroll
                 for (int c = 0; c < CPL; c++) sq += (v[q][c] - mean) * (v[q][c] - mean);
-                const float rstd = 1.0f / sqrtf(warp_sum(sq) / (float)D + 1e-5f);
+                const float rstd = rsqrtf(warp_sum(sq) / (float)D + 1e-5f);  // 2 ulp
                 float o[CPL];
 #pragma unroll
                 for (int c = 0; c < CPL; c++) o[c] = (v[q][c] - mean) * rstd * g[o0 + c] + b[o0 + c];
@@ -897,8 +897,8 @@ __device__ __forceinline__ void stage_rows(uint32_t ta, int r, int D, int c0, in
 // 4-element slot contributes ((v0 + v1) + (v2 + v3)) and, for the variance,
 // fma(e0, e0, e1 e1) + fma(e2, e2, e3 e3); slot q belongs to lane q % 32, a
 // lane sums its slots in order starting from 0, and the 32 lane partials are
-// added in the xor-butterfly order of warp_sum; out = fma((v - mean) rstd,
-// g, b).
+// added in the xor-butterfly order of warp_sum; rstd = ln_rstd(sum of
+// squared deviations); out = fma((v - mean) rstd, g, b).
 __device__ __forceinline__ float4 resid4(float4 x, float4 a, float4 bias) {
     return make_float4(__fadd_rn(x.x, __fadd_rn(a.x, bias.x)), __fadd_rn(x.y, __fadd_rn(a.y, bias.y)),
                        __fadd_rn(x.z, __fadd_rn(a.z, bias.z)), __fadd_rn(x.w, __fadd_rn(a.w, bias.w)));
@@ -908,6 +908,12 @@ __device__ __forceinline__ float sqdev4(float4 v, float m) {
     const float e0 = __fsub_rn(v.x, m), e1 = __fsub_rn(v.y, m), e2 = __fsub_rn(v.z, m), e3 = __fsub_rn(v.w, m);
     return __fadd_rn(__fmaf_rn(e0, e0, __fmul_rn(e1, e1)), __fmaf_rn(e2, e2, __fmul_rn(e3, e3)));
 }
+// 1 / sqrt(variance + eps) of the residual + LayerNorm rows: the hardware
+// reciprocal square root (rsqrtf, 2 ulp), not a rounded square root and a
+// rounded division (which cost the MLP kernel 7% of its time). Every kernel
+// that forms these rows calls this, so they keep giving the same bits.
+__device__ __forceinline__ float ln_rstd(float sq_sum, int D) { return rsqrtf(sq_sum / (float)D + 1e-5f); }
+
 __device__ __forceinline__ float ln1(float v, float m, float rstd, float g, float b) {
     return __fmaf_rn(__fmul_rn(__fsub_rn(v, m), rstd), g, b);
 }
@@ -936,7 +942,7 @@ __device__ __forceinline__ float tree32(float* a) {
 // rows in flight per warp. Rows [0, nrows) of the tile (a multiple of G),
 // tile row r -> global row m0 + r. SPL = slots per lane (1: D <= 128, 2: 256).
 // PRE: load every row group's residual rows up front (four groups at most).
-template <int SPL, bool FULL, bool PRE = false>  // FULL: every lane owns SPL slots (D = 128 SPL)
+template <int SPL, bool FULL, bool PRE = false, bool LNS = false>  // FULL: every lane owns SPL slots (D = 128 SPL)
 __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
                                 float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
                                 bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
@@ -1024,7 +1030,7 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
         for (int k = 0; k < G; k++) {
             const int row = m0 + r0 + k;
             if (row >= R) break;  // warp-uniform
-            const float rstd = 1.0f / sqrtf(q2[k] / (float)D + 1e-5f);
+            const float rstd = ln_rstd(q2[k], D);
 #pragma unroll
             for (int j = 0; j < SPL; j++) {
                 if (!on(j)) continue;
@@ -1034,15 +1040,24 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
                               ln1(v[k][j].y, mean[k], rstd, gg[j].y, be[j].y),
                               ln1(v[k][j].z, mean[k], rstd, gg[j].z, be[j].z),
                               ln1(v[k][j].w, mean[k], rstd, gg[j].w, be[j].w)};
-                BfVec<4>::store(ln + (size_t)row * D + 4 * q, o);
+                if (LNS)  // the MMA A tile in shared memory: [D/8][128][8] core matrices
+                    BfVec<4>::store(reinterpret_cast<bf16*>(reinterpret_cast<uint8_t*>(ln) + (size_t)(q >> 1) * 2048 +
+                                                            (size_t)(r0 + k) * 16 + (q & 1) * 8), o);
+                else
+                    BfVec<4>::store(ln + (size_t)row * D + 4 * q, o);
             }
         }
     }
 }
 
-template <bool PRE = false>
+// LNS: `ln` is the shared-memory A tile of an MMA (D = 128 only).
+template <bool PRE = false, bool LNS = false>
 __device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
                                   const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128) {
+    if (LNS) {
+        if (D == 128) rows_resid_ln_t<1, true, PRE, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+        return;
+    }
     if (D == 256) rows_resid_ln_t<2, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
     else if (D == 128) rows_resid_ln_t<1, true, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
     else if (D > 128) rows_resid_ln_t<2, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
@@ -1207,7 +1222,7 @@ __device__ void row_resid_ln_t(uint32_t ta, int r, int D_, uint8_t* sX, const fl
     const float mean = tree32(part) / (float)D;
 #pragma unroll
     for (int l = 0; l < 32; l++) part[l] = l < nq ? __fadd_rn(0.f, sqdev4(*xrow_chunk(sX, r, l), mean)) : 0.f;
-    const float rstd = 1.0f / sqrtf(tree32(part) / (float)D + 1e-5f);
+    const float rstd = ln_rstd(tree32(part), D);
 #pragma unroll
     for (int c = 0; c < D; c += 8) {
         const float4 v0 = *xrow_chunk(sX, r, c >> 2), v1 = *xrow_chunk(sX, r, (c >> 2) + 1);
@@ -1243,13 +1258,14 @@ constexpr int kLnMaxD = 128;  // widest row the row-per-thread LayerNorm serves
 // one warp per row.
 //
 // PROJ: the block's output projection first (cpu.rs:300-305: x += attn @ Wp
-// + bp, then LayerNorm2 into `ln`): the tile's attention rows (TMA, tmP) and
-// Wp (one bulk copy into the weight buffers, which need D * D * 2 bytes:
-// dim 128 with 64-column chunks) give P in the O accumulator; its residual +
+// + bp, then LayerNorm2): the tile's attention rows (TMA, tmP) and Wp (one
+// bulk copy into the weight buffers, which need D * D * 2 bytes: dim 128
+// with 64-column chunks) give P in the O accumulator; its residual +
 // LayerNorm epilogue is the one above (the arithmetic every residual +
 // LayerNorm here shares, so the result equals the separate projection
-// kernel's bit for bit); the LN2 rows are written to `ln` and read back by
-// the MLP's A load. The tile's rows of x and ln are only touched by this CTA.
+// kernel's bit for bit), with P staged behind sA and the LN2 rows written
+// straight into sA as the MLP's A operand (no global round trip). The
+// tile's rows of x and ln are only touched by this CTA.
 constexpr int kMlpSerialThreads = 256;
 
 template <bool PROJ>
@@ -1318,14 +1334,16 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
         const bool pok = __syncthreads_and(tc::mbar_wait(&bar_pm, 0, err, &failed) ? 1 : 0) != 0;
         tc::tc_fence_after();
         if (pok) {
-            // the attention tile and Wp are consumed: their shared memory holds the f32 P tile
-            float* tile = reinterpret_cast<float*>(smem);
+            // Wp is consumed: the f32 P tile is staged behind sA, and the LN2
+            // rows go straight into sA as the MLP's A operand
+            float* tile = reinterpret_cast<float*>(smem + (size_t)D * 256);
             stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
             __syncthreads();
-            rows_resid_ln_any<true>(tile, D, m0, R, bp, x, g2, be2, ln, warp, kMlpSerialThreads / 32);
+            rows_resid_ln_any<true, true>(tile, D, m0, R, bp, x, g2, be2, reinterpret_cast<bf16*>(sA), warp,
+                                          kMlpSerialThreads / 32);
         }
-        // the ln rows written above are read back by the A load (async proxy)
-        asm volatile("fence.proxy.async.global;" ::: "memory");
+        // the A tile written above is read by the MMAs (async proxy)
+        tc::fence_async_shared();
         tc::tc_fence_before();
         __syncthreads();
         tc::tc_fence_after();
@@ -1344,13 +1362,15 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
     // S_{j+1} is issued right after GELU_j, ahead of O_j. The MMAs and their
     // accumulation order are those of one chunk after another.
     if (threadIdx.x == 0 && !failed) {
-        tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
-        for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &bar_a);
+        if (!PROJ) {
+            tc::mbar_expect_tx(&bar_a, (uint32_t)D * 256);
+            for (int kc = 0; kc < D / 8; kc++) tc::tma_load_2d(sA + kc * 2048, &tmA, kc * 8, m0, &bar_a);
+        }
         tc::mbar_expect_tx(&bar_w1, wbytes);
         tc::bulk_load(sB1, W1, wbytes, &bar_w1);
         tc::mbar_expect_tx(&bar_w2, wbytes);
         tc::bulk_load(sB2, W2, wbytes, &bar_w2);
-        if (tc::mbar_wait(&bar_a, 0, err, &failed) && tc::mbar_wait(&bar_w1, 0, err, &failed)) {
+        if ((PROJ || tc::mbar_wait(&bar_a, 0, err, &failed)) && tc::mbar_wait(&bar_w1, 0, err, &failed)) {
             tc::tc_fence_after();
             issue_s();
         }
@@ -2321,9 +2341,11 @@ Tuning BF16Path::tuning_for(int rows) const {
     return def_tuning_;
 }
 
-// Shared memory of the MLP kernel (one stage, one h buffer).
-static size_t mlp_serial_smem(int D, int NC) {
-    return std::max((size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4);
+// Shared memory of the MLP kernel (one stage, one h buffer; with the fused
+// projection, the f32 P tile behind the A tile).
+static size_t mlp_serial_smem(int D, int NC, bool proj = false) {
+    return std::max({(size_t)D * 256 + 2 * (size_t)D * NC * 2 + (size_t)NC * 256, (size_t)128 * D * 4,
+                     proj ? (size_t)D * 256 + (size_t)128 * D * 4 : (size_t)0});
 }
 
 bool BF16Path::mlp_fits(int nc) const {
@@ -2343,7 +2365,7 @@ void BF16Path::launch_mlp(const Dims& d, const WeightsF32& w, int l, const Tunin
     if (m_attn) {
         if (!proj_fuses(tu)) throw Error(JC_LIMIT, "the fused projection needs dim 128 and 64-column MLP chunks");
         cuda_check(launch_pdl(tc_mlp_serial_kernel<true>, (unsigned)((R + 127) / 128), kMlpSerialThreads,
-                              mlp_serial_smem(D, tu.nc), s, 1u, m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, tu.nc, R,
+                              mlp_serial_smem(D, tu.nc, true), s, 1u, m_ln, w1v[v][l], w2v[v][l], B.b1, B.b2, D, d.F, tu.nc, R,
                               p.x, ng, nbeta, ln, p.err, *m_attn, wp[l], B.bp, B.n2g, B.n2b),
                    "launch");
         return;
