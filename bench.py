@@ -177,7 +177,7 @@ def kernel_work(name: str, B: int, cells: int, D: int, F: int):
             "tc_token_mix": 18 * R * D * D, "tc_to_cells": 2 * R * D * 32, "tc_conv1": 2 * N * 35 * 9 * 32,
             "f32_ln_qkv": 2 * R * D * 3 * D, "f32_proj": 2 * R * D * D, "f32_ln_ff1": 2 * R * D * F,
             "f32_ff2": 2 * R * F * D, "f32_token_mix": 18 * R * D * D, "f32_to_cells": 2 * R * D * 32,
-            "f32_conv1": 2 * N * 35 * 9 * 32, "bf_conv2_step": 2 * N * 32 * 9 * 3, "f32_conv2_step": 2 * N * 32 * 9 * 3}
+            "f32_conv1": 2 * N * 35 * 9 * 32, "tc_conv2": 2 * N * 32 * 9 * 3, "f32_conv2_step": 2 * N * 32 * 9 * 3}
     byte = {"bf_attention": R * (3 * D * 2 + D * 2), "bf_embed": N * 12 + R * (4 * D + 2 * D),
             "bf_upsample": R * 32 * 4 + N * (12 + 96), "projection": N * 12 * 4 + N * 12,
             "f32_attention": R * (3 * D * 4 + D * 4), "f32_embed": N * 12 + R * 4 * D,

@@ -132,6 +132,23 @@ static CUtensorMap tile_store_map(const void* base, int C, int nx, int ny, bool 
                     CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+// One instance's plane-major f16 cell-head grid: `planes` planes of
+// [ny][nx][8 channels], `plane` bytes apart, seen as a [planes][ny][nx * 8]
+// tensor, so each box row is a run of whole positions (one 16-byte chunk
+// each) and a box of a conv tile moves in a few long rows instead of one
+// 16-byte row per position. Halo loads: 10 x 18 positions of every plane
+// from element (x0 - 1) * 8 (a 16-byte boundary; the fill covers the grid's
+// edges), landing as [planes][18][10][8]; tile stores: 8 x 16 positions of
+// every plane from [planes][16][8][8] (positions outside the grid are not
+// written).
+static CUtensorMap cell_plane_map(const void* base, int planes, long long plane, int nx, int ny, bool halo) {
+    uint64_t dims[3] = {(uint64_t)nx * 8, (uint64_t)ny, (uint64_t)planes};
+    uint64_t strides[2] = {(uint64_t)nx * 16, (uint64_t)plane};
+    uint32_t box[3] = {(uint32_t)(halo ? (kConvTX + 2) * 8 : kConvTX * 8), (uint32_t)(halo ? kConvTY + 2 : kConvTY),
+                       (uint32_t)planes};
+    return make_map(base, 3, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT16);
+}
+
 // One instance's qkv rows as a [ty, tx, 3D] grid, loaded as 64-channel boxes
 // of side x side tokens in the 128-byte swizzled layout (attention tiles).
 static CUtensorMap att_map(const void* base, int D, int tx, int ty, int side) {
@@ -161,8 +178,12 @@ constexpr int kZcCh = 48;
 constexpr int kZcState = 32;
 constexpr int kHaloW = kConvTX + 2, kHaloH = kConvTY + 2;
 // bytes of one 8-channel plane of a halo tile (2880 used), padded so every
-// plane starts on a 128-byte boundary for TMA
+// plane starts on a 128-byte boundary for TMA (token-level halos, one load
+// per plane)
 constexpr int kHaloPlane = (kHaloW * kHaloH * 16 + 127) / 128 * 128;
+// one 8-channel plane of a cell-level halo tile, loaded with every other
+// plane by one TMA box (planes packed)
+constexpr int kCellPlane = kHaloW * kHaloH * 16;
 
 __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 
@@ -209,7 +230,11 @@ __global__ void __launch_bounds__(256, (CPL <= 4 ? 3 : 1)) bf_embed_kernel(Dims 
     static_assert(256 % kEmbedRows == 0, "embed copy layout");
     auto issue = [&](int t, int buf) {
         const int i = threadIdx.x % kEmbedRows, r = t * kEmbedRows + i;
-        const int ii = r < R ? inst_of_row(inst, n_inst, r) : -1;
+        // a warp's rows are consecutive: the instance of its first row by a
+        // warp-wide search, then at most a step or two per lane
+        int ii = warp_find_last_le(n_inst, __shfl_sync(0xffffffffu, r, 0), [&](int k) { return (long long)inst[k].row0; });
+        while (ii + 1 < n_inst && inst[ii + 1].row0 <= r) ii++;
+        if (r >= R) ii = -1;
         for (int e = threadIdx.x; e < kEmbedRows * kEmbedGroups; e += blockDim.x) {
             const int gq = e / kEmbedRows;  // (channel, patch row)
             if (gq == 0) rinst[buf][i] = ii;
@@ -677,14 +702,11 @@ __global__ void __launch_bounds__(64 * (64 / HD), 5) bf_attn_tile_kernel(Dims d,
     __shared__ uint64_t bar;
     __shared__ volatile int failed;
     const int tile = blockIdx.x, half = blockIdx.y;
-    int lo = 0, hi = n_inst - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (inst[mid].tt0 <= tile) lo = mid; else hi = mid - 1;
-    }
-    const InstDev& I = inst[lo];
-    const int tiles_x = (I.tx + kConvTX - 1) / kConvTX;
-    const int tl = tile - I.tt0;
+    const int lo = warp_find_last_le(n_inst, tile, [&](int i) { return (long long)inst[i].tt0; });
+    // the instance's fields in registers (no reloads after the barriers)
+    const int Itx = inst[lo].tx, Ity = inst[lo].ty, Itt0 = inst[lo].tt0, Irow0 = inst[lo].row0;
+    const int tiles_x = (Itx + kConvTX - 1) / kConvTX;
+    const int tl = tile - Itt0;
     const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY + half * kAttTile;
     const CUtensorMap* mkv = maps + kMapsPerInst * lo + kv_slot;
     const CUtensorMap* mq = maps + kMapsPerInst * lo + q_slot;
@@ -699,7 +721,7 @@ __global__ void __launch_bounds__(64 * (64 / HD), 5) bf_attn_tile_kernel(Dims d,
     }
     __syncthreads();
     JC_PDL_ENTRY;
-    if (y0 >= I.ty) return;  // the lower half of a tile that overhangs the grid (uniform per CTA)
+    if (y0 >= Ity) return;  // the lower half of a tile that overhangs the grid (uniform per CTA)
     if (threadIdx.x == 0 && !failed) {
         tc::tensormap_acquire(mkv);
         tc::tensormap_acquire(mq);
@@ -717,15 +739,16 @@ __global__ void __launch_bounds__(64 * (64 / HD), 5) bf_attn_tile_kernel(Dims d,
     if (tok >= kAttTile * kAttTile) return;
     const int lx = tok & 7, ly = tok >> 3;
     const int qx = x0 + lx, qy = y0 + ly;
-    if (qx >= I.tx || qy >= I.ty) return;
+    if (qx >= Itx || qy >= Ity) return;
     const float scale = 1.0f / sqrtf((float)HD);
     float acc[HD];
-    attn_stencil_token<HD>(sQ, sK, sV, lx, ly, qx, qy, I.tx, I.ty, hl, scale, acc);
-    store_head<HD>(out + ((size_t)I.row0 + (size_t)qy * I.tx + qx) * D + h * HD, acc);
+    attn_stencil_token<HD>(sQ, sK, sV, lx, ly, qx, qy, Itx, Ity, hl, scale, acc);
+    store_head<HD>(out + ((size_t)Irow0 + (size_t)qy * Itx + qx) * D + h * HD, acc);
 }
 
-// to_cells' output (f32 [rows, HD]) -> the cell-head input zc (f16 [cells,
-// 48], conv1's operand type): upsample along y then x (cpu.rs:211-245;
+// to_cells' output (f32 [rows, HD]) -> the cell-head input zc (f16, 48
+// channels, conv1's operand type, plane-major: [6][cells][8], `zc_plane`
+// elements between planes): upsample along y then x (cpu.rs:211-245;
 // weights (i + 1/2) / P, the far neighbour clamped to the grid), the state
 // appended split exactly into f16 parts (cpu.rs:339-342), zero padding. One CTA per 8 x 16 cell tile
 // (the conv tiles): the 5 x 3 tokens it reads are staged in shared memory
@@ -735,18 +758,15 @@ constexpr int kUpTokY = kConvTY / 4 + 1, kUpTokX = kConvTX / 4 + 1, kUpPitch = 3
 
 template <int HD, int C>
 __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* __restrict__ z0, const InstDev* inst,
-                                                          int n_inst, __half* __restrict__ zc) {
-    JC_PDL_ENTRY;
+                                                          int n_inst, __half* __restrict__ zc, long long zc_plane) {
     static_assert(kZcState == HD && kZcState + 3 * C <= kZcCh && HD + 4 <= kUpPitch, "zc layout");
     constexpr int P = 4;  // patch (the BF16 path is built for 4); (i + 1/2) / 4 is exact as a product
     __shared__ __align__(16) float win[kUpTokY * kUpTokX * kUpPitch];
     const int tile = blockIdx.x;
-    int lo = 0, hi = n_inst - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (inst[mid].ct0 <= tile) lo = mid; else hi = mid - 1;
-    }
-    const InstDev& I = inst[lo];
+    // the instance descriptors are written before the forward's first kernel
+    const int lo = warp_find_last_le(n_inst, tile, [&](int i) { return (long long)inst[i].ct0; });
+    const InstDev I = inst[lo];
+    JC_PDL_ENTRY;
     const int tiles_x = (I.nx + kConvTX - 1) / kConvTX;
     const int tl = tile - I.ct0;
     const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY;
@@ -789,7 +809,7 @@ __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* _
         vals[kZcState + 3 + ch] = sv - hi;  // exact in f32; rounded to f16 below
         vals[kZcState + 6 + ch] = hi;
     }
-    uint4* o = reinterpret_cast<uint4*>(zc + ((size_t)I.cell0 + cl) * kZcCh);
+    __half* o = zc + ((size_t)I.cell0 + cl) * 8;
 #pragma unroll
     for (int q = 0; q < kZcCh / 8; q++) {
         uint32_t w[4];
@@ -798,7 +818,7 @@ __global__ void __launch_bounds__(128) bf_upsample_kernel(Dims d, const float* _
             __half2 h = __floats2half2_rn(vals[8 * q + 2 * i], vals[8 * q + 2 * i + 1]);
             w[i] = *reinterpret_cast<uint32_t*>(&h);
         }
-        o[q] = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(o + q * zc_plane) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
@@ -1785,13 +1805,10 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     const int warp = threadIdx.x >> 5;
     // tile -> instance
     const int tile = blockIdx.x, nb = blockIdx.y;
-    int lo = 0, hi = n_inst - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        int t0 = KIND == CONV_TOKMIX ? inst[mid].tt0 : inst[mid].ct0;
-        if (t0 <= tile) lo = mid; else hi = mid - 1;
-    }
-    const InstDev& I = inst[lo];
+    const int lo = warp_find_last_le(n_inst, tile, [&](int i) {
+        return (long long)(KIND == CONV_TOKMIX ? inst[i].tt0 : inst[i].ct0);
+    });
+    const InstDev I = inst[lo];
     const int gw = KIND == CONV_TOKMIX ? I.tx : I.nx;
     const int tiles_x = (gw + kConvTX - 1) / kConvTX;
     const int tl = tile - (KIND == CONV_TOKMIX ? I.tt0 : I.ct0);
@@ -1916,47 +1933,74 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
-// Persistent form of conv1 (cpu.rs:343-346: 3x3 conv of the cell-head input,
-// then GELU): one CTA walks cell tiles tile = blockIdx.x + k gridDim.x with
-// its stages on separate warps, so the halo loads, the MMAs and the epilogue
-// of consecutive tiles overlap:
-//   warp 0     (one lane) TMA-loads each tile's halo into one of two slots;
-//   warp 1     (one lane) issues the 9 taps x C/16 MMAs of a tile into one of
-//              two TMEM accumulators (all nine taps' weights stay resident);
-//   warps 2-5  (one TMEM lane quarter each) add the bias, apply GELU, stage
-//              the f32 tile in one of two 128-byte swizzled boxes and store
-//              it with TMA.
-// The MMA order and the epilogue arithmetic are those of tc_conv3_kernel, so
-// the output is bit-identical.
+// Persistent cell-head convolutions on the tensor cores, one CTA walking
+// cell tiles tile = blockIdx.x + k gridDim.x with its stages on separate
+// warps, so the halo loads, the MMAs and the epilogue of consecutive tiles
+// overlap:
+//   warp 0     (one lane) TMA-loads each tile's halo into one of three slots;
+//   warp 1     (one lane) issues a tile's MMAs into one of two TMEM
+//              accumulators (the weights stay resident);
+//   warps 2-5  (one TMEM lane quarter each) run the epilogue.
+// kCellConv1, conv1 (cpu.rs:343-346): the 3x3 conv of the cell-head input zc
+// (48 f16 channels) to 32 channels as 9 taps x 3 MMAs (tap (ky, kx) is the
+// halo tile addressed from position (ky, kx)), + bias, GELU, stored as f16
+// (c1) through a staged box and a TMA store; the MMA order and the epilogue
+// arithmetic are those of tc_conv3_kernel.
+// kCellConv2, conv2 and the step (cpu.rs:347-348, 84-88): 32 -> 3 channels.
+// With 3 outputs the per-tap form would re-read the whole halo tile from
+// shared memory for 9 tiny MMAs; instead one GEMM gives every halo position
+// p its 27 tap contributions Z[p][(ky, kx), co] = c1[p] . W[co][.][ky][kx]
+// (M = the 180 halo positions in two 128-row MMAs, N = 32 with 5 zero
+// columns, K = 32 f16 channels, f32 sums), the epilogue stages Z in shared
+// memory and each output cell adds its nine neighbours' contributions in
+// tap order, + bias, + the state when the tick writes the next state, into
+// the instance's planar output. Its f16 operands and sum order make it the
+// BF16 form's own conv2 (the FP32 path keeps the reference's f32 order).
 constexpr int kC1PThreads = 6 * 32;
+constexpr int kCellConv1 = 0, kCellConv2 = 1;
 
 constexpr int kC1PHaloStages = 3;  // halo tiles in flight per CTA
+constexpr int kHaloPos = kHaloW * kHaloH;  // 180 halo positions
+constexpr int kZPitch = 33;                // f32 per staged Z row (bank-conflict-free column reads)
+
+// TMEM columns per accumulator, weight bytes and staged bytes of each kind.
+__host__ __device__ constexpr int cellconv_bn(int kind) { return kind == kCellConv1 ? 32 : 64; }
+__host__ __device__ constexpr size_t cellconv_wbytes(int kind, int C) {
+    return kind == kCellConv1 ? (size_t)9 * C * 32 * 2 : (size_t)C * 32 * 2;
+}
+__host__ __device__ constexpr size_t cellconv_stage(int kind) {
+    return kind == kCellConv1 ? (size_t)2 * 128 * 32 * 2 : (size_t)kHaloPos * kZPitch * 4;
+}
 
 struct C1PSmem {
     size_t halo, w, stage, total;
-    __host__ __device__ C1PSmem(int C, int BN) {
-        halo = 0;                                                                // stages x [C/8][18][10][8]
-        w = halo + (size_t)kC1PHaloStages * (C / 8) * kHaloPlane;                // 9 x [C/8][BN][8]
-        stage = (w + (size_t)9 * C * BN * 2 + 1023) / 1024 * 1024;  // 2 x 16 KB boxes
-        total = stage + 2 * 16384;
+    __host__ __device__ C1PSmem(int kind, int C) {
+        halo = 0;                                                          // stages x [C/8][18][10][8]
+        w = halo + (size_t)kC1PHaloStages * (C / 8) * kCellPlane;          // the weight blocks
+        stage = (w + cellconv_wbytes(kind, C) + 1023) / 1024 * 1024;       // staged output
+        total = stage + cellconv_stage(kind);
     }
 };
 
-__global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const CUtensorMap* __restrict__ maps,
-                                                                           const bf16* __restrict__ Wt,
-                                                                           const float* __restrict__ bias, int C,
-                                                                           int n_tiles, const InstDev* inst,
-                                                                           int n_inst, int* err) {
+template <int KIND>
+__global__ void __launch_bounds__(kC1PThreads) tc_cellconv_kernel(const CUtensorMap* __restrict__ maps,
+                                                                   const bf16* __restrict__ Wt,
+                                                                   const float* __restrict__ bias, int C,
+                                                                   int n_tiles, const InstDev* inst, int n_inst,
+                                                                   int mode, int* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    constexpr int BN = 32;  // conv1 outputs: one 128-byte f32 box row per position
-    const C1PSmem L(C, BN);
+    constexpr int BN = cellconv_bn(KIND);
+    constexpr int kInSlot = KIND == kCellConv1 ? 1 : 6;  // zc halo | c1 halo
+    const C1PSmem L(KIND, C);
     uint8_t* sHalo = smem + L.halo;
     uint8_t* sW = smem + L.w;
     uint8_t* sStage = smem + L.stage;
-    const size_t halo_bytes = (size_t)(C / 8) * kHaloPlane;
+    const size_t halo_bytes = (size_t)(C / 8) * kCellPlane;
+    const uint32_t wbytes = (uint32_t)cellconv_wbytes(KIND, C);
     constexpr int HS = kC1PHaloStages;
+    constexpr int kBias = KIND == kCellConv1 ? 32 : 3;
     __shared__ uint64_t w_full, h_full[HS], h_empty[HS], a_full[2], a_empty[2];
-    __shared__ __align__(16) float sbias[BN];
+    __shared__ __align__(16) float sbias[32];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1978,7 +2022,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
             atomicExch(err, 2);
         }
     }
-    if (threadIdx.x < BN) sbias[threadIdx.x] = bias[threadIdx.x];
+    if (threadIdx.x < 32) sbias[threadIdx.x] = (int)threadIdx.x < kBias ? bias[threadIdx.x] : 0.f;
     if (warp == 0) tc::tmem_alloc(&tmem_base, 2 * BN);
     tc::tc_fence_before();
     __syncthreads();
@@ -2007,22 +2051,20 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
                 if (it >= HS && !tc::mbar_wait(&h_empty[hb], (uint32_t)((it - HS) / HS) & 1u, err, &failed)) break;
                 int ii, x0, y0;
                 locate((int)blockIdx.x + it * (int)gridDim.x, ii, x0, y0);
-                const CUtensorMap* map = maps + kMapsPerInst * ii + 1;
+                const CUtensorMap* map = maps + kMapsPerInst * ii + kInSlot;
                 tc::tensormap_acquire(map);
-                tc::mbar_expect_tx(&h_full[hb], (uint32_t)(C / 8) * (kHaloW * kHaloH * 16));
-                for (int kc = 0; kc < C / 8; kc++)
-                    tc::tma_load_3d(sHalo + hb * halo_bytes + kc * kHaloPlane, map, kc * 8, x0 - 1, y0 - 1,
-                                    &h_full[hb]);
+                tc::mbar_expect_tx(&h_full[hb], (uint32_t)halo_bytes);
+                tc::tma_load_3d(sHalo + hb * halo_bytes, map, (x0 - 1) * 8, y0 - 1, 0, &h_full[hb]);
             }
         }
         __syncwarp();
     } else if (warp == 1) {
         if (lane == 0 && !failed) {
-            // MMA issuer: the nine taps' weights once, then every tile
-            tc::mbar_expect_tx(&w_full, (uint32_t)9 * C * BN * 2);
-            tc::bulk_load(sW, Wt, (uint32_t)9 * C * BN * 2, &w_full);
+            // MMA issuer: the weights once, then every tile
+            tc::mbar_expect_tx(&w_full, wbytes);
+            tc::bulk_load(sW, Wt, wbytes, &w_full);
             bool good = tc::mbar_wait(&w_full, 0, err, &failed);
-            const uint32_t idesc = tc::idesc_f16(128, BN);  // f16 input and weights
+            const uint32_t idesc = tc::idesc_f16(128, 32);  // f16 input and weights, N = 32
             const uint32_t w0 = tc::smem_u32(sW);
             for (int it = 0; it < my_tiles && good; it++) {
                 const int b = it & 1, hb = it % HS;
@@ -2032,14 +2074,27 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
                 tc::tc_fence_after();
                 const uint32_t h0 = tc::smem_u32(sHalo + hb * halo_bytes);
                 const uint32_t acc = tmem + (uint32_t)b * BN;
-                for (int t = 0; t < 9; t++) {
-                    const int ky = t / 3, kx = t % 3;
-                    const uint32_t b0 = w0 + (uint32_t)t * C * BN * 2;
-                    for (int k = 0; k < C / 16; k++) {
-                        uint64_t ad = tc::sdesc(h0 + 2 * k * kHaloPlane + (ky * kHaloW + kx) * 16, kHaloPlane, kHaloW * 16);
-                        uint64_t bd = tc::sdesc(b0 + 2 * k * BN * 16, BN * 16, 128);
-                        tc::mma_bf16(acc, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
+                if constexpr (KIND == kCellConv1) {
+                    // rows = the 8 x 16 output positions (8-row groups 10 positions apart)
+                    for (int t = 0; t < 9; t++) {
+                        const int ky = t / 3, kx = t % 3;
+                        const uint32_t b0 = w0 + (uint32_t)t * C * 32 * 2;
+                        for (int k = 0; k < C / 16; k++) {
+                            uint64_t ad = tc::sdesc(h0 + 2 * k * kCellPlane + (ky * kHaloW + kx) * 16, kCellPlane,
+                                                    kHaloW * 16);
+                            uint64_t bd = tc::sdesc(b0 + 2 * k * 32 * 16, 32 * 16, 128);
+                            tc::mma_bf16(acc, ad, bd, idesc, (t > 0 || k > 0) ? 1u : 0u);
+                        }
                     }
+                } else {
+                    // rows = halo positions 0..127 and 128..255 (those past 179,
+                    // read past the plane, are never used)
+                    for (int m = 0; m < 2; m++)
+                        for (int k = 0; k < C / 16; k++) {
+                            uint64_t ad = tc::sdesc(h0 + 2 * k * kCellPlane + m * 128 * 16, kCellPlane, 128);
+                            uint64_t bd = tc::sdesc(w0 + 2 * k * 32 * 16, 32 * 16, 128);
+                            tc::mma_bf16(acc + (uint32_t)m * 32, ad, bd, idesc, k > 0 ? 1u : 0u);
+                        }
                 }
                 tc::mma_commit(&h_empty[hb]);
                 tc::mma_commit(&a_full[b]);
@@ -2047,11 +2102,26 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
         }
         __syncwarp();
     } else {
-        // epilogue: thread r = TMEM lane r = tile position (y0 + r / 8, x0 + r % 8)
+        // epilogue: thread r = TMEM lane r
         const int r = (warp & 3) * 32 + lane;
         const bool leader = warp == 2 && lane == 0;
         for (int it = 0; it < my_tiles; it++) {
             const int b = it & 1;
+            // the tile's instance, origin and (conv2) state, fetched before
+            // the wait so their latency overlaps the MMAs
+            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+            const int ii = warp_find_last_le(n_inst, tile, [&](int i) { return (long long)inst[i].ct0; });
+            const InstDev I = inst[ii];
+            const int tiles_x = (I.nx + kConvTX - 1) / kConvTX;
+            const int x0 = ((tile - I.ct0) % tiles_x) * kConvTX, y0 = ((tile - I.ct0) / tiles_x) * kConvTY;
+            const int x = x0 + (r & 7), y = y0 + (r >> 3);
+            const bool inside = x < I.nx && y < I.ny;
+            const size_t plane = (size_t)I.nx * I.ny, cl = inside ? (size_t)y * I.nx + x : 0;
+            float st[3] = {0.f, 0.f, 0.f};
+            if (KIND == kCellConv2 && inside && mode == kWriteNextState) {
+#pragma unroll
+                for (int co = 0; co < 3; co++) st[co] = I.state[co * plane + cl];
+            }
             const bool ready = tc::mbar_wait(&a_full[b], (uint32_t)(it >> 1) & 1u, err, &failed);
             uint32_t all_ready;
             asm volatile(
@@ -2062,36 +2132,72 @@ __global__ void __launch_bounds__(kC1PThreads) tc_conv1_persistent_kernel(const 
                 : "memory");
             if (!all_ready) break;
             tc::tc_fence_after();
-            // the staging box used two tiles ago must have been read by its store
-            if (leader && it >= 2) tc::bulk_wait_read_1();
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            uint8_t* box = sStage + (size_t)b * 16384 + (size_t)r * 128;
             const uint32_t ta = lane_addr(tmem + (uint32_t)b * BN);
-            for (int c = 0; c < BN; c += 16) {
-                float a[16];
-                tc::tmem_ld16(ta + c, a);
+            if constexpr (KIND == kCellConv2) {
+                // Z rows r and 128 + r -> shared memory, then output cell r
+                float* Z = reinterpret_cast<float*>(sStage);
 #pragma unroll
-                for (int i = 0; i < 16; i += 2) gelu_fast_pair(a[i], a[i + 1], sbias[c + i], sbias[c + i + 1]);
-                const int j0 = c / 4;
+                for (int m = 0; m < 2; m++) {
+                    float a[32];
+                    tc::tmem_ld32(ta + m * 32, a);
+                    const int pos = m * 128 + r;
+                    if (pos < kHaloPos) {
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    *reinterpret_cast<float4*>(box + (((j0 + q) ^ (r & 7)) << 4)) =
-                        make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
-            }
-            tc::tc_fence_before();
-            tc::mbar_arrive(&a_empty[b]);
-            tc::fence_async_shared();
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            if (leader) {
-                int ii, x0, y0;
-                locate((int)blockIdx.x + it * (int)gridDim.x, ii, x0, y0);
-                const CUtensorMap* omap = maps + kMapsPerInst * ii + 3;
-                tc::tensormap_acquire(omap);
-                tc::tma_store_3d(omap, sStage + (size_t)b * 16384, 0, x0, y0);
-                tc::bulk_commit();
+                        for (int c = 0; c < 27; c++) Z[pos * kZPitch + c] = a[c];
+                    }
+                }
+                tc::tc_fence_before();
+                tc::mbar_arrive(&a_empty[b]);
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                const int lx = r & 7, ly = r >> 3;
+                float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int t = 0; t < 9; t++) {
+                    const float* zr = Z + ((ly + t / 3) * kHaloW + lx + t % 3) * kZPitch + 3 * t;
+#pragma unroll
+                    for (int co = 0; co < 3; co++) v[co] += zr[co];
+                }
+                if (inside) {
+#pragma unroll
+                    for (int co = 0; co < 3; co++) {
+                        float o = v[co] + sbias[co];
+                        if (mode == kWriteNextState) o = o + st[co];
+                        I.out[co * plane + cl] = o;
+                    }
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");  // Z is rewritten by the next tile
+            } else {
+                // the staging box used two tiles ago must have been read by its store
+                if (leader && it >= 2) tc::bulk_wait_read_1();
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                uint8_t* box = sStage + (size_t)b * (128 * 64) + (size_t)r * 16;  // [4 planes][128][8] f16
+                for (int c = 0; c < BN; c += 16) {
+                    float a[16];
+                    tc::tmem_ld16(ta + c, a);
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2) gelu_fast_pair(a[i], a[i + 1], sbias[c + i], sbias[c + i + 1]);
+                    uint32_t w[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        __half2 h = __floats2half2_rn(a[2 * i], a[2 * i + 1]);
+                        w[i] = *reinterpret_cast<uint32_t*>(&h);
+                    }
+                    *reinterpret_cast<uint4*>(box + (c / 8) * 2048) = make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4*>(box + (c / 8 + 1) * 2048) = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+                tc::tc_fence_before();
+                tc::mbar_arrive(&a_empty[b]);
+                tc::fence_async_shared();
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                if (leader) {
+                    const CUtensorMap* omap = maps + kMapsPerInst * ii + 3;
+                    tc::tensormap_acquire(omap);
+                    tc::tma_store_3d(omap, sStage + (size_t)b * (128 * 64), x0 * 8, y0, 0);
+                    tc::bulk_commit();
+                }
             }
         }
-        if (leader) tc::bulk_wait_read();
+        if (KIND == kCellConv1 && leader) tc::bulk_wait_read();
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -2150,6 +2256,7 @@ void BF16Path::weight_slots(std::vector<const void**>& out) const {
     add(wtm);
     add(wtc);
     add(wc1);
+    add(wc2);
 }
 
 BF16Path::BF16Path(const Dims& d, const TensorMap* tp, DeviceArena* ap) {
@@ -2258,6 +2365,18 @@ void BF16Path::upload_weights(const Dims& d, const TensorMap& t, DeviceArena& ar
                     }
         wc1 = upload_bf16(arena, o);  // f16 bits
     }
+    {
+        // conv2 (f16 operands): [32/8][32][8] over the c1 channels, column
+        // n = 3 tap + co for tap = 3 ky + kx, columns 27..31 zero
+        const auto& w = tget(t, "head.conv2.weight").data;  // [C][HD][3][3]
+        std::vector<uint16_t> o((size_t)HD * 32);
+        size_t i = 0;
+        for (int kc = 0; kc < HD / 8; kc++)
+            for (int n = 0; n < 32; n++)
+                for (int e = 0; e < 8; e++)
+                    o[i++] = f2h(n < 9 * d.C ? w[((size_t)(n % 3) * HD + kc * 8 + e) * 9 + n / 3] : 0.0f);
+        wc2 = upload_bf16(arena, o);  // f16 bits
+    }
 }
 
 void BF16Path::set_kernel_attributes() {
@@ -2268,11 +2387,11 @@ void BF16Path::set_kernel_attributes() {
     set_smem(tc_mlp_serial_kernel<true>, kMlpSmemMax);
     set_smem(tc_projln_persistent_kernel, 225 * 1024);  // 227 KB per CTA less the static shared memory
     set_smem(tc_qkv_persistent_kernel, 225 * 1024);
-    set_smem(tc_conv1_persistent_kernel, 200 * 1024);
+    set_smem(tc_cellconv_kernel<kCellConv1>, 200 * 1024);
+    set_smem(tc_cellconv_kernel<kCellConv2>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<32>, 200 * 1024);
     set_smem(bf_attn_tile_kernel<64>, 200 * 1024);
     set_smem(tc_conv3_kernel<CONV_TOKMIX>, 200 * 1024);
-    set_smem(tc_conv3_kernel<CONV_CELL1>, 200 * 1024);
     set_smem(bf_embed_kernel<1>, 100 * 1024);
     set_smem(bf_embed_kernel<2>, 100 * 1024);
     set_smem(bf_embed_kernel<3>, 100 * 1024);
@@ -2497,10 +2616,13 @@ void BF16Path::alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows,
         p.bt[i] = static_cast<char*>(a.alloc(R * strides[i] + 256));
         p.bt_stride[i] = strides[i];
     }
-    p.bc[0] = static_cast<char*>(a.alloc(NC * kZcCh * 2 + 256));
-    p.bc_stride[0] = kZcCh * 2;
-    p.bc[1] = static_cast<char*>(a.alloc(NC * d.HD * 4 + 256));  // c1, f32
-    p.bc_stride[1] = d.HD * 4;
+    // zc and c1, f16, plane-major: [channels / 8][cells][8]
+    const int planes[2] = {kZcCh / 8, d.HD / 8};
+    for (int i = 0; i < 2; i++) {
+        p.bc[i] = static_cast<char*>(a.alloc(NC * planes[i] * 16 + 256));
+        p.bc_stride[i] = 16;
+        p.bc_plane[i] = (long long)NC * 16;
+    }
     p.tmaps = a.alloc((size_t)max_inst * kMapsPerInst * sizeof(CUtensorMap));
 }
 
@@ -2510,9 +2632,10 @@ void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaS
         const InstDev& I = hinst[i];
         CUtensorMap* m = &maps[(size_t)kMapsPerInst * i];
         m[0] = halo_map(p.bt[0] + (size_t)I.row0 * p.bt_stride[0], d.D, I.tx, I.ty);
-        m[1] = halo_map(p.bc[0] + (size_t)I.cell0 * p.bc_stride[0], kZcCh, I.nx, I.ny);
+        m[1] = cell_plane_map(p.bc[0] + (size_t)I.cell0 * 16, kZcCh / 8, p.bc_plane[0], I.nx, I.ny, true);
         m[2] = tile_store_map(p.bt[3] + (size_t)I.row0 * p.bt_stride[3], d.D, I.tx, I.ty, false);
-        m[3] = tile_store_map(p.bc[1] + (size_t)I.cell0 * p.bc_stride[1], d.HD, I.nx, I.ny, true);
+        m[3] = cell_plane_map(p.bc[1] + (size_t)I.cell0 * 16, d.HD / 8, p.bc_plane[1], I.nx, I.ny, false);
+        m[6] = cell_plane_map(p.bc[1] + (size_t)I.cell0 * 16, d.HD / 8, p.bc_plane[1], I.nx, I.ny, true);
         if (attn_tile_ok(d)) {
             m[4] = att_map(p.bt[1] + (size_t)I.row0 * p.bt_stride[1], d.D, I.tx, I.ty, kAttHalo);
             m[5] = att_map(p.bt[1] + (size_t)I.row0 * p.bt_stride[1], d.D, I.tx, I.ty, kAttTile);
@@ -2531,7 +2654,6 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     bf16* qkv = reinterpret_cast<bf16*>(p.bt[1]);
     bf16* attn = reinterpret_cast<bf16*>(p.bt[2]);
     bf16* t1 = reinterpret_cast<bf16*>(p.bt[3]);
-    float* c1 = reinterpret_cast<float*>(p.bc[1]);
     const CUtensorMap m_ln = rows_map(ln, D, R), m_attn = rows_map(attn, D, R), m_t1 = rows_map(t1, D, R);
     const CUtensorMap m_qkv_out = store_map(qkv, 3 * D, R, 3 * D, false), m_z0_out = store_map(p.z0, d.HD, R, d.HD, true);
     const CUtensorMap m_x = store_map(p.x, D, R, D, true);
@@ -2629,17 +2751,28 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     {
         KScope k("bf_upsample", s);
         cuda_check(launch_pdl(bf_upsample_kernel<32, 3>, (unsigned)p.n_ctiles, 128, 0, s, 1u, d, p.z0, p.inst, n,
-                                                                       reinterpret_cast<__half*>(p.bc[0])), "launch");
+                                                                       reinterpret_cast<__half*>(p.bc[0]), p.bc_plane[0] / 2), "launch");
         check_launch("bf_upsample");
     }
     {
         KScope k("tc_conv1", s);
         const unsigned grid = (unsigned)std::min(p.n_ctiles, 2 * n_sms_);
-        cuda_check(launch_pdl(tc_conv1_persistent_kernel, grid, kC1PThreads, C1PSmem(kZcCh, d.HD).total, s, 1u, 
-            reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n, p.err), "launch");
+        cuda_check(launch_pdl(tc_cellconv_kernel<kCellConv1>, grid, kC1PThreads,
+                              C1PSmem(kCellConv1, kZcCh).total, s, 1u,
+                              reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n,
+                              mode, p.err),
+                   "launch");
         check_launch("tc_conv1");
     }
-    conv2_step(d, c1, w, p, mode, "bf_conv2_step", s);
+    {
+        KScope k("tc_conv2", s);
+        const unsigned grid = (unsigned)std::min(p.n_ctiles, 3 * n_sms_);
+        cuda_check(launch_pdl(tc_cellconv_kernel<kCellConv2>, grid, kC1PThreads, C1PSmem(kCellConv2, d.HD).total, s, 1u,
+                              reinterpret_cast<const CUtensorMap*>(p.tmaps), wc2, w.c2_b, d.HD, p.n_ctiles, p.inst, n,
+                              mode, p.err),
+                   "launch");
+        check_launch("tc_conv2");
+    }
 }
 
 }  // namespace jc

@@ -54,7 +54,7 @@ class BF16Path {
     // the MLP weights arranged for each chunk width: [0] nc 64, [1] nc 128
     const __nv_bfloat16 *w1v[2][kMaxLayers], *w2v[2][kMaxLayers];  // chunk widths 32 | 64
     int n_nc = 1;
-    const __nv_bfloat16 *wtm, *wtc, *wc1;
+    const __nv_bfloat16 *wtm, *wtc, *wc1, *wc2;
     int bn_qkv;  // N block of the q/k/v GEMM
     int bn_tm;   // N block of the token_mix convolution
 

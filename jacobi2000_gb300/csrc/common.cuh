@@ -67,6 +67,24 @@ __device__ __forceinline__ int inst_of_row(const InstDev* inst, int n, int r) {
     }
     return lo;
 }
+// The last i in [0, n) with key(i) <= v, for keys non-decreasing in i with
+// key(0) <= v, found by a whole warp (every lane calls it with the same
+// arguments and gets the answer): 32-way splits, one load per lane per
+// round, so ceil(log32 n) dependent loads instead of ceil(log2 n).
+template <class Key>
+__device__ __forceinline__ int warp_find_last_le(int n, long long v, Key key) {
+    const int lane = threadIdx.x & 31;
+    int base = 0, span = n;
+    while (span > 1) {
+        const int step = (span + 31) >> 5;
+        const bool le = lane * step < span && key(base + lane * step) <= v;
+        const unsigned m = __ballot_sync(0xffffffffu, le);
+        const int last = 31 - __clz(m);
+        base += last * step;
+        span = min(step, span - last * step);
+    }
+    return base;
+}
 __device__ __forceinline__ int inst_of_cell(const InstDev* inst, int n, long long c) {
     int lo = 0, hi = n - 1;
     while (lo < hi) {

@@ -13,7 +13,7 @@
 namespace jc {
 
 constexpr int kMaxLayers = 32;
-constexpr int kMapsPerInst = 6;  // BF16 path: ln halo, zc halo, t1 store, c1 store, qkv halo, q block
+constexpr int kMapsPerInst = 7;  // BF16 path: ln halo, zc halo, t1 store, c1 store, qkv halo, q block, c1 halo
 constexpr int kZcStride = 36;  // channel-last stride of the cell-head input: 32 z + 3 state + 1 zero
 
 // Model hyper-parameters shared by every instance of a launch.
@@ -73,6 +73,7 @@ struct Pack {
     int bt_stride[kTokBufs];
     char* bc[kCellBufs];
     int bc_stride[kCellBufs];
+    long long bc_plane[kCellBufs];  // bytes between the 8-channel planes of a plane-major cell buffer
 };
 
 enum TickMode { kWriteIncrement = 0, kWriteNextState = 1 };

@@ -511,7 +511,7 @@ uint64_t source_hash(const uint8_t* st, size_t st_len, const char* config_json) 
 }
 
 // ---------------------------------------------------------------------------
-// Pre-packed checkpoint: "JCPACK01", then little-endian u32 version (1),
+// Pre-packed checkpoint: "JCPACK01", then little-endian u32 version (2),
 // u32 precision, u64 source hash, u64 shared-tensor hash, the jc_config
 // struct, u32 has-conv2 + the Conv2Params struct, u32 slot count + u64
 // offsets, u64 image length, the image. Host and device are little-endian
@@ -551,7 +551,7 @@ PackHeader read_pack_header(const uint8_t* p, size_t n) {
     char magic[8];
     r.get(magic, 8);
     if (std::memcmp(magic, kPackMagic, 8) != 0) throw Error(JC_BAD_CHECKPOINT, "not a pre-packed checkpoint");
-    if (r.get<uint32_t>() != 1) throw Error(JC_BAD_CHECKPOINT, "unsupported pre-packed checkpoint version");
+    if (r.get<uint32_t>() != 2) throw Error(JC_BAD_CHECKPOINT, "unsupported pre-packed checkpoint version");
     PackHeader h;
     h.precision = r.get<uint32_t>();
     h.source = r.get<uint64_t>();
@@ -631,7 +631,7 @@ std::vector<uint8_t> Model::pack() const {
         out.insert(out.end(), b, b + k);
     };
     put(kPackMagic, 8);
-    const uint32_t version = 1, prec = (uint32_t)precision, has_conv2 = w.conv2 ? 1u : 0u;
+    const uint32_t version = 2, prec = (uint32_t)precision, has_conv2 = w.conv2 ? 1u : 0u;
     put(&version, 4);
     put(&prec, 4);
     put(&source_hash, 8);

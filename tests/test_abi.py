@@ -170,7 +170,7 @@ def test_packed_checkpoint_header_is_checked_before_device_work(pt_tiny):
     L = engine.load_library()
     engine._declare_pack(L)
     h = C.c_void_p()
-    for bad in (b"", b"JCPACK01", b"NOTAPACK" + bytes(64), b"JCPACK01" + (2).to_bytes(4, "little") + bytes(64)):
+    for bad in (b"", b"JCPACK01", b"NOTAPACK" + bytes(64), b"JCPACK01" + (1).to_bytes(4, "little") + bytes(64)):
         assert engine.STATUS[L.jc_model_create_packed(bad, len(bad), C.byref(h))] == "BAD_CHECKPOINT"
     st, cj = pt_tiny["st_bytes"], pt_tiny["config"]
     a = engine.source_hash(st, cj)
