@@ -15,10 +15,12 @@ saturating rate).
   (requests carry device pointers), timed on the device: CUDA events on the
   server's stream from the start of its first iteration to the end of its
   last, summed over the timed steps.
-* ``e2e``: the same runs through the C ABI with host buffers
-  (jc_server_submit / jc_server_wait): wall clock from the first arrival to
-  the last result in host memory, host->device and device->host copies
-  inside.
+* ``e2e``: the same runs through the C ABI from the caller's page-locked
+  host buffers (jc_server_submit / jc_server_wait with
+  JC_REQUEST_DEVICE_BUFFERS): wall clock from the first arrival to the last
+  result in host memory, every request's host->device and device->host
+  copies inside. ``served.pageable_host_buffers``: the same from pageable
+  numpy buffers, which the server stages.
 * ``served.rates``: throughput and p50/p99 latency per arrival rate (host
   buffers).
 * ``fp32_plain``: the plain FP32 kernel path, one request at a time; and
@@ -322,13 +324,15 @@ def c5_configs(args):
     return [parse_config(fam[(s, s)][1], fam[(s, s)][0]) for s in C5_SIDES]
 
 
-def run_served(srv, wl, reqs, metas, device=False, concurrent=True):
+def run_served(srv, wl, reqs, metas, device=False, concurrent=True, pinned=False):
     """Submits `reqs` at their arrival times (concurrent) or one after the
     previous result (sequential) and collects every result. Host mode: host
-    buffers in and out through jc_server_submit / jc_server_wait. Device mode:
-    inputs already in device memory, results copied to device memory
-    (JC_REQUEST_DEVICE_BUFFERS). Latency per request is the server's submit to
-    completion time plus how late the submission was."""
+    buffers (numpy, pageable) in and out through jc_server_submit /
+    jc_server_wait, which stage them. Pinned mode: the caller's page-locked
+    host buffers, read and written by DMA (JC_REQUEST_DEVICE_BUFFERS). Device
+    mode: inputs already in device memory, results copied to device memory.
+    Latency per request is the server's submit to completion time plus how
+    late the submission was."""
     import threading
 
     from jacobi2000_gb300 import engine
@@ -337,13 +341,15 @@ def run_served(srv, wl, reqs, metas, device=False, concurrent=True):
     h2d = sum(x.nbytes + (k.nbytes if k is not None else 0) + metas[r["g"]].nbytes for r, (x, k) in zip(reqs, ins))
     d2h = sum(x.nbytes for x, _ in ins)
     dev = None
-    if device:
+    if device or pinned:
         import torch
 
-        dev = [(torch.from_numpy(x).cuda(), torch.from_numpy(k).cuda() if k is not None else None,
-                torch.from_numpy(metas[r["g"]]).cuda(), torch.empty(x.shape, device="cuda"))
+        put = (lambda a: torch.from_numpy(a).pin_memory()) if pinned else (lambda a: torch.from_numpy(a).cuda())
+        dev = [(put(x), put(k) if k is not None else None, put(metas[r["g"]]),
+                torch.empty(x.shape, pin_memory=True) if pinned else torch.empty(x.shape, device="cuda"))
                for r, (x, k) in zip(reqs, ins)]
         torch.cuda.synchronize()
+        device = True
     srv.reset_stats()
     lat = [None] * len(reqs)
     ids = [None] * len(reqs)
@@ -871,8 +877,14 @@ def main():
     useful = wl.useful(step_reqs)
     value = whole_job_rate(useful, world, ms)
     launches = sum(r["launches"] for r in runs)
-    # end to end with host buffers through the C ABI
-    e2e_runs = [run_served(srv, wl, step_reqs, metas, device=False) for _ in range(2)]
+    # end to end through the C ABI from page-locked host buffers: every
+    # request's inputs copied host -> device and its result device -> host
+    # inside the timed wall time
+    e2e_runs = [run_served(srv, wl, step_reqs, metas, pinned=True) for _ in range(2)]
+    # and from pageable host buffers, which the server stages (one untimed run
+    # first: its page-locked staging buffers are allocated on first use)
+    run_served(srv, wl, step_reqs, metas, device=False)
+    staged = run_served(srv, wl, step_reqs, metas, device=False)
     e2e_ms = max_over_ranks(1e3 * statistics.mean(r["wall_s"] for r in e2e_runs), world, "cuda")
     # one more step with CUDA events around every launch of the loop: the
     # per-kernel table and the roofline of the served workload's top kernel
@@ -891,8 +903,10 @@ def main():
                                      "p99_ms": statistics.median(r["p99_ms"] for r in runs),
                                      "iterations_per_step": statistics.mean(r["iterations"] for r in runs),
                                      "work_cell_ticks_per_s": wl.work(step_reqs) / (dev_s / args.steps)},
-                  "host_buffers": {k: e2e_runs[-1][k] for k in ("cell_ticks_per_s_wall", "p50_ms", "p99_ms",
-                                                                  "wall_s")},
+                  "pinned_host_buffers": {k: e2e_runs[-1][k] for k in ("cell_ticks_per_s_wall", "p50_ms",
+                                                                         "p99_ms", "wall_s")},
+                  "pageable_host_buffers": {k: staged[k] for k in ("cell_ticks_per_s_wall", "p50_ms", "p99_ms",
+                                                                   "wall_s")},
                   "rates": []}
         if not args.no_sweep:
             for r_ in C5_RATES:

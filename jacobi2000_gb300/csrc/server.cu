@@ -74,10 +74,82 @@ __global__ void recon_fill_kernel(float* __restrict__ vol, const float* __restri
     }
 }
 
+// Page-locked host buffers for the inputs and results of host-buffer
+// requests, kept per power-of-two size class and reused: copies between them
+// and the device are asynchronous DMA, where pageable memory would make each
+// copy a staged, synchronous one on the serving thread. The pool only grows
+// (to the peak of buffers in use) and is freed with the server.
+class PinnedPool {
+   public:
+    ~PinnedPool() {
+        for (void* p : all_) cudaFreeHost(p);
+    }
+    void* get(size_t bytes, size_t& cap) {
+        cap = kMin;
+        while (cap < bytes) cap <<= 1;
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            auto& f = free_[cap];
+            if (!f.empty()) {
+                void* p = f.back();
+                f.pop_back();
+                return p;
+            }
+        }
+        void* p = nullptr;
+        cuda_check(cudaMallocHost(&p, cap), "cudaMallocHost", JC_OVER_BUDGET);
+        std::lock_guard<std::mutex> g(mu_);
+        all_.push_back(p);
+        return p;
+    }
+    void put(void* p, size_t cap) {
+        std::lock_guard<std::mutex> g(mu_);
+        free_[cap].push_back(p);
+    }
+
+   private:
+    static constexpr size_t kMin = 4096;
+    std::mutex mu_;
+    std::map<size_t, std::vector<void*>> free_;
+    std::vector<void*> all_;
+};
+
+// A buffer of the pool, returned to it when the owner is destroyed or
+// reassigned (move-only, like the request that owns it).
+struct PinnedBuf {
+    PinnedPool* pool = nullptr;
+    void* p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(PinnedPool& pl, size_t bytes) : pool(&pl) { p = pl.get(bytes, cap); }
+    PinnedBuf(PinnedBuf&& o) noexcept : pool(o.pool), p(o.p), cap(o.cap) { o.p = nullptr; }
+    PinnedBuf& operator=(PinnedBuf&& o) noexcept {
+        if (this != &o) {
+            reset();
+            pool = o.pool;
+            p = o.p;
+            cap = o.cap;
+            o.p = nullptr;
+        }
+        return *this;
+    }
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { reset(); }
+    void reset() {
+        if (p) pool->put(p, cap);
+        p = nullptr;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
 }  // namespace
 
-// Request flag: x, known and meta are device pointers (valid until the request
-// is done), and jc_server_wait's `out` is a device pointer.
+// Request flag: x, known and meta are caller-owned device or page-locked host
+// buffers (valid until the request is done), and so is jc_server_wait's `out`.
 constexpr uint32_t kDeviceBuffers = JC_REQUEST_DEVICE_BUFFERS;
 
 struct Request {
@@ -93,10 +165,8 @@ struct Request {
     int sweeps = 0, frozen = 0;          // reconstruct: host copy of the device bookkeeping
     float residual = 0.f;
     size_t cells = 0, bytes = 0;
-    // host copies of the inputs (host buffers), and the result
-    std::vector<float> x, out;
-    std::vector<uint8_t> known;
-    std::vector<float> meta;
+    // page-locked copies of the inputs (host buffers), and the result
+    PinnedBuf x, out, known, meta;
     // caller's device inputs (device buffers)
     const float* dev_x = nullptr;
     const uint8_t* dev_known = nullptr;
@@ -132,6 +202,7 @@ class Server {
     std::map<std::string, std::pair<int, double>> profile_stop();
 
    private:
+    PinnedPool pinned_;  // first member: outlives every request's buffers
     std::vector<Model*> fwd_, rev_;
     Dims dims_{};
     int precision_ = JC_FP32;
@@ -282,17 +353,25 @@ uint64_t Server::submit(const jc_request& r) {
             q.dev_x = r.x;
             q.dev_known = r.known;
         } else {
-            q.x.assign(r.x, r.x + vol * len);
-            q.known.assign(r.known, r.known + vol * q.cells);
+            q.x = PinnedBuf(pinned_, vol * len * 4);
+            std::memcpy(q.x.p, r.x, vol * len * 4);
+            q.known = PinnedBuf(pinned_, vol * q.cells);
+            std::memcpy(q.known.p, r.known, vol * q.cells);
         }
         q.bytes = vol * len * 4 * 2 + 2 * (size_t)r.ticks * len * 4 + vol * q.cells + 4096;
     } else {
         if (q.device_io) q.dev_x = r.x;
-        else q.x.assign(r.x, r.x + len);
+        else {
+            q.x = PinnedBuf(pinned_, len * 4);
+            std::memcpy(q.x.p, r.x, len * 4);
+        }
         q.bytes = len * 4 + 4096;
     }
     if (q.device_io) q.dev_meta = r.meta;
-    else q.meta.assign(r.meta, r.meta + m.cfg.meta_dim);
+    else {
+        q.meta = PinnedBuf(pinned_, (size_t)m.cfg.meta_dim * 4);
+        std::memcpy(q.meta.p, r.meta, (size_t)m.cfg.meta_dim * 4);
+    }
     q.r.x = nullptr;
     q.r.known = nullptr;
     q.r.meta = nullptr;
@@ -344,11 +423,11 @@ void Server::wait(uint64_t id, float* out, size_t out_len, jc_result* info, doub
         // the result is in the request's device buffer, written by work that
         // has completed (the chunk that finished it was synchronized)
         if (out) {
-            cuda_check(cudaMemcpyAsync(out, q.d_state, n * 4, cudaMemcpyDeviceToDevice, wait_stream_), "D2D", JC_MAP);
+            cuda_check(cudaMemcpyAsync(out, q.d_state, n * 4, cudaMemcpyDefault, wait_stream_), "result copy", JC_MAP);
             cuda_check(cudaStreamSynchronize(wait_stream_), "cudaStreamSynchronize", JC_POLL);
         }
     } else if (out) {
-        std::memcpy(out, q.out.data(), n * 4);
+        std::memcpy(out, q.out.p, n * 4);
     }
     if (info) {
         info->latency_s = q.t_done - q.t_submit;
@@ -412,10 +491,11 @@ void Server::allocate(Request& q) {
         cuda_check(cudaMallocAsync(&p, bytes, stream_), "cudaMallocAsync", JC_OVER_BUDGET);
         return p;
     };
-    const cudaMemcpyKind in_kind = q.device_io ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    // caller-owned buffers: device or page-locked host memory (unified addressing tells which)
+    const cudaMemcpyKind in_kind = q.device_io ? cudaMemcpyDefault : cudaMemcpyHostToDevice;
     q.d_meta = static_cast<float*>(get(64 * 4));
     q.d_slot = static_cast<ProjSlot*>(get(sizeof(ProjSlot)));
-    cuda_check(cudaMemcpyAsync(q.d_meta, q.device_io ? q.dev_meta : q.meta.data(), dims_.meta_dim * 4, in_kind,
+    cuda_check(cudaMemcpyAsync(q.d_meta, q.device_io ? q.dev_meta : q.meta.as<float>(), dims_.meta_dim * 4, in_kind,
                                stream_),
                "meta", JC_MAP);
     if (q.recon()) {
@@ -425,9 +505,9 @@ void Server::allocate(Request& q) {
         q.d_F = static_cast<float*>(get(H * len * 4));
         q.d_R = static_cast<float*>(get(H * len * 4));
         q.d_known = static_cast<uint8_t*>(get((H + 1) * q.cells));
-        cuda_check(cudaMemcpyAsync(q.d_vals, q.device_io ? q.dev_x : q.x.data(), (H + 1) * len * 4, in_kind, stream_),
+        cuda_check(cudaMemcpyAsync(q.d_vals, q.device_io ? q.dev_x : q.x.as<float>(), (H + 1) * len * 4, in_kind, stream_),
                    "reconstruct values", JC_MAP);
-        cuda_check(cudaMemcpyAsync(q.d_known, q.device_io ? q.dev_known : q.known.data(), (H + 1) * q.cells, in_kind,
+        cuda_check(cudaMemcpyAsync(q.d_known, q.device_io ? q.dev_known : q.known.as<uint8_t>(), (H + 1) * q.cells, in_kind,
                                    stream_),
                    "reconstruct mask", JC_MAP);
         KScope k("recon_fill", stream_);
@@ -436,7 +516,7 @@ void Server::allocate(Request& q) {
         cuda_check(cudaGetLastError(), "reconstruct fill");
     } else {
         q.d_state = static_cast<float*>(get(len * 4));
-        cuda_check(cudaMemcpyAsync(q.d_state, q.device_io ? q.dev_x : q.x.data(), len * 4, in_kind, stream_), "state",
+        cuda_check(cudaMemcpyAsync(q.d_state, q.device_io ? q.dev_x : q.x.as<float>(), len * 4, in_kind, stream_), "state",
                    JC_MAP);
     }
 }
@@ -801,9 +881,9 @@ void Server::iteration(std::vector<Request*>& act, int K) {
     for (Request* q : act) {
         if (q->recon() || q->remaining() > K) continue;
         if (!q->device_io) {
-            q->out.resize(3 * q->cells);
-            cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s),
-                       "D2H", JC_MAP);
+            q->out = PinnedBuf(pinned_, 3 * q->cells * 4);
+            cuda_check(cudaMemcpyAsync(q->out.p, q->d_state, 3 * q->cells * 4, cudaMemcpyDeviceToHost, s), "D2H",
+                       JC_MAP);
         }
         cuda_check(cudaMemcpyAsync(&h_slots_[finishing.size()], q->d_slot, sizeof(ProjSlot), cudaMemcpyDeviceToHost, s),
                    "D2H", JC_MAP);
@@ -850,8 +930,8 @@ void Server::iteration(std::vector<Request*>& act, int K) {
         q->residual = h_recon_[i].last_resid;
         if (q->frozen) {
             if (!q->device_io) {
-                q->out.resize(q->out_floats());
-                cuda_check(cudaMemcpyAsync(q->out.data(), q->d_state, q->out.size() * 4, cudaMemcpyDeviceToHost, s),
+                q->out = PinnedBuf(pinned_, q->out_floats() * 4);
+                cuda_check(cudaMemcpyAsync(q->out.p, q->d_state, q->out_floats() * 4, cudaMemcpyDeviceToHost, s),
                            "D2H", JC_MAP);
             }
             recon_done.push_back(q);

@@ -473,15 +473,17 @@ class Server:
     def submit_device(self, task: int, grid: int, x_ptr: int, meta_ptr: int, ticks: int,
                       flags: int = PROJECT_MASS | PROJECT_ENERGY, known_ptr: int | None = None, max_sweeps: int = 4,
                       tol: float = 1e-3) -> int:
-        """submit() with device-resident inputs (device pointers that must stay
-        valid until the request is done); collect with wait_device()."""
+        """submit() with caller-owned inputs: device pointers, or page-locked
+        host pointers (copied by DMA), that must stay valid until the request
+        is done; collect with wait_device()."""
         req = JcRequest(int(task), int(grid), int(ticks), int(flags) | REQUEST_DEVICE_BUFFERS, int(x_ptr),
                         int(known_ptr) if known_ptr else None, int(meta_ptr), int(max_sweeps), float(tol))
         return self._submit(req)
 
     def wait_device(self, rid: int, out_ptr: int | None, out_len: int, timeout: float = -1.0) -> dict:
         """Waits for a request submitted with submit_device and copies its
-        result to the device pointer `out_ptr` (out_len floats; None: drop it)."""
+        result to `out_ptr`, a device or page-locked host pointer (out_len
+        floats; None: drop it)."""
         info = JcResult()
         _check(self._L.jc_server_wait(self._h, int(rid), int(out_ptr) if out_ptr else None, int(out_len),
                                       C.byref(info), float(timeout)))
