@@ -88,6 +88,9 @@ def parse_args():
     ap.add_argument("--no-eval", action="store_true", help="skip the eval-metrics measurement")
     ap.add_argument("--only-served", action="store_true",
                     help="the served steps alone (for profiling): no FP32, batched, CPU or accuracy runs")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="the batched extra alone (for profiling): --instances x --side^2 grids, --ticks ticks; "
+                         "prints its JSON and exits")
     return ap.parse_args()
 
 
@@ -849,6 +852,12 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    if args.only_batched:
+        batched, broof, btable = batched_bench(args, world, barrier)
+        if rank == 0:
+            batched.update({"roofline": broof, "kernels": btable})
+            print(json.dumps(batched), flush=True)
+        return
     pk, pk_kind = peaks()
     cfgs = c5_configs(args)
     metas = [meta_of(c) for c in cfgs]

@@ -1937,14 +1937,15 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
 // cell tiles tile = blockIdx.x + k gridDim.x with its stages on separate
 // warps, so the halo loads, the MMAs and the epilogue of consecutive tiles
 // overlap:
-//   warp 0     (one lane) TMA-loads each tile's halo into one of three slots;
+//   warp 0     (one lane) TMA-loads each tile's halo into one of two slots;
 //   warp 1     (one lane) issues a tile's MMAs into one of two TMEM
 //              accumulators (the weights stay resident);
 //   warps 2-5  (one TMEM lane quarter each) run the epilogue.
 // kCellConv1, conv1 (cpu.rs:343-346): the 3x3 conv of the cell-head input zc
 // (48 f16 channels) to 32 channels as 9 taps x 3 MMAs (tap (ky, kx) is the
 // halo tile addressed from position (ky, kx)), + bias, GELU, stored as f16
-// (c1) through a staged box and a TMA store; the MMA order and the epilogue
+// (c1) through one staged box (the next tile's epilogue waits until the
+// store has read it) and a TMA store; the MMA order and the epilogue
 // arithmetic are those of tc_conv3_kernel.
 // kCellConv2, conv2 and the step (cpu.rs:347-348, 84-88): 32 -> 3 channels.
 // With 3 outputs the per-tap form would re-read the whole halo tile from
@@ -1959,7 +1960,9 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
 constexpr int kC1PThreads = 6 * 32;
 constexpr int kCellConv1 = 0, kCellConv2 = 1;
 
-constexpr int kC1PHaloStages = 3;  // halo tiles in flight per CTA
+// halo tiles in flight per CTA: two, so that three conv1 CTAs (four conv2
+// CTAs) fit on an SM, which measured faster than three stages at two (three)
+constexpr int kC1PHaloStages = 2;
 constexpr int kHaloPos = kHaloW * kHaloH;  // 180 halo positions
 constexpr int kZPitch = 33;                // f32 per staged Z row (bank-conflict-free column reads)
 
@@ -1969,7 +1972,7 @@ __host__ __device__ constexpr size_t cellconv_wbytes(int kind, int C) {
     return kind == kCellConv1 ? (size_t)9 * C * 32 * 2 : (size_t)C * 32 * 2;
 }
 __host__ __device__ constexpr size_t cellconv_stage(int kind) {
-    return kind == kCellConv1 ? (size_t)2 * 128 * 32 * 2 : (size_t)kHaloPos * kZPitch * 4;
+    return kind == kCellConv1 ? (size_t)128 * 32 * 2 : (size_t)kHaloPos * kZPitch * 4;
 }
 
 struct C1PSmem {
@@ -2168,9 +2171,9 @@ __global__ void __launch_bounds__(kC1PThreads) tc_cellconv_kernel(const CUtensor
                 asm volatile("bar.sync 1, 128;" ::: "memory");  // Z is rewritten by the next tile
             } else {
                 // the staging box used two tiles ago must have been read by its store
-                if (leader && it >= 2) tc::bulk_wait_read_1();
+                if (leader && it >= 1) tc::bulk_wait_read();
                 asm volatile("bar.sync 1, 128;" ::: "memory");
-                uint8_t* box = sStage + (size_t)b * (128 * 64) + (size_t)r * 16;  // [4 planes][128][8] f16
+                uint8_t* box = sStage + (size_t)r * 16;  // [4 planes][128][8] f16
                 for (int c = 0; c < BN; c += 16) {
                     float a[16];
                     tc::tmem_ld16(ta + c, a);
@@ -2192,7 +2195,7 @@ __global__ void __launch_bounds__(kC1PThreads) tc_cellconv_kernel(const CUtensor
                 if (leader) {
                     const CUtensorMap* omap = maps + kMapsPerInst * ii + 3;
                     tc::tensormap_acquire(omap);
-                    tc::tma_store_3d(omap, sStage + (size_t)b * (128 * 64), x0 * 8, y0, 0);
+                    tc::tma_store_3d(omap, sStage, x0 * 8, y0, 0);
                     tc::bulk_commit();
                 }
             }
@@ -2756,7 +2759,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     }
     {
         KScope k("tc_conv1", s);
-        const unsigned grid = (unsigned)std::min(p.n_ctiles, 2 * n_sms_);
+        const unsigned grid = (unsigned)std::min(p.n_ctiles, 3 * n_sms_);
         cuda_check(launch_pdl(tc_cellconv_kernel<kCellConv1>, grid, kC1PThreads,
                               C1PSmem(kCellConv1, kZcCh).total, s, 1u,
                               reinterpret_cast<const CUtensorMap*>(p.tmaps), wc1, w.c1_b, kZcCh, p.n_ctiles, p.inst, n,
@@ -2766,7 +2769,7 @@ void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mo
     }
     {
         KScope k("tc_conv2", s);
-        const unsigned grid = (unsigned)std::min(p.n_ctiles, 3 * n_sms_);
+        const unsigned grid = (unsigned)std::min(p.n_ctiles, 4 * n_sms_);
         cuda_check(launch_pdl(tc_cellconv_kernel<kCellConv2>, grid, kC1PThreads, C1PSmem(kCellConv2, d.HD).total, s, 1u,
                               reinterpret_cast<const CUtensorMap*>(p.tmaps), wc2, w.c2_b, d.HD, p.n_ctiles, p.inst, n,
                               mode, p.err),
