@@ -172,10 +172,11 @@ def test_submissions_from_many_threads(families):
 
 
 def test_device_buffer_requests_equal_host_requests(families):
-    """Requests whose inputs and results are device memory
-    (JC_REQUEST_DEVICE_BUFFERS) give the same bits as host-buffer requests
-    and as the model's own rollout; the server's device-timed span covers
-    the work."""
+    """Requests whose inputs and results are the caller's buffers
+    (JC_REQUEST_DEVICE_BUFFERS), device memory or page-locked host memory,
+    give the same bits as host-buffer requests (staged by the server) and as
+    the model's own rollout; the server's device-timed span covers the
+    work."""
     torch = pytest.importorskip("torch")
     (fm, _, cfgs), (rm, _, _) = families
     rng = np.random.default_rng(11)
@@ -208,8 +209,19 @@ def test_device_buffer_requests_equal_host_requests(families):
         for rid, o in zip(ids, outs):
             srv.wait_device(rid, o.data_ptr(), o.numel(), timeout=60)
         st = srv.stats()
-    for (task, g, H, x, known, meta), h, o in zip(reqs, host, outs):
+        # the same flag with page-locked host buffers: copied by DMA, no staging
+        pin_in = [(torch.from_numpy(np.ascontiguousarray(x)).pin_memory(),
+                   torch.from_numpy(np.ascontiguousarray(known)).pin_memory() if known is not None else None,
+                   torch.from_numpy(np.ascontiguousarray(meta)).pin_memory()) for _, _, _, x, known, meta in reqs]
+        pin_out = [torch.empty(srv.out_shape(task, g, H), pin_memory=True) for task, g, H, _, _, _ in reqs]
+        ids = [srv.submit_device(task, g, px.data_ptr(), pm.data_ptr(), H, ME,
+                                 known_ptr=pk.data_ptr() if pk is not None else None, max_sweeps=3, tol=0.0)
+               for (task, g, H, _, _, _), (px, pk, pm) in zip(reqs, pin_in)]
+        for rid, o in zip(ids, pin_out):
+            srv.wait_device(rid, o.data_ptr(), o.numel(), timeout=60)
+    for (task, g, H, x, known, meta), h, o, po in zip(reqs, host, outs, pin_out):
         assert np.array_equal(o.cpu().numpy(), h), (task, g, H)
+        assert np.array_equal(po.numpy(), h), (task, g, H)
         if task != engine.TASK_RECONSTRUCT:
             model = fm[g] if task == engine.TASK_FORWARD else rm[g]
             assert np.array_equal(h, model.rollout(x, meta, H, ME)[0])
