@@ -82,7 +82,8 @@ enum TickMode { kWriteIncrement = 0, kWriteNextState = 1 };
 // state to each instance's `out`.
 void forward_f32(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cudaStream_t s);
 
-// head.conv2 + the step's residual over f32 c1 [cells, HD] (both paths).
+// head.conv2 + the step's residual over f32 c1 [cells, HD], in the reference's
+// f32 order (the FP32 path; the BF16 form runs its own tensor-core conv2).
 void conv2_step(const Dims& d, const float* c1, const WeightsF32& w, const Pack& p, int mode, const char* name,
                 cudaStream_t s);
 
