@@ -1767,9 +1767,9 @@ __global__ void __launch_bounds__(kQKVPThreads, 1) tc_qkv_persistent_kernel(
 // (y0 + r/8, x0 + r%8)); the halo tile [C/8 planes][18][10][8] is loaded by
 // TMA (zero fill outside the grid); tap (ky, kx) is the halo addressed from
 // offset (ky*10 + kx)*16 bytes. B per tap: [C/8][BN][8] (the N block `nb`).
-// Epilogues: TOKMIX: out = xn + gelu(acc + b) (cpu.rs:326-328), bf16;
-//            CONV1:  out = gelu(acc + b)      (cpu.rs:345-346), f32.
-enum { CONV_TOKMIX = 0, CONV_CELL1 = 1 };
+// Epilogue (token_mix): out = xn + gelu(acc + b) (cpu.rs:326-328), bf16. The
+// cell-head convolutions have their own persistent kernel (tc_cellconv_kernel).
+enum { CONV_TOKMIX = 0 };
 
 // Shared memory of tc_conv3_kernel: the halo planes, then NS tap weight
 // blocks; with NS = 9 every tap is resident and loaded once.
@@ -1794,6 +1794,7 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
                                                        int store_slot, const bf16* __restrict__ Wt,
                                                        const float* __restrict__ bias, int C, int BN, int NS,
                                                        const InstDev* inst, int n_inst, int* err) {
+    static_assert(KIND == CONV_TOKMIX, "token_mix only");
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sHalo = smem;                                   // [C/8][18][10][8]
     uint8_t* sB = smem + (size_t)(C / 8) * kHaloPlane;       // NS x [C/8][BN][8]
@@ -1806,12 +1807,12 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
     // tile -> instance
     const int tile = blockIdx.x, nb = blockIdx.y;
     const int lo = warp_find_last_le(n_inst, tile, [&](int i) {
-        return (long long)(KIND == CONV_TOKMIX ? inst[i].tt0 : inst[i].ct0);
+        return (long long)inst[i].tt0;
     });
     const InstDev I = inst[lo];
-    const int gw = KIND == CONV_TOKMIX ? I.tx : I.nx;
+    const int gw = I.tx;
     const int tiles_x = (gw + kConvTX - 1) / kConvTX;
-    const int tl = tile - (KIND == CONV_TOKMIX ? I.tt0 : I.ct0);
+    const int tl = tile - I.tt0;
     const int x0 = (tl % tiles_x) * kConvTX, y0 = (tl / tiles_x) * kConvTY;
     const CUtensorMap* map = maps + kMapsPerInst * lo + map_slot;
     const CUtensorMap* omap = maps + kMapsPerInst * lo + store_slot;
@@ -1884,40 +1885,28 @@ __global__ void __launch_bounds__(128) tc_conv3_kernel(const CUtensorMap* __rest
         // positions outside the grid are clipped by the store
         const int r = threadIdx.x;
         const uint32_t ta = lane_addr(tmem);
-        constexpr int EB = KIND == CONV_TOKMIX ? 2 : 4;  // bytes per output element
-        constexpr int PB = 128 / EB;                     // elements per box row
-        // TOKMIX still reads the halo centre, so it stages after the halo
-        uint8_t* stage = smem + conv3_stage_offset(C, KIND == CONV_TOKMIX);
+        constexpr int EB = 2;        // bytes per output element (bf16)
+        constexpr int PB = 128 / EB;  // elements per box row
+        // the epilogue still reads the halo centre, so it stages after the halo
+        uint8_t* stage = smem + conv3_stage_offset(C, true);
         for (int c = 0; c < BN; c += 16) {
             float a[16];
             tc::tmem_ld16(ta + c, a);
-            if (KIND == CONV_TOKMIX) {
-                // the centre of the halo tile is xn at this token
-                const uint8_t* centre = sHalo + ((r / kConvTX + 1) * kHaloW + (r % kConvTX + 1)) * 16;
-                const int n0 = nb * BN;
+            // the centre of the halo tile is xn at this token
+            const uint8_t* centre = sHalo + ((r / kConvTX + 1) * kHaloW + (r % kConvTX + 1)) * 16;
+            const int n0 = nb * BN;
 #pragma unroll
-                for (int i = 0; i < 16; i += 2) gelu_fast_pair(a[i], a[i + 1], sbias[c + i], sbias[c + i + 1]);
+            for (int i = 0; i < 16; i += 2) gelu_fast_pair(a[i], a[i + 1], sbias[c + i], sbias[c + i + 1]);
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const int ch = n0 + c + i;
-                    const float xn = bf2f(*reinterpret_cast<const bf16*>(centre + (size_t)(ch / 8) * kHaloPlane + (ch % 8) * 2));
-                    a[i] = xn + a[i];
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 16; i++) a[i] = gelu_fast(a[i] + sbias[c + i]);
+            for (int i = 0; i < 16; i++) {
+                const int ch = n0 + c + i;
+                const float xn = bf2f(*reinterpret_cast<const bf16*>(centre + (size_t)(ch / 8) * kHaloPlane + (ch % 8) * 2));
+                a[i] = xn + a[i];
             }
             uint8_t* box = stage + (size_t)(c / PB) * 16384 + (size_t)r * 128;
             const int j0 = (c % PB) * EB / 16;
-            if (KIND == CONV_TOKMIX) {
-                BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
-                BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    *reinterpret_cast<float4*>(box + (((j0 + q) ^ (r & 7)) << 4)) =
-                        make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
-            }
+            BfVec<8>::store(reinterpret_cast<bf16*>(box + ((j0 ^ (r & 7)) << 4)), a);
+            BfVec<8>::store(reinterpret_cast<bf16*>(box + (((j0 + 1) ^ (r & 7)) << 4)), a + 8);
         }
         tc::fence_async_shared();
         __syncthreads();
