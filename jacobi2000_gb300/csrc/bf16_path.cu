@@ -962,10 +962,31 @@ __device__ __forceinline__ float tree32(float* a) {
 // rows in flight per warp. Rows [0, nrows) of the tile (a multiple of G),
 // tile row r -> global row m0 + r. SPL = slots per lane (1: D <= 128, 2: 256).
 // PRE: load every row group's residual rows up front (four groups at most).
+// A warp's residual rows for rows_resid_ln_t at D = 128 (lane l's slot of
+// each of its up to 16 rows), loaded ahead of the epilogue by load_xrows so
+// the loads overlap an MMA wait.
+struct XRows {
+    float4 v[4][4];
+};
+__device__ __forceinline__ void load_xrows(const float* __restrict__ x, int m0, int R, int warp, int nwarps,
+                                           int nrows, XRows& xr) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int r0 = warp * 4 + i * nwarps * 4;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int row = m0 + r0 + k;
+            xr.v[i][k] = r0 < nrows && row < R ? reinterpret_cast<const float4*>(x + (size_t)row * 128)[lane]
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
 template <int SPL, bool FULL, bool PRE = false, bool LNS = false>  // FULL: every lane owns SPL slots (D = 128 SPL)
-__device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
+__device__ __forceinline__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const float* __restrict__ bias,
                                 float* __restrict__ x, const float* __restrict__ g, const float* __restrict__ b,
-                                bf16* __restrict__ ln, int warp, int nwarps, int nrows) {
+                                bf16* __restrict__ ln, int warp, int nwarps, int nrows, const XRows* xin = nullptr) {
     const int lane = threadIdx.x & 31;
     const int nq = D / 4;
     const int swz = D >= 128 ? 31 : nq - 1;  // slot_swz mask
@@ -985,7 +1006,12 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
     constexpr int PF = 4;
     float4 xpre[SPL == 1 && PRE ? PF : 1][G];
     const bool prefetched = PRE && SPL == 1 && nrows <= PF * nwarps * G;
-    if (SPL == 1 && prefetched) {
+    if (SPL == 1 && prefetched && xin) {
+#pragma unroll
+        for (int i = 0; i < PF; i++)
+#pragma unroll
+            for (int k = 0; k < G; k++) xpre[SPL == 1 && PRE ? i : 0][k] = xin->v[i][k];
+    } else if (SPL == 1 && prefetched) {
 #pragma unroll
         for (int i = 0; i < PF; i++) {
             const int r0 = warp * G + i * nwarps * G;
@@ -1072,14 +1098,15 @@ __device__ void rows_resid_ln_t(const float* tile, int D, int m0, int R, const f
 
 // LNS: `ln` is the shared-memory A tile of an MMA (D = 128 only).
 template <bool PRE = false, bool LNS = false>
-__device__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
-                                  const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128) {
+__device__ __forceinline__ void rows_resid_ln_any(const float* tile, int D, int m0, int R, const float* bias, float* x,
+                                  const float* g, const float* b, bf16* ln, int warp, int nwarps, int nrows = 128,
+                                  const XRows* xin = nullptr) {
     if (LNS) {
-        if (D == 128) rows_resid_ln_t<1, true, PRE, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+        if (D == 128) rows_resid_ln_t<1, true, PRE, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows, xin);
         return;
     }
     if (D == 256) rows_resid_ln_t<2, true>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
-    else if (D == 128) rows_resid_ln_t<1, true, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
+    else if (D == 128) rows_resid_ln_t<1, true, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows, xin);
     else if (D > 128) rows_resid_ln_t<2, false>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
     else rows_resid_ln_t<1, false, PRE>(tile, D, m0, R, bias, x, g, b, ln, warp, nwarps, nrows);
 }
@@ -1351,6 +1378,8 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
             }
         }
         __syncwarp();
+        XRows xr;  // the residual rows, loaded while P is computed
+        if (D == 128) load_xrows(x, m0, R, warp, kMlpSerialThreads / 32, 128, xr);
         const bool pok = __syncthreads_and(tc::mbar_wait(&bar_pm, 0, err, &failed) ? 1 : 0) != 0;
         tc::tc_fence_after();
         if (pok) {
@@ -1360,7 +1389,7 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
             stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
             __syncthreads();
             rows_resid_ln_any<true, true>(tile, D, m0, R, bp, x, g2, be2, reinterpret_cast<bf16*>(sA), warp,
-                                          kMlpSerialThreads / 32);
+                                          kMlpSerialThreads / 32, 128, &xr);
         }
         // the A tile written above is read by the MMAs (async proxy)
         tc::fence_async_shared();
@@ -1449,6 +1478,8 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
         }
         __syncwarp();
     }
+    XRows xr2;  // the residual rows (this CTA wrote them above, or an earlier kernel), loaded while the last O runs
+    if (D == 128) load_xrows(x, m0, R, warp, kMlpSerialThreads / 32, 128, xr2);
     if (ok) {  // the last O
         ok = __syncthreads_and(tc::mbar_wait(&bar_o, (nchunks - 1) & 1, err, &failed) ? 1 : 0) != 0;
         tc::tc_fence_after();
@@ -1458,7 +1489,8 @@ __global__ void __launch_bounds__(kMlpSerialThreads, 2) tc_mlp_serial_kernel(con
         float* tile = reinterpret_cast<float*>(smem);
         stage_rows(lane_addr(tO), quarter * 32 + lane, D, half * (D / 2), (half + 1) * (D / 2), tile);
         __syncthreads();
-        rows_resid_ln_any<true>(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpSerialThreads / 32);
+        rows_resid_ln_any<true>(tile, D, m0, R, b2, x, g, b, ln, warp, kMlpSerialThreads / 32, 128,
+                                D == 128 ? &xr2 : nullptr);
     }
     tc::tc_fence_before();
     __syncthreads();
