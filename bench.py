@@ -912,11 +912,12 @@ def main():
                   "device_buffers": {"p50_ms": statistics.median(r["p50_ms"] for r in runs),
                                      "p99_ms": statistics.median(r["p99_ms"] for r in runs),
                                      "iterations_per_step": statistics.mean(r["iterations"] for r in runs),
+                                     "wall_s": statistics.mean(r["wall_s"] for r in runs),
                                      "work_cell_ticks_per_s": wl.work(step_reqs) / (dev_s / args.steps)},
                   "pinned_host_buffers": {k: e2e_runs[-1][k] for k in ("cell_ticks_per_s_wall", "p50_ms",
-                                                                         "p99_ms", "wall_s")},
+                                                                         "p99_ms", "wall_s", "device_span_s")},
                   "pageable_host_buffers": {k: staged[k] for k in ("cell_ticks_per_s_wall", "p50_ms", "p99_ms",
-                                                                   "wall_s")},
+                                                                   "wall_s", "device_span_s")},
                   "rates": []}
         if not args.no_sweep:
             for r_ in C5_RATES:
