@@ -187,6 +187,15 @@ constexpr int kCellPlane = kHaloW * kHaloH * 16;
 
 __device__ __forceinline__ float bf2f(bf16 v) { return __bfloat162float(v); }
 
+// d0 = fma(a0, b0, d0), d1 = fma(a1, b1, d1) in one paired instruction
+// (fma.rn.f32x2: each lane rounds like fmaf).
+__device__ __forceinline__ void fma2_f32(float& d0, float& d1, float a0, float a1, float b0, float b1) {
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tmov.b64 d, {%0, %1};\n\t"
+        "fma.rn.f32x2 d, a, b, d;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "+f"(d0), "+f"(d1)
+        : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 // Token embedding and the first LayerNorm (cpu.rs:253-280, 289). Persistent
 // CTAs walk tiles of 64 token rows: the embed weights [pd][D] are staged in
 // shared memory once per CTA, and each tile's patches arrive as 16-byte
@@ -295,8 +304,13 @@ __global__ void __launch_bounds__(256, (CPL <= 4 ? 3 : 1)) bf_embed_kernel(Dims 
 #pragma unroll
                     for (int q = 0; q < 8; q++) {
                         const float pv = px == 0 ? p4[q].x : px == 1 ? p4[q].y : px == 2 ? p4[q].z : p4[q].w;
+                        if (CPL % 2 == 0) {
 #pragma unroll
-                        for (int c = 0; c < CPL; c++) v[q][c] = fmaf(pv, wv[c], v[q][c]);
+                            for (int c = 0; c < CPL; c += 2) fma2_f32(v[q][c], v[q][c + 1], pv, pv, wv[c], wv[c + 1]);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < CPL; c++) v[q][c] = fmaf(pv, wv[c], v[q][c]);
+                        }
                     }
                 }
             }
