@@ -27,6 +27,10 @@
 // Requests that arrive while a chunk runs are admitted at the next iteration,
 // while their instances fit the workspace and their buffers fit the device
 // memory budget; each request's state stays on the device until it is done.
+// A request is staged at submit when the budget has room (its buffers
+// reserved and its inputs copied on a separate copy stream while chunks
+// run), so that admitting it costs the next chunk an event wait, not the
+// copies.
 // A request's result does not depend on which other requests share its
 // launches (no kernel's arithmetic for one instance reads another's data),
 // nor on how its ticks are cut into chunks.
@@ -178,6 +182,10 @@ struct Request {
     float* d_vals = nullptr;    // reconstruct: [H+1][3][cells]
     uint8_t* d_known = nullptr; // reconstruct: [H+1][cells]
     float* d_meta = nullptr;
+    // staged at submit: its buffers reserved and its inputs copied on the
+    // server's copy stream, complete when `ready` is
+    bool reserved = false;
+    cudaEvent_t ready = nullptr;
     ProjSlot* d_slot = nullptr;
     double energy = 0, max_viol = 0;
     bool recon() const { return r.task == JC_TASK_RECONSTRUCT; }
@@ -210,6 +218,8 @@ class Server {
     Workspace ws_;
     cudaStream_t stream_ = nullptr;
     cudaStream_t wait_stream_ = nullptr;  // result copies of device-buffer requests in wait()
+    cudaStream_t copy_stream_ = nullptr;  // inputs of requests staged at submit
+    int unreserved_pending_ = 0;          // waiting requests without staged buffers
     InstDev* h_inst_ = nullptr;    // pinned mirror of the descriptor array
     ReconDev* h_recon_ = nullptr;  // pinned mirror of the reconstruct bookkeeping
     ReconDev* d_recon_ = nullptr;
@@ -242,7 +252,7 @@ class Server {
     int chunk_length(const std::vector<Request*>& act, long long head_cells, int head_inst) const;
     void iteration(std::vector<Request*>& act, int K);
     void admit_locked();
-    void allocate(Request& q);
+    void allocate(Request& q, cudaStream_t st);
     void release(Request& q);
     void release_on(Request& q, cudaStream_t st);
     void fail_locked(Request& q, int status, const std::string& msg);
@@ -288,6 +298,7 @@ Server::Server(jc_model* const* fwd, jc_model* const* rev, int n_grids, long lon
     max_recon_ = max_inst_ / 2 + 1;
     cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     cuda_check(cudaStreamCreateWithFlags(&wait_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     for (cudaEvent_t* e : {&ev_first_, &ev_a_, &ev_b_}) cuda_check(cudaEventCreate(e), "cudaEventCreate");
     const int pp = dims_.P * dims_.P;
     ws_.alloc(arena_, dims_, (int)(max_cells_ / pp) + 1, max_cells_, max_inst_, fwd_[0]->w.bf16.get());
@@ -317,6 +328,10 @@ Server::~Server() {
     if (wait_stream_) {
         cudaStreamSynchronize(wait_stream_);
         cudaStreamDestroy(wait_stream_);
+    }
+    if (copy_stream_) {
+        cudaStreamSynchronize(copy_stream_);
+        cudaStreamDestroy(copy_stream_);
     }
     for (cudaEvent_t e : {ev_first_, ev_a_, ev_b_})
         if (e) cudaEventDestroy(e);
@@ -376,7 +391,36 @@ uint64_t Server::submit(const jc_request& r) {
     q.r.known = nullptr;
     q.r.meta = nullptr;
     if (q.bytes > budget_bytes_) throw Error(JC_OVER_BUDGET, "this request alone exceeds the device memory budget");
+    // Stage now, while earlier chunks run: reserve the request's device
+    // memory and copy its inputs on the copy stream, so that its admission
+    // does not put those copies in front of the next chunk's kernels.
+    // Only while no earlier request waits unstaged (memory is reserved in
+    // arrival order) and the budget has room; else it is staged at admission.
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (unreserved_pending_ == 0 && used_bytes_ + q.bytes <= budget_bytes_) {
+            used_bytes_ += q.bytes;
+            q.reserved = true;
+        }
+    }
+    long long staged_launches = 0;  // kernels launched here (reconstruct: the volume fill)
+    if (q.reserved) {
+        try {
+            const long long l0 = g_launches;
+            allocate(q, copy_stream_);
+            staged_launches = g_launches - l0;
+            cuda_check(cudaEventCreateWithFlags(&q.ready, cudaEventDisableTiming), "cudaEventCreate");
+            cuda_check(cudaEventRecord(q.ready, copy_stream_), "cudaEventRecord");
+        } catch (...) {
+            release_on(q, copy_stream_);
+            std::lock_guard<std::mutex> lk(mu_);
+            used_bytes_ -= q.bytes;
+            throw;
+        }
+    }
     std::lock_guard<std::mutex> lk(mu_);
+    launches_ += staged_launches;
+    if (!q.reserved) unreserved_pending_++;
     q.id = next_id_++;
     q.t_submit = now_s();
     if (first_submit_ == 0) first_submit_ = q.t_submit;
@@ -484,11 +528,11 @@ void Server::fail_locked(Request& q, int status, const std::string& msg) {
     q.t_done = now_s();
 }
 
-void Server::allocate(Request& q) {
+void Server::allocate(Request& q, cudaStream_t st) {
     const size_t len = 3 * q.cells;
     auto get = [&](size_t bytes) {
         void* p = nullptr;
-        cuda_check(cudaMallocAsync(&p, bytes, stream_), "cudaMallocAsync", JC_OVER_BUDGET);
+        cuda_check(cudaMallocAsync(&p, bytes, st), "cudaMallocAsync", JC_OVER_BUDGET);
         return p;
     };
     // caller-owned buffers: device or page-locked host memory (unified addressing tells which)
@@ -496,7 +540,7 @@ void Server::allocate(Request& q) {
     q.d_meta = static_cast<float*>(get(64 * 4));
     q.d_slot = static_cast<ProjSlot*>(get(sizeof(ProjSlot)));
     cuda_check(cudaMemcpyAsync(q.d_meta, q.device_io ? q.dev_meta : q.meta.as<float>(), dims_.meta_dim * 4, in_kind,
-                               stream_),
+                               st),
                "meta", JC_MAP);
     if (q.recon()) {
         const size_t H = (size_t)q.r.ticks;
@@ -505,18 +549,18 @@ void Server::allocate(Request& q) {
         q.d_F = static_cast<float*>(get(H * len * 4));
         q.d_R = static_cast<float*>(get(H * len * 4));
         q.d_known = static_cast<uint8_t*>(get((H + 1) * q.cells));
-        cuda_check(cudaMemcpyAsync(q.d_vals, q.device_io ? q.dev_x : q.x.as<float>(), (H + 1) * len * 4, in_kind, stream_),
+        cuda_check(cudaMemcpyAsync(q.d_vals, q.device_io ? q.dev_x : q.x.as<float>(), (H + 1) * len * 4, in_kind, st),
                    "reconstruct values", JC_MAP);
         cuda_check(cudaMemcpyAsync(q.d_known, q.device_io ? q.dev_known : q.known.as<uint8_t>(), (H + 1) * q.cells, in_kind,
-                                   stream_),
+                                   st),
                    "reconstruct mask", JC_MAP);
-        KScope k("recon_fill", stream_);
-        recon_fill_kernel<<<(unsigned)std::min<size_t>((H + 1) * ((q.cells + 255) / 256), 4096), 256, 0, stream_>>>(
+        KScope k("recon_fill", st);
+        recon_fill_kernel<<<(unsigned)std::min<size_t>((H + 1) * ((q.cells + 255) / 256), 4096), 256, 0, st>>>(
             q.d_state, q.d_vals, q.d_known, (int)H, (long long)q.cells);
         cuda_check(cudaGetLastError(), "reconstruct fill");
     } else {
         q.d_state = static_cast<float*>(get(len * 4));
-        cuda_check(cudaMemcpyAsync(q.d_state, q.device_io ? q.dev_x : q.x.as<float>(), len * 4, in_kind, stream_), "state",
+        cuda_check(cudaMemcpyAsync(q.d_state, q.device_io ? q.dev_x : q.x.as<float>(), len * 4, in_kind, st), "state",
                    JC_MAP);
     }
 }
@@ -524,9 +568,13 @@ void Server::allocate(Request& q) {
 void Server::release(Request& q) { release_on(q, stream_); }
 
 void Server::release_on(Request& q, cudaStream_t st) {
+    // buffers staged at submit: the frees follow the staging copies
+    if (q.ready) cudaStreamWaitEvent(st, q.ready, 0);
     for (void* p : {(void*)q.d_state, (void*)q.d_F, (void*)q.d_R, (void*)q.d_vals, (void*)q.d_known,
                     (void*)q.d_meta, (void*)q.d_slot})
         if (p) cudaFreeAsync(p, st);
+    if (q.ready) cudaEventDestroy(q.ready);
+    q.ready = nullptr;
     q.d_state = q.d_F = q.d_R = q.d_vals = nullptr;
     q.d_known = nullptr;
     q.d_meta = nullptr;
@@ -543,12 +591,16 @@ void Server::admit_locked() {
     }
     while (!pending_.empty()) {
         Request& q = reqs_[pending_.front()];
-        if (cells + q.inst_cells() > max_cells_ || inst + q.n_inst() > max_inst_ || used_bytes_ + q.bytes > budget_bytes_)
+        if (cells + q.inst_cells() > max_cells_ || inst + q.n_inst() > max_inst_ ||
+            (!q.reserved && used_bytes_ + q.bytes > budget_bytes_))
             break;  // first in, first admitted: later requests wait behind it
         pending_.pop_front();
         cells += q.inst_cells();
         inst += q.n_inst();
-        used_bytes_ += q.bytes;
+        if (!q.reserved) {
+            used_bytes_ += q.bytes;
+            unreserved_pending_--;
+        }
         q.admitted = true;
         q.fresh = true;
         q.t_admit = now_s();
@@ -717,8 +769,11 @@ struct GroupPlan {
 void Server::iteration(std::vector<Request*>& act, int K) {
     cudaStream_t s = stream_;
     // new requests: buffers and inputs on the device
-    for (Request* q : act)
-        if (q->fresh && !q->d_state) allocate(*q);
+    for (Request* q : act) {
+        if (!q->fresh) continue;
+        if (q->ready) cuda_check(cudaStreamWaitEvent(s, q->ready, 0), "cudaStreamWaitEvent");  // staged at submit
+        else if (!q->d_state) allocate(*q, s);
+    }
     auto base_inst = [&](const Model& m) {
         InstDev d{};
         d.tx = m.cfg.nx / m.cfg.patch;
