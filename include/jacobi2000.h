@@ -205,11 +205,12 @@ enum { JC_TASK_FORWARD = 0, JC_TASK_REWIND = 1, JC_TASK_RECONSTRUCT = 2 };
 /* Request flag: x, known and meta are caller-owned buffers that stay valid
  * until the request is done, and so is jc_server_wait's `out`: device memory,
  * or page-locked host memory (cudaMallocHost / cudaHostRegister), which the
- * copies then read or write by DMA. The result stays in the server's device
- * memory (counted against its budget) until jc_server_wait copies it out.
- * Without it, inputs and results are host memory of any kind: jc_server_submit
- * copies the inputs into the server's page-locked staging buffers, and the
- * result comes back through them. */
+ * copies then read or write by DMA. Without it, inputs and results are host
+ * memory of any kind: jc_server_submit copies the inputs into the server's
+ * page-locked staging buffers, and the result comes back through them. Either
+ * way a finished request's result stays in the server's device memory (counted
+ * against its budget) until jc_server_wait copies it out, so requests that are
+ * never collected keep their memory. */
 #define JC_REQUEST_DEVICE_BUFFERS 0x100u
 
 typedef struct {

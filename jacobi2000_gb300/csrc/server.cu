@@ -26,7 +26,8 @@
 // kChunkTargetS of device time when nothing waits.
 // Requests that arrive while a chunk runs are admitted at the next iteration,
 // while their instances fit the workspace and their buffers fit the device
-// memory budget; each request's state stays on the device until it is done.
+// memory budget; each request's state stays on the device until jc_server_wait
+// has copied its result out.
 // A request is staged at submit when the budget has room (its buffers
 // reserved and its inputs copied on a separate copy stream while chunks
 // run), so that admitting it costs the next chunk an event wait, not the
@@ -448,11 +449,10 @@ void Server::wait(uint64_t id, float* out, size_t out_len, jc_result* info, doub
     lk.unlock();
     if (q.status != JC_OK) throw Error((jc_status)q.status, q.error);
     const size_t n = q.out_floats();
-    struct Settle {  // device results: free the buffers and the budget even on errors
+    struct Settle {  // free the result's buffers and its budget, even on errors
         Server* s;
         Request* q;
         ~Settle() {
-            if (!q->device_io) return;
             s->release_on(*q, s->wait_stream_);
             cudaStreamSynchronize(s->wait_stream_);
             {
@@ -471,6 +471,10 @@ void Server::wait(uint64_t id, float* out, size_t out_len, jc_result* info, doub
             cuda_check(cudaStreamSynchronize(wait_stream_), "cudaStreamSynchronize", JC_POLL);
         }
     } else if (out) {
+        // host result: device -> the server's page-locked staging buffer -> `out`
+        q.out = PinnedBuf(pinned_, n * 4);
+        cuda_check(cudaMemcpyAsync(q.out.p, q.d_state, n * 4, cudaMemcpyDeviceToHost, wait_stream_), "D2H", JC_MAP);
+        cuda_check(cudaStreamSynchronize(wait_stream_), "cudaStreamSynchronize", JC_POLL);
         std::memcpy(out, q.out.p, n * 4);
     }
     if (info) {
@@ -709,7 +713,7 @@ void Server::loop() {
                 completed_++;
                 cell_ticks_ += (double)q->cells * q->r.ticks;
                 last_done_ = q->t_done;
-                if (!q->device_io) used_bytes_ -= q->bytes;  // device results free their memory in wait()
+                // the result's memory is freed (and its budget returned) in wait()
             } else {
                 still.push_back(q->id);
             }
@@ -935,11 +939,6 @@ void Server::iteration(std::vector<Request*>& act, int K) {
     std::vector<Request*> finishing;
     for (Request* q : act) {
         if (q->recon() || q->remaining() > K) continue;
-        if (!q->device_io) {
-            q->out = PinnedBuf(pinned_, 3 * q->cells * 4);
-            cuda_check(cudaMemcpyAsync(q->out.p, q->d_state, 3 * q->cells * 4, cudaMemcpyDeviceToHost, s), "D2H",
-                       JC_MAP);
-        }
         cuda_check(cudaMemcpyAsync(&h_slots_[finishing.size()], q->d_slot, sizeof(ProjSlot), cudaMemcpyDeviceToHost, s),
                    "D2H", JC_MAP);
         finishing.push_back(q);
@@ -971,8 +970,7 @@ void Server::iteration(std::vector<Request*>& act, int K) {
         if (q->recon()) continue;
         const int rem = q->remaining();
         q->ticks_done += std::min(rem, K);
-        if (q->ticks_done == q->r.ticks) {
-            if (!q->device_io) release(*q);
+        if (q->ticks_done == q->r.ticks) {  // the result stays on the device until wait()
             q->finished = true;
             q->t_done = t;
         }
@@ -983,23 +981,11 @@ void Server::iteration(std::vector<Request*>& act, int K) {
         q->sweeps = h_recon_[i].sweeps;
         q->frozen = h_recon_[i].frozen;
         q->residual = h_recon_[i].last_resid;
-        if (q->frozen) {
-            if (!q->device_io) {
-                q->out = PinnedBuf(pinned_, q->out_floats() * 4);
-                cuda_check(cudaMemcpyAsync(q->out.p, q->d_state, q->out_floats() * 4, cudaMemcpyDeviceToHost, s),
-                           "D2H", JC_MAP);
-            }
-            recon_done.push_back(q);
-        }
+        if (q->frozen) recon_done.push_back(q);
     }
-    if (!recon_done.empty()) {
-        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize", JC_POLL);
-        const double t2 = now_s();
-        for (Request* q : recon_done) {
-            if (!q->device_io) release(*q);
-            q->finished = true;
-            q->t_done = t2;
-        }
+    for (Request* q : recon_done) {  // the volume stays on the device until wait()
+        q->finished = true;
+        q->t_done = t;
     }
 }
 
