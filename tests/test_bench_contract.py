@@ -77,3 +77,19 @@ def test_two_ranks_take_the_slowest_step_and_count_every_rank():
         assert p.exitcode == 0
     # both ranks see the slowest rank's 15 ms; 2 x 1000 units in 15 ms
     assert got == [(0, 15.0, 2000.0 / 0.015), (1, 15.0, 2000.0 / 0.015)]
+
+
+def test_profiled_kernel_names_are_known_to_the_roofline():
+    """Every kernel of the committed ncu traffic table has algorithmic work in
+    the bench (so the roofline's `traffic` is found for it), and the per-layer
+    kernels count once per layer."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    traffic = bench.ncu_traffic()
+    assert {"tc_proj_mlp", "bf_attention", "tc_qkv", "tc_conv1", "tc_conv2"} <= set(traffic)
+    for name, nbytes in traffic.items():
+        kind, amount = bench.kernel_work(name, 64, 128 * 128, 128, 512)
+        assert kind in ("flop", "byte") and amount > 0, name
+        assert nbytes > 0
+    assert {"tc_qkv", "bf_attention", "tc_proj_mlp"} <= set(bench.PER_LAYER)
