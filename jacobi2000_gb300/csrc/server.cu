@@ -966,6 +966,11 @@ void Server::iteration(std::vector<Request*>& act, int K) {
         q->max_viol = h_slots_[i].max_viol;
     }
     for (Request* q : act) {
+        if (q->fresh) {  // its inputs are on the device (the chunk above waited for them): back to the pool
+            q->x.reset();
+            q->known.reset();
+            q->meta.reset();
+        }
         q->fresh = false;
         if (q->recon()) continue;
         const int rem = q->remaining();
