@@ -2664,8 +2664,9 @@ void BF16Path::alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows,
     p.tmaps = a.alloc((size_t)max_inst * kMapsPerInst * sizeof(CUtensorMap));
 }
 
-void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s) const {
-    std::vector<CUtensorMap> maps((size_t)p.n_inst * kMapsPerInst);
+void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s, CUtensorMap* hstage) const {
+    std::vector<CUtensorMap> tmp(hstage ? 0 : (size_t)p.n_inst * kMapsPerInst);
+    CUtensorMap* maps = hstage ? hstage : tmp.data();
     for (int i = 0; i < p.n_inst; i++) {
         const InstDev& I = hinst[i];
         CUtensorMap* m = &maps[(size_t)kMapsPerInst * i];
@@ -2679,10 +2680,11 @@ void BF16Path::prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaS
             m[5] = att_map(p.bt[1] + (size_t)I.row0 * p.bt_stride[1], d.D, I.tx, I.ty, kAttTile);
         }
     }
-    // synchronous: the host vector is released on return
-    cuda_check(cudaMemcpyAsync(p.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s),
+    cuda_check(cudaMemcpyAsync(p.tmaps, maps, (size_t)p.n_inst * kMapsPerInst * sizeof(CUtensorMap),
+                               cudaMemcpyHostToDevice, s),
                "tensor maps", JC_MAP);
-    cuda_check(cudaStreamSynchronize(s), "tensor maps", JC_POLL);
+    // a temporary host array is released on return: wait for the copy
+    if (!hstage) cuda_check(cudaStreamSynchronize(s), "tensor maps", JC_POLL);
 }
 
 void BF16Path::forward(const Dims& d, const WeightsF32& w, const Pack& p, int mode, cudaStream_t s) const {

@@ -41,7 +41,11 @@ class BF16Path {
     void alloc_workspace(DeviceArena& a, const Dims& d, Pack& p, int rows, long long cells, int max_inst) const;
     // Encodes and uploads the per-instance tensor maps of a pack view whose
     // host-side descriptors are `hinst` (same order as the device array).
-    void prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s) const;
+    // With `hstage` (page-locked, room for the view's maps, not reused until
+    // the copy has run) the maps are encoded there and copied asynchronously;
+    // without, through a temporary host array and a stream synchronisation.
+    void prepare(const Dims& d, const Pack& p, const InstDev* hinst, cudaStream_t s,
+                 CUtensorMap* hstage = nullptr) const;
     void forward(const Dims& d, const WeightsF32& w32, const Pack& p, int mode, cudaStream_t s) const;
     // Picks the schedule for p's row count (timing the candidates on p's own
     // workspace) unless it is known or autotuning is off. Never call while

@@ -222,6 +222,7 @@ class Server {
     cudaStream_t copy_stream_ = nullptr;  // inputs of requests staged at submit
     int unreserved_pending_ = 0;          // waiting requests without staged buffers
     InstDev* h_inst_ = nullptr;    // pinned mirror of the descriptor array
+    CUtensorMap* h_maps_ = nullptr;  // pinned staging of the tensor maps (BF16), kMapsPerInst per instance
     ReconDev* h_recon_ = nullptr;  // pinned mirror of the reconstruct bookkeeping
     ReconDev* d_recon_ = nullptr;
     ProjSlot* h_slots_ = nullptr;  // pinned: slots of the requests finishing in a chunk
@@ -305,6 +306,9 @@ Server::Server(jc_model* const* fwd, jc_model* const* rev, int n_grids, long lon
     ws_.alloc(arena_, dims_, (int)(max_cells_ / pp) + 1, max_cells_, max_inst_, fwd_[0]->w.bf16.get());
     d_recon_ = arena_.alloc_n<ReconDev>(max_recon_);
     cuda_check(cudaMallocHost(&h_inst_, (size_t)max_inst_ * sizeof(InstDev)), "cudaMallocHost", JC_OVER_BUDGET);
+    if (precision_ == JC_BF16)
+        cuda_check(cudaMallocHost(&h_maps_, (size_t)max_inst_ * kMapsPerInst * sizeof(CUtensorMap)), "cudaMallocHost",
+                   JC_OVER_BUDGET);
     cuda_check(cudaMallocHost(&h_recon_, (size_t)max_recon_ * sizeof(ReconDev)), "cudaMallocHost", JC_OVER_BUDGET);
     cuda_check(cudaMallocHost(&h_slots_, (size_t)max_inst_ * sizeof(ProjSlot)), "cudaMallocHost", JC_OVER_BUDGET);
     size_t free_b = 0, total_b = 0;
@@ -337,6 +341,7 @@ Server::~Server() {
     for (cudaEvent_t e : {ev_first_, ev_a_, ev_b_})
         if (e) cudaEventDestroy(e);
     if (h_inst_) cudaFreeHost(h_inst_);
+    if (h_maps_) cudaFreeHost(h_maps_);
     if (h_recon_) cudaFreeHost(h_recon_);
     if (h_slots_) cudaFreeHost(h_slots_);
 }
@@ -876,12 +881,12 @@ void Server::iteration(std::vector<Request*>& act, int K) {
     if (bf) {
         if (!fg.inst.empty()) {
             Pack v = fg.view(ws_, dims_, (int)fg.inst.size());
-            bf->prepare(dims_, v, h_inst_ + fg.inst_base, s);
+            bf->prepare(dims_, v, h_inst_ + fg.inst_base, s, h_maps_ + (size_t)fg.inst_base * kMapsPerInst);
             bf->tune(dims_, fwd_[0]->w.f32, v, s);
         }
         if (!rg.inst.empty()) {
             Pack v = rg.view(ws_, dims_, (int)rg.inst.size());
-            bf->prepare(dims_, v, h_inst_ + rg.inst_base, s);
+            bf->prepare(dims_, v, h_inst_ + rg.inst_base, s, h_maps_ + (size_t)rg.inst_base * kMapsPerInst);
             rev_[0]->w.bf16->tune(dims_, rev_[0]->w.f32, v, s);
         }
     }
